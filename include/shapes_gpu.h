@@ -1,0 +1,204 @@
+/*
+ * shapes_gpu.h — C ABI of the GB300 world step for ublubu/shapes.
+ *
+ * This is the drop-in boundary for `Physics.Engine.Main`
+ * (shapes/src/Physics/Engine/Main.hs:32-98): a Haskell caller keeps its
+ * `EngineST` API and marshals world state through `foreign import ccall` into
+ * device-resident structure-of-arrays buffers owned by this library.  Every
+ * entry point is plain C: pointers, sizes, status codes.
+ *
+ * Conventions
+ *   - Every function returns an int status: SHAPES_OK (0) or a negative
+ *     SHAPES_E_* code.  Nothing aborts, exits or traps.
+ *   - Host pointers passed in are only read during the call (copied).
+ *     Out-buffers are caller-allocated; size them with the matching count
+ *     query first.
+ *   - A handle is single-threaded, like the reference's `ST` state thread.
+ *     Different handles may be used from different threads; each owns a CUDA
+ *     stream on the current device.
+ *   - Body indices in keys and pairs are world-local slot indices, exactly the
+ *     reference's World slot keys after `fromList` (World.hs:118-124).
+ *   - Limits: at most 2^20 bodies per world, 3..64 vertices per convex hull
+ *     (counter-clockwise, strictly convex), circles unsupported.
+ */
+#ifndef SHAPES_GPU_H
+#define SHAPES_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SHAPES_OK 0
+#define SHAPES_E_INVALID_ARG (-1)
+#define SHAPES_E_UNSUPPORTED (-2) /* circles, more than 64 vertices, custom External */
+#define SHAPES_E_NONCONVEX (-3)   /* hull not strictly convex and counter-clockwise */
+#define SHAPES_E_CAPACITY (-4)    /* internal buffer could not grow */
+#define SHAPES_E_CUDA (-5)        /* CUDA runtime error (no device, launch failure) */
+#define SHAPES_E_TIMEOUT (-6)     /* a bounded device wait gave up */
+#define SHAPES_E_NAN (-7)         /* non-finite body state passed in */
+#define SHAPES_E_BUFFER (-8)      /* caller's out-buffer too small */
+
+#define SHAPES_SHAPE_HULL 0
+#define SHAPES_SHAPE_CIRCLE 1
+
+/* External effects (World.hs:33 `type External`): the reference's closures
+ * cannot cross the FFI; the two the reference's scenes use are supported. */
+#define SHAPES_EXTERNAL_NONE 0           /* `const id` (Scenes/TwoFlyingBoxes.hs:30-31) */
+#define SHAPES_EXTERNAL_CONSTANT_ACCEL 1 /* constantAccel (World/External.hs:23-28) */
+
+#define SHAPES_WARM_START_OFF 0
+#define SHAPES_WARM_START_CACHE 1 /* applyCachedSlns (Solvers/Contact.hs:74-121) */
+
+/* Structure-of-arrays body state: PhysicalObj (Constraint.hs:52-57) plus
+ * Material (World.hs:35-38).  inv_mass_* are the stored InvMass2 fields, i.e.
+ * toInvMass2 (Constraint.hs:79-83) already applied: 0 means infinite mass. */
+typedef struct shapes_bodies {
+  double* vel_x;
+  double* vel_y;
+  double* rot_vel;
+  double* pos_x;
+  double* pos_y;
+  double* rot;
+  double* inv_mass_lin;
+  double* inv_mass_rot;
+  double* mu;
+  double* bounce;
+} shapes_bodies;
+
+/* EngineConfig (Engine/Main.hs:34-37) + ContactBehavior (Contact/Types.hs:20-25)
+ * + the External, plus the solver sweep count the reference hard-codes to 2
+ * (Engine/Main.hs:81-82). */
+typedef struct shapes_config {
+  double dt;
+  double baumgarte;
+  double slop;
+  double accel_x;
+  double accel_y;
+  int32_t iterations; /* improveWorld sweeps per step; 2 = reference */
+  int32_t warm_start; /* SHAPES_WARM_START_* */
+  int32_t external;   /* SHAPES_EXTERNAL_* */
+  int32_t reserved;   /* must be 0 */
+} shapes_config;
+
+/* Counters of the most recent step or collide call, summed over worlds. */
+typedef struct shapes_stats {
+  int64_t pairs;
+  int64_t contacts;
+  int64_t cache_hits;
+  int64_t solver_items;  /* warm-start applications + sweep updates */
+  int64_t solver_levels; /* sum over solver groups of dependency levels */
+  int64_t retries;       /* buffer regrowths during the last call */
+} shapes_stats;
+
+typedef struct shapes_batch shapes_batch;
+
+/* Build `n_worlds` independent worlds in one handle.
+ *   world_body_offsets[n_worlds+1]: bodies of world w are [off[w], off[w+1]).
+ *   bodies: SoA arrays of length off[n_worlds].
+ *   vert_offsets[n_bodies+1]: hull vertices of body b are
+ *     local_verts_xy[2*vert_offsets[b] .. 2*vert_offsets[b+1]).
+ *   shape_kind: per body SHAPES_SHAPE_*, or NULL for all hulls.
+ * Shapes are posed from the bodies' positions on creation (makeWorldObj,
+ * World.hs:142-149) and the contact cache starts empty (initEngine,
+ * Engine/Main.hs:43-46).
+ * Replaces: makeWorld/fromList (Engine.hs:41-42, World.hs:118-124), makeHull /
+ * makeRectangleHull + listToHull (Engine.hs:47-51, ConvexHull.hs:151-167),
+ * initEngine (Engine/Main.hs:43-46). */
+int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets,
+                        const shapes_bodies* bodies, const int32_t* vert_offsets,
+                        const double* local_verts_xy, const uint8_t* shape_kind,
+                        shapes_batch** out);
+
+/* Advance every world by `nsteps` world steps.
+ * Replaces: updateWorld (Engine/Main.hs:71-84) and stepWorld (Engine/Main.hs:88-89). */
+int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps);
+
+/* Broadphase + contact generation on the current poses only (no forces, no
+ * solve); results readable with the pair/contact getters.
+ * Replaces: G.culledKeys . G.toGrid (Engine/Main.hs:75) followed by
+ * prepareFrame (Solvers/Contact.hs:40-52), as the demo's worldContacts query
+ * does (shapes-demo/src/Physics/Demo/IOWorld.hs:74-81). */
+int shapes_batch_collide(shapes_batch* b);
+
+/* Body state read/write.  set re-poses the shapes and keeps the cache.
+ * Replaces: readPhysObj / updatePhysObj (World.hs:93-97). */
+int shapes_batch_get_bodies(shapes_batch* b, shapes_bodies* out);
+int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in);
+
+/* Counts of the handle. */
+int shapes_batch_num_worlds(shapes_batch* b, int32_t* out);
+int shapes_batch_num_bodies(shapes_batch* b, int64_t* out);
+int shapes_batch_num_vertices(shapes_batch* b, int64_t* out);
+
+/* World-space hull vertices and unit edge normals of the current pose, in
+ * vertex order (2 doubles each).  Replaces: reading _hullVertices /
+ * _hullEdgeNormals of the posed Shape (ConvexHull.hs:61-68, World.hs:111-112). */
+int shapes_batch_get_shapes(shapes_batch* b, double* world_xy, double* normal_xy);
+
+/* Broadphase pairs of the last step/collide, descending (i, j), i > j,
+ * world-local indices, worlds in order; world_counts[n_worlds] may be NULL.
+ * Replaces: the Descending (Int, Int) keys of Aabb.culledKeys / Grid.culledKeys
+ * (Aabb.hs:168-183, Grid.hs:257-261). */
+int shapes_batch_num_pairs(shapes_batch* b, int64_t* out);
+int shapes_batch_get_pairs(shapes_batch* b, int32_t* ij, int64_t capacity, int32_t* world_counts);
+
+/* Contacts of the last step/collide in descending key order:
+ * keys5 = (i, j, feature_i, feature_j, flip), vals5 = (normal x, normal y,
+ * point x, point y, depth).
+ * Replaces: the Descending (ObjectFeatureKey Int, Flipping Contact) of
+ * prepareFrame (Solvers/Contact.hs:40-52, Constraints/Contact.hs:49-57). */
+int shapes_batch_num_contacts(shapes_batch* b, int64_t* out);
+int shapes_batch_get_contacts(shapes_batch* b, int32_t* keys5, double* vals5, int64_t capacity,
+                              int32_t* world_counts);
+
+/* Contact-solution cache: keys4 = (i, j, feature_i, feature_j), lam2 =
+ * (normal, friction) Lagrangians, per world in descending key order.
+ * set replaces the whole cache (checkpoint/resume); keys must be strictly
+ * descending within each world.
+ * Replaces: EngineCache (Engine/Main.hs:32) carried in EngineState. */
+int shapes_batch_num_cache(shapes_batch* b, int64_t* out);
+int shapes_batch_get_cache(shapes_batch* b, int32_t* keys4, double* lam2, int64_t capacity,
+                           int32_t* world_counts);
+int shapes_batch_set_cache(shapes_batch* b, const int32_t* world_counts, const int32_t* keys4,
+                           const double* lam2);
+
+int shapes_batch_get_stats(shapes_batch* b, shapes_stats* out);
+
+/* Solver packing: worlds per solver CTA and CTA size.  0 = automatic. */
+int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads);
+
+/* Run this handle's device work on a caller-owned CUDA stream (a
+ * cudaStream_t passed as void*), e.g. a framework's current stream; NULL
+ * returns to the handle's own stream.  The stream must stay valid while set. */
+int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream);
+
+/* Per-stage device timing.  While enabled, CUDA events on the handle's stream
+ * bracket each stage of every step; get_profile returns the accumulated
+ * milliseconds and kernel launches per stage since profiling was enabled or
+ * last read (reading resets).  Stages, in order: broadphase, narrowphase,
+ * constraint build, solver schedule, solver, integrate+pose, scans/offsets. */
+#define SHAPES_STAGE_COUNT 7
+int shapes_batch_set_profiling(shapes_batch* b, int32_t enabled);
+int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches);
+
+void shapes_batch_destroy(shapes_batch* b);
+
+/* Single-world convenience wrappers over a batch of one world. */
+int shapes_world_create(int32_t n_bodies, const shapes_bodies* bodies, const int32_t* vert_offsets,
+                        const double* local_verts_xy, const uint8_t* shape_kind,
+                        shapes_batch** out);
+
+/* Human-readable text for a status code (static storage). */
+const char* shapes_strerror(int status);
+
+/* Text of the last CUDA error seen by any handle on this thread (static
+ * storage, empty if none). */
+const char* shapes_last_error_detail(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHAPES_GPU_H */

@@ -1,0 +1,270 @@
+"""ctypes binding of the C ABI in include/shapes_gpu.h (libshapes_gpu.so).
+
+The library is built in-tree by ``shapes_gb300.build`` into
+``shapes_gb300/_build/libshapes_gpu.so``.  Loading fails loudly when it is
+missing: there is no CPU implementation of the step behind this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "libshapes_gpu.so"
+
+SHAPES_OK = 0
+SHAPES_E_INVALID_ARG = -1
+SHAPES_E_UNSUPPORTED = -2
+SHAPES_E_NONCONVEX = -3
+SHAPES_E_CAPACITY = -4
+SHAPES_E_CUDA = -5
+SHAPES_E_TIMEOUT = -6
+SHAPES_E_NAN = -7
+SHAPES_E_BUFFER = -8
+
+SHAPES_EXTERNAL_NONE = 0
+SHAPES_EXTERNAL_CONSTANT_ACCEL = 1
+SHAPES_WARM_START_OFF = 0
+SHAPES_WARM_START_CACHE = 1
+
+STAGE_NAMES = ("broadphase", "narrowphase", "build", "schedule", "solve", "integrate", "scan")
+STAGE_COUNT = len(STAGE_NAMES)
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_lp = ctypes.POINTER(ctypes.c_int64)
+_up = ctypes.POINTER(ctypes.c_uint8)
+
+
+class Bodies(ctypes.Structure):
+    """shapes_bodies: ten SoA double arrays."""
+
+    _fields_ = [(name, _dp) for name in (
+        "vel_x", "vel_y", "rot_vel", "pos_x", "pos_y", "rot",
+        "inv_mass_lin", "inv_mass_rot", "mu", "bounce")]
+
+
+BODY_FIELDS = [f[0] for f in Bodies._fields_]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("baumgarte", ctypes.c_double),
+        ("slop", ctypes.c_double),
+        ("accel_x", ctypes.c_double),
+        ("accel_y", ctypes.c_double),
+        ("iterations", ctypes.c_int32),
+        ("warm_start", ctypes.c_int32),
+        ("external", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "pairs", "contacts", "cache_hits", "solver_items", "solver_levels", "retries")]
+
+
+class ShapesError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        detail = ""
+        try:
+            detail = lib().shapes_last_error_detail().decode()
+        except Exception:  # pragma: no cover - best effort
+            pass
+        msg = f"{where}: {lib().shapes_strerror(status).decode()} ({status})"
+        if detail:
+            msg += f" [{detail}]"
+        super().__init__(msg)
+
+
+_LIB = None
+
+# (name, restype, argtypes) for every symbol the header declares.
+SIGNATURES = [
+    ("shapes_batch_create", ctypes.c_int, [ctypes.c_int32, _ip, ctypes.POINTER(Bodies), _ip, _dp, _up,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    ("shapes_batch_step", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Config), ctypes.c_int32]),
+    ("shapes_batch_collide", ctypes.c_int, [ctypes.c_void_p]),
+    ("shapes_batch_get_bodies", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Bodies)]),
+    ("shapes_batch_set_bodies", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Bodies)]),
+    ("shapes_batch_num_worlds", ctypes.c_int, [ctypes.c_void_p, _ip]),
+    ("shapes_batch_num_bodies", ctypes.c_int, [ctypes.c_void_p, _lp]),
+    ("shapes_batch_num_vertices", ctypes.c_int, [ctypes.c_void_p, _lp]),
+    ("shapes_batch_get_shapes", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    ("shapes_batch_num_pairs", ctypes.c_int, [ctypes.c_void_p, _lp]),
+    ("shapes_batch_get_pairs", ctypes.c_int, [ctypes.c_void_p, _ip, ctypes.c_int64, _ip]),
+    ("shapes_batch_num_contacts", ctypes.c_int, [ctypes.c_void_p, _lp]),
+    ("shapes_batch_get_contacts", ctypes.c_int, [ctypes.c_void_p, _ip, _dp, ctypes.c_int64, _ip]),
+    ("shapes_batch_num_cache", ctypes.c_int, [ctypes.c_void_p, _lp]),
+    ("shapes_batch_get_cache", ctypes.c_int, [ctypes.c_void_p, _ip, _dp, ctypes.c_int64, _ip]),
+    ("shapes_batch_set_cache", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _dp]),
+    ("shapes_batch_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    ("shapes_batch_set_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    ("shapes_batch_set_stream", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("shapes_batch_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_get_profile", ctypes.c_int, [ctypes.c_void_p, _dp, _lp]),
+    ("shapes_batch_destroy", None, [ctypes.c_void_p]),
+    ("shapes_world_create", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(Bodies), _ip, _dp, _up,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
+    ("shapes_last_error_detail", ctypes.c_char_p, []),
+]
+
+
+def lib() -> ctypes.CDLL:
+    """Load libshapes_gpu.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        path = os.environ.get("SHAPES_GPU_LIB", str(LIB_PATH))
+        if not Path(path).exists():
+            raise RuntimeError(
+                f"{path} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+                " (the step has no CPU fallback)")
+        handle = ctypes.CDLL(path)
+        for name, restype, argtypes in SIGNATURES:
+            fn = getattr(handle, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        _LIB = handle
+    return _LIB
+
+
+def check(status: int, where: str) -> None:
+    if status != SHAPES_OK:
+        raise ShapesError(status, where)
+
+
+def _ptr(a: np.ndarray, kind):
+    return a.ctypes.data_as(kind)
+
+
+def make_bodies(arrays: dict) -> tuple[Bodies, list]:
+    """Bodies struct over contiguous float64 arrays; returns (struct, keepalive)."""
+    keep = [np.ascontiguousarray(arrays[f], dtype=np.float64) for f in BODY_FIELDS]
+    b = Bodies(*[_ptr(a, _dp) for a in keep])
+    return b, keep
+
+
+class Batch:
+    """A handle over many independent worlds on the current CUDA device."""
+
+    def __init__(self, world_body_offsets, bodies: dict, vert_offsets, local_verts_xy, shape_kind=None):
+        L = lib()
+        self._off = np.ascontiguousarray(world_body_offsets, dtype=np.int32)
+        self._vo = np.ascontiguousarray(vert_offsets, dtype=np.int32)
+        self._xy = np.ascontiguousarray(local_verts_xy, dtype=np.float64).reshape(-1)
+        sk = None if shape_kind is None else np.ascontiguousarray(shape_kind, dtype=np.uint8)
+        b, keep = make_bodies(bodies)
+        h = ctypes.c_void_p()
+        st = L.shapes_batch_create(len(self._off) - 1, _ptr(self._off, _ip), ctypes.byref(b), _ptr(self._vo, _ip),
+                                   _ptr(self._xy, _dp), None if sk is None else _ptr(sk, _up), ctypes.byref(h))
+        check(st, "shapes_batch_create")
+        self._h = h
+        self.n_worlds = len(self._off) - 1
+        self.n_bodies = int(self._off[-1])
+        self.n_verts = int(self._vo[-1])
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().shapes_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def step(self, cfg: Config, nsteps: int = 1) -> None:
+        check(lib().shapes_batch_step(self._h, ctypes.byref(cfg), nsteps), "shapes_batch_step")
+
+    def collide(self) -> None:
+        check(lib().shapes_batch_collide(self._h), "shapes_batch_collide")
+
+    def get_bodies(self) -> dict:
+        out = {f: np.empty(self.n_bodies, dtype=np.float64) for f in BODY_FIELDS}
+        b, _ = make_bodies(out)
+        check(lib().shapes_batch_get_bodies(self._h, ctypes.byref(b)), "shapes_batch_get_bodies")
+        return out
+
+    def set_bodies(self, bodies: dict) -> None:
+        b, keep = make_bodies(bodies)
+        check(lib().shapes_batch_set_bodies(self._h, ctypes.byref(b)), "shapes_batch_set_bodies")
+
+    def get_shapes(self) -> tuple[np.ndarray, np.ndarray]:
+        xy = np.empty(2 * self.n_verts, dtype=np.float64)
+        nxy = np.empty(2 * self.n_verts, dtype=np.float64)
+        check(lib().shapes_batch_get_shapes(self._h, _ptr(xy, _dp), _ptr(nxy, _dp)), "shapes_batch_get_shapes")
+        return xy.reshape(-1, 2), nxy.reshape(-1, 2)
+
+    def get_pairs(self) -> tuple[np.ndarray, np.ndarray]:
+        n = ctypes.c_int64()
+        check(lib().shapes_batch_num_pairs(self._h, ctypes.byref(n)), "shapes_batch_num_pairs")
+        ij = np.empty(2 * max(n.value, 1), dtype=np.int32)
+        wc = np.empty(self.n_worlds, dtype=np.int32)
+        check(lib().shapes_batch_get_pairs(self._h, _ptr(ij, _ip), n.value, _ptr(wc, _ip)), "shapes_batch_get_pairs")
+        return ij[: 2 * n.value].reshape(-1, 2), wc
+
+    def get_contacts(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = ctypes.c_int64()
+        check(lib().shapes_batch_num_contacts(self._h, ctypes.byref(n)), "shapes_batch_num_contacts")
+        k = np.empty(5 * max(n.value, 1), dtype=np.int32)
+        v = np.empty(5 * max(n.value, 1), dtype=np.float64)
+        wc = np.empty(self.n_worlds, dtype=np.int32)
+        check(lib().shapes_batch_get_contacts(self._h, _ptr(k, _ip), _ptr(v, _dp), n.value, _ptr(wc, _ip)),
+              "shapes_batch_get_contacts")
+        return k[: 5 * n.value].reshape(-1, 5), v[: 5 * n.value].reshape(-1, 5), wc
+
+    def get_cache(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = ctypes.c_int64()
+        check(lib().shapes_batch_num_cache(self._h, ctypes.byref(n)), "shapes_batch_num_cache")
+        k = np.empty(4 * max(n.value, 1), dtype=np.int32)
+        lam = np.empty(2 * max(n.value, 1), dtype=np.float64)
+        wc = np.empty(self.n_worlds, dtype=np.int32)
+        check(lib().shapes_batch_get_cache(self._h, _ptr(k, _ip), _ptr(lam, _dp), n.value, _ptr(wc, _ip)),
+              "shapes_batch_get_cache")
+        return k[: 4 * n.value].reshape(-1, 4), lam[: 2 * n.value].reshape(-1, 2), wc
+
+    def set_cache(self, keys4: np.ndarray, lam2: np.ndarray, world_counts: np.ndarray) -> None:
+        k = np.ascontiguousarray(keys4, dtype=np.int32).reshape(-1)
+        lam = np.ascontiguousarray(lam2, dtype=np.float64).reshape(-1)
+        wc = np.ascontiguousarray(world_counts, dtype=np.int32)
+        check(lib().shapes_batch_set_cache(self._h, _ptr(wc, _ip), _ptr(k, _ip), _ptr(lam, _dp)),
+              "shapes_batch_set_cache")
+
+    def stats(self) -> dict:
+        s = Stats()
+        check(lib().shapes_batch_get_stats(self._h, ctypes.byref(s)), "shapes_batch_get_stats")
+        return {f[0]: getattr(s, f[0]) for f in Stats._fields_}
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        check(lib().shapes_batch_set_stream(self._h, ctypes.c_void_p(cuda_stream or None)), "shapes_batch_set_stream")
+
+    def set_profiling(self, enabled: bool) -> None:
+        check(lib().shapes_batch_set_profiling(self._h, int(bool(enabled))), "shapes_batch_set_profiling")
+
+    def get_profile(self) -> dict:
+        ms = np.zeros(STAGE_COUNT, dtype=np.float64)
+        n = np.zeros(STAGE_COUNT, dtype=np.int64)
+        check(lib().shapes_batch_get_profile(self._h, _ptr(ms, _dp), _ptr(n, _lp)), "shapes_batch_get_profile")
+        return {name: (float(ms[k]), int(n[k])) for k, name in enumerate(STAGE_NAMES)}
+
+    def set_launch(self, target_bodies_per_group: int, threads: int) -> None:
+        check(lib().shapes_batch_set_launch(self._h, target_bodies_per_group, threads), "shapes_batch_set_launch")
+
+
+def make_config(dt: float, baumgarte: float = 0.01, slop: float = 0.02, accel=(0.0, -9.8),
+                iterations: int = 2, warm_start: bool = True, external: bool = True) -> Config:
+    return Config(dt, baumgarte, slop, float(accel[0]), float(accel[1]), int(iterations),
+                  SHAPES_WARM_START_CACHE if warm_start else SHAPES_WARM_START_OFF,
+                  SHAPES_EXTERNAL_CONSTANT_ACCEL if external else SHAPES_EXTERNAL_NONE, 0)

@@ -1,0 +1,940 @@
+/*
+ * Host runtime behind include/shapes_gpu.h: one handle = a batch of
+ * independent worlds resident on the device as structure-of-arrays, stepped by
+ * the kernels of step_kernels.cuh on the handle's own CUDA stream.
+ *
+ * Buffers whose size depends on the step (pairs, contacts, solver updates) are
+ * sized generously up front.  Kernels never write past a capacity: they raise a
+ * sticky overflow flag instead, and the host then restores the state saved at
+ * the start of the call, doubles the capacities and runs the call again, so a
+ * call either completes exactly or returns an error with the state untouched.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/shapes_gpu.h"
+#include "step_kernels.cuh"
+
+using shapes::Con;
+using shapes::Dev;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct CudaError {
+  cudaError_t err;
+};
+
+inline void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    throw CudaError{e};
+  }
+}
+
+constexpr int kSMs = 152;
+
+template <typename T>
+T* dalloc(size_t n, const char* what) {
+  void* p = nullptr;
+  ck(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), what);
+  return static_cast<T*>(p);
+}
+
+inline void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+inline int grid_for(long long n, int threads) {
+  long long blocks = (n + threads - 1) / threads;
+  long long cap = (long long)kSMs * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+}  // namespace
+
+struct shapes_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int32_t W = 0, N = 0, V = 0;
+  std::vector<int32_t> h_world_body_off;
+  std::vector<int32_t> h_body_world;
+
+  /* topology */
+  int32_t* world_body_off = nullptr;
+  int32_t* body_world = nullptr;
+  int32_t* vert_off = nullptr;
+  double* lx = nullptr;
+  double* ly = nullptr;
+  int32_t* emin = nullptr;
+  int32_t* emax = nullptr;
+  /* state */
+  double* body[10] = {nullptr};
+  double* wx = nullptr;
+  double* wy = nullptr;
+  double* nx = nullptr;
+  double* ny = nullptr;
+  double* box = nullptr;
+  uint64_t* boxk = nullptr;
+  uint8_t* flags = nullptr;
+  /* broadphase / narrowphase */
+  int32_t pair_cap = 0, contact_cap = 0;
+  int64_t item_cap = 0;
+  int32_t* row_cnt = nullptr;
+  int32_t* row_off = nullptr;
+  int32_t* pair_a = nullptr;
+  int32_t* pair_b = nullptr;
+  int32_t* slot_cnt = nullptr;
+  int32_t* slot_off = nullptr;
+  int32_t* slot_feat = nullptr;
+  double* slot_val = nullptr;
+  int32_t* world_pair_off = nullptr;
+  /* contacts: ping-pong between two buffers, the cache of step s is the
+   * contact keys + Lagrangians of step s */
+  uint64_t* c_key[2] = {nullptr, nullptr};
+  double* lam[2] = {nullptr, nullptr};
+  int32_t* cwo[2] = {nullptr, nullptr};
+  int cache_buf = 0;   /* buffer holding the current cache */
+  int results_buf = 0; /* buffer holding the last pairs/contacts results */
+  bool have_results = false;
+  int32_t* c_ga = nullptr;
+  int32_t* c_gb = nullptr;
+  uint8_t* c_flip = nullptr;
+  uint8_t* c_hit = nullptr;
+  double* c_val = nullptr;
+  Con* con = nullptr;
+  /* scheduler */
+  int32_t* last = nullptr;
+  uint32_t* items = nullptr;
+  int32_t* ilevel = nullptr;
+  uint32_t* isorted = nullptr;
+  int32_t* ihist = nullptr;
+  int32_t* world_items = nullptr;
+  int32_t* group_depth = nullptr;
+  int32_t* group_world_off = nullptr;
+  std::vector<int32_t> h_group_world_off;
+  int32_t target_group_bodies = 0;
+  int32_t solve_threads = 128;
+  /* scans */
+  int32_t* tile_sums = nullptr;
+  int32_t tile_cap = 0;
+  unsigned long long* counters = nullptr;
+  /* snapshot for retries */
+  double* snap_body[6] = {nullptr};
+  uint64_t* snap_key = nullptr;
+  double* snap_lam = nullptr;
+  int32_t* snap_cwo = nullptr;
+  int32_t snap_cap = 0;
+
+  shapes_stats stats{};
+
+  /* caller stream + per-stage profiling */
+  cudaStream_t own_stream = nullptr;
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_stage; /* stage of each recorded (start, end) pair */
+  size_t ev_used = 0;
+  double prof_ms[SHAPES_STAGE_COUNT] = {0};
+  int64_t prof_launches[SHAPES_STAGE_COUNT] = {0};
+
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      ck(cudaEventCreate(&e), "cudaEventCreate");
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+
+  /* Brackets `launches` kernel launches of stage `st` issued by f(). */
+  template <typename F>
+  void stage(int st, int launches, F&& f) {
+    if (!profiling) {
+      f();
+      return;
+    }
+    ck(cudaEventRecord(next_event(), stream), "cudaEventRecord");
+    f();
+    ck(cudaEventRecord(next_event(), stream), "cudaEventRecord");
+    ev_stage.push_back(st);
+    prof_launches[st] += launches;
+  }
+
+  /* Accumulates the recorded stage times (stream already synchronized). */
+  void collect_profile() {
+    for (size_t k = 0; k < ev_stage.size(); ++k) {
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, ev_pool[2 * k], ev_pool[2 * k + 1]), "cudaEventElapsedTime");
+      prof_ms[ev_stage[k]] += ms;
+    }
+    ev_stage.clear();
+    ev_used = 0;
+  }
+
+  Dev view(int write_buf) const {
+    Dev d{};
+    d.n_worlds = W;
+    d.n_bodies = N;
+    d.n_verts = V;
+    d.pair_cap = pair_cap;
+    d.contact_cap = contact_cap;
+    d.item_cap = (int32_t)std::min<int64_t>(item_cap, INT32_MAX);
+    d.world_body_off = world_body_off;
+    d.body_world = body_world;
+    d.vert_off = vert_off;
+    d.lx = lx;
+    d.ly = ly;
+    d.emin = emin;
+    d.emax = emax;
+    d.vx = body[0];
+    d.vy = body[1];
+    d.w = body[2];
+    d.px = body[3];
+    d.py = body[4];
+    d.th = body[5];
+    d.iml = body[6];
+    d.imr = body[7];
+    d.mu = body[8];
+    d.bounce = body[9];
+    d.wx = wx;
+    d.wy = wy;
+    d.nx = nx;
+    d.ny = ny;
+    d.box = box;
+    d.boxk = boxk;
+    d.flags = flags;
+    d.row_cnt = row_cnt;
+    d.row_off = row_off;
+    d.pair_a = pair_a;
+    d.pair_b = pair_b;
+    d.slot_cnt = slot_cnt;
+    d.slot_off = slot_off;
+    d.slot_feat = slot_feat;
+    d.slot_val = slot_val;
+    d.c_key = c_key[write_buf];
+    d.c_ga = c_ga;
+    d.c_gb = c_gb;
+    d.c_flip = c_flip;
+    d.c_hit = c_hit;
+    d.c_val = c_val;
+    d.con = con;
+    d.lam = lam[write_buf];
+    d.old_key = c_key[1 - write_buf];
+    d.old_lam = lam[1 - write_buf];
+    d.old_cwo = cwo[1 - write_buf];
+    d.world_pair_off = world_pair_off;
+    d.world_contact_off = cwo[write_buf];
+    d.last = last;
+    d.items = items;
+    d.ilevel = ilevel;
+    d.isorted = isorted;
+    d.ihist = ihist;
+    d.world_items = world_items;
+    d.group_depth = group_depth;
+    d.group_world_off = group_world_off;
+    d.counters = counters;
+    return d;
+  }
+
+  void free_step_buffers() {
+    dfree(pair_a); dfree(pair_b); dfree(slot_cnt); dfree(slot_off); dfree(slot_feat); dfree(slot_val);
+    for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
+    dfree(c_ga); dfree(c_gb); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
+    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist);
+    dfree(tile_sums);
+    dfree(snap_key); dfree(snap_lam);
+    pair_a = pair_b = slot_cnt = slot_off = slot_feat = nullptr;
+    slot_val = nullptr;
+    c_key[0] = c_key[1] = nullptr;
+    lam[0] = lam[1] = nullptr;
+    c_ga = c_gb = nullptr;
+    c_flip = c_hit = nullptr;
+    c_val = nullptr;
+    con = nullptr;
+    items = isorted = nullptr;
+    ilevel = ihist = nullptr;
+    tile_sums = nullptr;
+    snap_key = nullptr;
+    snap_lam = nullptr;
+  }
+
+  /* (Re)allocates every buffer sized by pairs/contacts/updates.  Cache
+   * contents in c_key/lam[cache_buf] are preserved across a regrowth. */
+  void alloc_step_buffers(int32_t new_pair_cap, int32_t new_contact_cap, int iterations) {
+    const int32_t old_cap = contact_cap;
+    uint64_t* keep_key = nullptr;
+    double* keep_lam = nullptr;
+    if (c_key[cache_buf] && old_cap > 0) {
+      keep_key = dalloc<uint64_t>(old_cap, "cudaMalloc keep");
+      keep_lam = dalloc<double>(2 * (size_t)old_cap, "cudaMalloc keep");
+      ck(cudaMemcpyAsync(keep_key, c_key[cache_buf], sizeof(uint64_t) * old_cap, cudaMemcpyDeviceToDevice, stream), "copy");
+      ck(cudaMemcpyAsync(keep_lam, lam[cache_buf], sizeof(double) * 2 * old_cap, cudaMemcpyDeviceToDevice, stream), "copy");
+      ck(cudaStreamSynchronize(stream), "sync");
+    }
+    free_step_buffers();
+    pair_cap = new_pair_cap;
+    contact_cap = new_contact_cap;
+    item_cap = (int64_t)(iterations + 1) * contact_cap;
+    pair_a = dalloc<int32_t>(pair_cap, "cudaMalloc pairs");
+    pair_b = dalloc<int32_t>(pair_cap, "cudaMalloc pairs");
+    slot_cnt = dalloc<int32_t>(pair_cap, "cudaMalloc slots");
+    slot_off = dalloc<int32_t>((size_t)pair_cap + 1, "cudaMalloc slots");
+    slot_feat = dalloc<int32_t>(2 * (size_t)pair_cap, "cudaMalloc slots");
+    slot_val = dalloc<double>(10 * (size_t)pair_cap, "cudaMalloc slots");
+    for (int k = 0; k < 2; ++k) {
+      c_key[k] = dalloc<uint64_t>(contact_cap, "cudaMalloc contacts");
+      lam[k] = dalloc<double>(2 * (size_t)contact_cap, "cudaMalloc contacts");
+    }
+    c_ga = dalloc<int32_t>(contact_cap, "cudaMalloc contacts");
+    c_gb = dalloc<int32_t>(contact_cap, "cudaMalloc contacts");
+    c_flip = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
+    c_hit = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
+    c_val = dalloc<double>(5 * (size_t)contact_cap, "cudaMalloc contacts");
+    con = dalloc<Con>(contact_cap, "cudaMalloc constraints");
+    items = dalloc<uint32_t>(item_cap, "cudaMalloc items");
+    ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
+    isorted = dalloc<uint32_t>(item_cap, "cudaMalloc items");
+    ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
+    const int64_t scan_n = std::max<int64_t>(N, pair_cap) + 1;
+    tile_cap = (int32_t)((scan_n + shapes::kScanTile - 1) / shapes::kScanTile) + 1;
+    tile_sums = dalloc<int32_t>(tile_cap, "cudaMalloc scan");
+    snap_cap = contact_cap;
+    snap_key = dalloc<uint64_t>(snap_cap, "cudaMalloc snapshot");
+    snap_lam = dalloc<double>(2 * (size_t)snap_cap, "cudaMalloc snapshot");
+    if (keep_key) {
+      ck(cudaMemcpyAsync(c_key[cache_buf], keep_key, sizeof(uint64_t) * old_cap, cudaMemcpyDeviceToDevice, stream), "copy");
+      ck(cudaMemcpyAsync(lam[cache_buf], keep_lam, sizeof(double) * 2 * old_cap, cudaMemcpyDeviceToDevice, stream), "copy");
+      ck(cudaStreamSynchronize(stream), "sync");
+      dfree(keep_key);
+      dfree(keep_lam);
+    }
+  }
+
+  int32_t cached_iterations = -1;
+
+  void ensure_items(int iterations) {
+    if ((int64_t)(iterations + 1) * contact_cap <= item_cap) return;
+    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist);
+    item_cap = (int64_t)(iterations + 1) * contact_cap;
+    items = dalloc<uint32_t>(item_cap, "cudaMalloc items");
+    ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
+    isorted = dalloc<uint32_t>(item_cap, "cudaMalloc items");
+    ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
+  }
+
+  void make_groups() {
+    h_group_world_off.clear();
+    h_group_world_off.push_back(0);
+    int64_t target = target_group_bodies;
+    if (target <= 0) target = std::max<int64_t>(64, (int64_t)N / (kSMs * 2));
+    int64_t acc = 0;
+    for (int w = 0; w < W; ++w) {
+      acc += h_world_body_off[w + 1] - h_world_body_off[w];
+      if (acc >= target) {
+        h_group_world_off.push_back(w + 1);
+        acc = 0;
+      }
+    }
+    if (h_group_world_off.back() != W) h_group_world_off.push_back(W);
+    dfree(group_world_off);
+    dfree(group_depth);
+    const size_t G = h_group_world_off.size() - 1;
+    group_world_off = dalloc<int32_t>(G + 1, "cudaMalloc groups");
+    group_depth = dalloc<int32_t>(G, "cudaMalloc groups");
+    ck(cudaMemcpy(group_world_off, h_group_world_off.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice), "upload groups");
+  }
+
+  int num_groups() const { return (int)h_group_world_off.size() - 1; }
+
+  void scan(const int32_t* in, int n_cap, const unsigned long long* n_dev, int32_t* out) {
+    stage(6, 3, [&]() { scan_raw(in, n_cap, n_dev, out); });
+  }
+
+  void scan_raw(const int32_t* in, int n_cap, const unsigned long long* n_dev, int32_t* out) {
+    const int tiles = (n_cap + 1 + shapes::kScanTile - 1) / shapes::kScanTile;
+    shapes::k_scan_tiles<<<tiles, shapes::kScanThreads, 0, stream>>>(in, n_cap, n_dev, tile_sums);
+    shapes::k_scan_tile_sums<<<1, 1024, 0, stream>>>(tile_sums, tiles);
+    shapes::k_scan_apply<<<tiles, shapes::kScanThreads, 0, stream>>>(in, n_cap, n_dev, tile_sums, out);
+  }
+
+  void pose(int advance, double dt) {
+    Dev d = view(0);
+    shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, dt, advance);
+  }
+
+  /* Broadphase + narrowphase into buffer `wb`; with `solve`, also constraint
+   * build, warm start, sweeps, integration. */
+  void enqueue_step(const shapes_config& cfg, bool solve, int wb) {
+    Dev d = view(wb);
+    ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntOverflow, stream), "memset");
+    stage(0, 1, [&]() { shapes::k_broadphase<true><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d); });
+    scan(row_cnt, N, nullptr, row_off);
+    stage(0, 1, [&]() { shapes::k_broadphase<false><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d); });
+    stage(6, 1, [&]() { shapes::k_world_pair_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
+    stage(1, 1, [&]() { shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d); });
+    scan(slot_cnt, pair_cap, counters + shapes::kCntPairs, slot_off);
+    stage(6, 1, [&]() { shapes::k_world_contact_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
+    stage(2, 1, [&]() {
+      shapes::k_build<<<grid_for(2LL * pair_cap, 128), 128, 0, stream>>>(d, cfg.dt, cfg.baumgarte, cfg.slop,
+                                                                           cfg.warm_start, solve ? 1 : 0);
+    });
+    if (!solve) return;
+    const int G = num_groups();
+    stage(3, 1, [&]() { shapes::k_schedule<<<G, 128, 0, stream>>>(d, cfg.iterations, cfg.warm_start); });
+    stage(4, 1, [&]() {
+      shapes::k_solve<<<G, solve_threads, 0, stream>>>(d, cfg.iterations, cfg.external, cfg.accel_x, cfg.accel_y,
+                                                       cfg.dt);
+    });
+    stage(5, 1, [&]() { shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, cfg.dt, 1); });
+  }
+
+  void snapshot() {
+    for (int k = 0; k < 6; ++k)
+      ck(cudaMemcpyAsync(snap_body[k], body[k], sizeof(double) * N, cudaMemcpyDeviceToDevice, stream), "snapshot");
+    ck(cudaMemcpyAsync(snap_key, c_key[cache_buf], sizeof(uint64_t) * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
+    ck(cudaMemcpyAsync(snap_lam, lam[cache_buf], sizeof(double) * 2 * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
+    ck(cudaMemcpyAsync(snap_cwo, cwo[cache_buf], sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "snapshot");
+  }
+
+  /* Restore into buffer `buf` (which becomes the cache buffer). */
+  void restore(int saved_cap) {
+    for (int k = 0; k < 6; ++k)
+      ck(cudaMemcpyAsync(body[k], snap_body[k], sizeof(double) * N, cudaMemcpyDeviceToDevice, stream), "restore");
+    ck(cudaMemcpyAsync(c_key[cache_buf], snap_key, sizeof(uint64_t) * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
+    ck(cudaMemcpyAsync(lam[cache_buf], snap_lam, sizeof(double) * 2 * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
+    ck(cudaMemcpyAsync(cwo[cache_buf], snap_cwo, sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "restore");
+  }
+
+  /* Runs `nsteps` steps (or one collide when !solve) with overflow retries. */
+  int run(const shapes_config& cfg, int32_t nsteps, bool solve) {
+    ensure_items(solve ? cfg.iterations : 0);
+    int retries = 0;
+    for (;;) {
+      ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 8, stream), "memset");
+      const int saved_cache_buf = cache_buf;
+      const int saved_cap = contact_cap;
+      if (solve) snapshot();
+      unsigned long long agg[8] = {0};
+      unsigned long long h[8];
+      for (int s = 0; s < (solve ? nsteps : 1); ++s) {
+        const int wb = 1 - cache_buf;
+        enqueue_step(cfg, solve, wb);
+        if (solve) cache_buf = wb;
+        results_buf = wb;
+        if (solve && nsteps > 1) {
+          /* accumulate per-step counters on the host only for the last step */
+        }
+      }
+      ck(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, stream), "read counters");
+      ck(cudaStreamSynchronize(stream), "step");
+      ck(cudaGetLastError(), "launch");
+      if (profiling) collect_profile();
+      for (int k = 0; k < 8; ++k) agg[k] = h[k];
+      if (!agg[shapes::kCntOverflow]) {
+        stats.pairs = (int64_t)agg[shapes::kCntPairs];
+        stats.contacts = (int64_t)agg[shapes::kCntContacts];
+        stats.cache_hits = (int64_t)agg[shapes::kCntHits];
+        stats.solver_items = (int64_t)agg[shapes::kCntItems];
+        stats.solver_levels = (int64_t)agg[shapes::kCntLevels];
+        stats.retries = retries;
+        have_results = true;
+        return SHAPES_OK;
+      }
+      if (++retries > 6) return SHAPES_E_CAPACITY;
+      /* undo, grow, redo */
+      cache_buf = saved_cache_buf;
+      if (solve) restore(saved_cap);
+      ck(cudaStreamSynchronize(stream), "restore");
+      const int64_t np = (int64_t)pair_cap * ((agg[shapes::kCntOverflow] & 1ull) ? 2 : 1);
+      const int64_t nc = (int64_t)contact_cap * 2;
+      if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
+      alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
+      ensure_items(solve ? cfg.iterations : 0);
+      if (solve) pose(0, 0.0);
+    }
+  }
+
+  ~shapes_batch() {
+    free_step_buffers();
+    dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly);
+    dfree(emin); dfree(emax);
+    for (int k = 0; k < 10; ++k) dfree(body[k]);
+    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
+    dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
+    for (int k = 0; k < 2; ++k) dfree(cwo[k]);
+    dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off);
+    dfree(counters);
+    for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
+    dfree(snap_cwo);
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+};
+
+namespace {
+
+bool body_arrays_ok(const shapes_bodies* b) {
+  return b && b->vel_x && b->vel_y && b->rot_vel && b->pos_x && b->pos_y && b->rot &&
+         b->inv_mass_lin && b->inv_mass_rot && b->mu && b->bounce;
+}
+
+double* const* body_ptrs(const shapes_bodies* b, double* out[10]) {
+  out[0] = b->vel_x; out[1] = b->vel_y; out[2] = b->rot_vel; out[3] = b->pos_x; out[4] = b->pos_y;
+  out[5] = b->rot; out[6] = b->inv_mass_lin; out[7] = b->inv_mass_rot; out[8] = b->mu; out[9] = b->bounce;
+  return out;
+}
+
+/* Strictly convex, counter-clockwise, no zero-length edge. */
+int check_hull(int nv, const double* xy) {
+  if (nv < 3) return SHAPES_E_INVALID_ARG;
+  if (nv > shapes::kMaxVerts) return SHAPES_E_UNSUPPORTED;
+  for (int k = 0; k < 2 * nv; ++k)
+    if (!std::isfinite(xy[k])) return SHAPES_E_NAN;
+  for (int k = 0; k < nv; ++k) {
+    const int k1 = (k + 1) % nv, k2 = (k + 2) % nv;
+    const double ex = xy[2 * k1] - xy[2 * k], ey = xy[2 * k1 + 1] - xy[2 * k + 1];
+    const double fx = xy[2 * k2] - xy[2 * k1], fy = xy[2 * k2 + 1] - xy[2 * k1 + 1];
+    if (ex == 0.0 && ey == 0.0) return SHAPES_E_INVALID_ARG;
+    if (ex * fy - ey * fx <= 0.0) return SHAPES_E_NONCONVEX;
+  }
+  return SHAPES_OK;
+}
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const CudaError&) {
+    return SHAPES_E_CUDA;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return SHAPES_E_CAPACITY;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* shapes_strerror(int status) {
+  switch (status) {
+    case SHAPES_OK: return "ok";
+    case SHAPES_E_INVALID_ARG: return "invalid argument";
+    case SHAPES_E_UNSUPPORTED: return "unsupported shape or option";
+    case SHAPES_E_NONCONVEX: return "hull is not strictly convex and counter-clockwise";
+    case SHAPES_E_CAPACITY: return "internal buffer could not grow";
+    case SHAPES_E_CUDA: return "CUDA error";
+    case SHAPES_E_TIMEOUT: return "bounded device wait gave up";
+    case SHAPES_E_NAN: return "non-finite body state";
+    case SHAPES_E_BUFFER: return "caller buffer too small";
+    default: return "unknown status";
+  }
+}
+
+const char* shapes_last_error_detail(void) { return g_last_error.c_str(); }
+
+int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, const shapes_bodies* bodies,
+                        const int32_t* vert_offsets, const double* local_verts_xy, const uint8_t* shape_kind,
+                        shapes_batch** out) {
+  if (!out || n_worlds < 1 || !world_body_offsets || !vert_offsets || !local_verts_xy || !body_arrays_ok(bodies))
+    return SHAPES_E_INVALID_ARG;
+  *out = nullptr;
+  if (world_body_offsets[0] != 0) return SHAPES_E_INVALID_ARG;
+  for (int w = 0; w < n_worlds; ++w) {
+    const int32_t n = world_body_offsets[w + 1] - world_body_offsets[w];
+    if (n < 0 || n >= (1 << 20)) return SHAPES_E_INVALID_ARG;
+  }
+  const int32_t N = world_body_offsets[n_worlds];
+  if (N < 1) return SHAPES_E_INVALID_ARG;
+  if (vert_offsets[0] != 0) return SHAPES_E_INVALID_ARG;
+  for (int32_t b = 0; b < N; ++b) {
+    if (shape_kind && shape_kind[b] == SHAPES_SHAPE_CIRCLE) return SHAPES_E_UNSUPPORTED;
+    if (shape_kind && shape_kind[b] != SHAPES_SHAPE_HULL) return SHAPES_E_INVALID_ARG;
+    const int32_t nv = vert_offsets[b + 1] - vert_offsets[b];
+    const int rc = check_hull(nv, local_verts_xy + 2 * (size_t)vert_offsets[b]);
+    if (rc != SHAPES_OK) return rc;
+  }
+  double* bp[10];
+  body_ptrs(bodies, bp);
+  for (int k = 0; k < 10; ++k)
+    for (int32_t b = 0; b < N; ++b)
+      if (!std::isfinite(bp[k][b])) return SHAPES_E_NAN;
+  return guarded([&]() -> int {
+    shapes_batch* h = new shapes_batch();
+    try {
+      ck(cudaGetDevice(&h->device), "cudaGetDevice");
+      ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      h->stream = h->own_stream;
+      h->W = n_worlds;
+      h->N = N;
+      h->V = vert_offsets[N];
+      h->h_world_body_off.assign(world_body_offsets, world_body_offsets + n_worlds + 1);
+      h->h_body_world.resize(N);
+      for (int w = 0; w < n_worlds; ++w)
+        for (int32_t b = world_body_offsets[w]; b < world_body_offsets[w + 1]; ++b) h->h_body_world[b] = w;
+      h->world_body_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+      h->body_world = dalloc<int32_t>(N, "cudaMalloc");
+      h->vert_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
+      h->lx = dalloc<double>(h->V, "cudaMalloc");
+      h->ly = dalloc<double>(h->V, "cudaMalloc");
+      h->emin = dalloc<int32_t>(h->V, "cudaMalloc");
+      h->emax = dalloc<int32_t>(h->V, "cudaMalloc");
+      for (int k = 0; k < 10; ++k) h->body[k] = dalloc<double>(N, "cudaMalloc bodies");
+      h->wx = dalloc<double>(h->V, "cudaMalloc");
+      h->wy = dalloc<double>(h->V, "cudaMalloc");
+      h->nx = dalloc<double>(h->V, "cudaMalloc");
+      h->ny = dalloc<double>(h->V, "cudaMalloc");
+      h->box = dalloc<double>(4 * (size_t)N, "cudaMalloc");
+      h->boxk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc");
+      h->flags = dalloc<uint8_t>(N, "cudaMalloc");
+      h->row_cnt = dalloc<int32_t>(N, "cudaMalloc");
+      h->row_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
+      h->world_pair_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+      for (int k = 0; k < 2; ++k) h->cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+      h->last = dalloc<int32_t>(N, "cudaMalloc");
+      h->world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
+      h->counters = dalloc<unsigned long long>(8, "cudaMalloc");
+      for (int k = 0; k < 6; ++k) h->snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
+      h->snap_cwo = dalloc<int32_t>(n_worlds + 1, "cudaMalloc snapshot");
+      ck(cudaMemcpy(h->world_body_off, world_body_offsets, sizeof(int32_t) * (n_worlds + 1), cudaMemcpyHostToDevice), "upload");
+      ck(cudaMemcpy(h->body_world, h->h_body_world.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
+      ck(cudaMemcpy(h->vert_off, vert_offsets, sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "upload");
+      std::vector<double> tmp(h->V);
+      for (int32_t v = 0; v < h->V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v];
+      ck(cudaMemcpy(h->lx, tmp.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice), "upload");
+      for (int32_t v = 0; v < h->V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v + 1];
+      ck(cudaMemcpy(h->ly, tmp.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice), "upload");
+      for (int k = 0; k < 10; ++k)
+        ck(cudaMemcpy(h->body[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice), "upload bodies");
+      /* empty cache: every world offset 0 */
+      for (int k = 0; k < 2; ++k) ck(cudaMemset(h->cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
+      const int32_t pcap = (int32_t)std::min<int64_t>(std::max<int64_t>(1024, 8LL * N), INT32_MAX / 4);
+      h->alloc_step_buffers(pcap, 2 * pcap, 8);
+      h->make_groups();
+      Dev d = h->view(0);
+      shapes::k_init_extents<<<grid_for(h->V, 128), 128, 0, h->stream>>>(d);
+      h->pose(0, 0.0);
+      ck(cudaGetLastError(), "launch");
+      ck(cudaStreamSynchronize(h->stream), "create");
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_world_create(int32_t n_bodies, const shapes_bodies* bodies, const int32_t* vert_offsets,
+                        const double* local_verts_xy, const uint8_t* shape_kind, shapes_batch** out) {
+  const int32_t off[2] = {0, n_bodies};
+  return shapes_batch_create(1, off, bodies, vert_offsets, local_verts_xy, shape_kind, out);
+}
+
+void shapes_batch_destroy(shapes_batch* b) { delete b; }
+
+static int check_cfg(const shapes_config* c) {
+  if (!c) return SHAPES_E_INVALID_ARG;
+  if (!std::isfinite(c->dt) || !std::isfinite(c->baumgarte) || !std::isfinite(c->slop) ||
+      !std::isfinite(c->accel_x) || !std::isfinite(c->accel_y))
+    return SHAPES_E_INVALID_ARG;
+  if (c->iterations < 0 || c->iterations > 64) return SHAPES_E_INVALID_ARG;
+  if (c->warm_start != SHAPES_WARM_START_OFF && c->warm_start != SHAPES_WARM_START_CACHE)
+    return SHAPES_E_UNSUPPORTED;
+  if (c->external != SHAPES_EXTERNAL_NONE && c->external != SHAPES_EXTERNAL_CONSTANT_ACCEL)
+    return SHAPES_E_UNSUPPORTED;
+  if (c->reserved != 0) return SHAPES_E_INVALID_ARG;
+  return SHAPES_OK;
+}
+
+int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps) {
+  if (!b || nsteps < 0) return SHAPES_E_INVALID_ARG;
+  const int rc = check_cfg(cfg);
+  if (rc != SHAPES_OK) return rc;
+  if (nsteps == 0) return SHAPES_OK;
+  return guarded([&]() -> int {
+    ck(cudaSetDevice(b->device), "cudaSetDevice");
+    return b->run(*cfg, nsteps, true);
+  });
+}
+
+int shapes_batch_collide(shapes_batch* b) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  shapes_config cfg{};
+  cfg.dt = 1.0;
+  return guarded([&]() -> int {
+    ck(cudaSetDevice(b->device), "cudaSetDevice");
+    return b->run(cfg, 1, false);
+  });
+}
+
+int shapes_batch_get_bodies(shapes_batch* b, shapes_bodies* out) {
+  if (!b || !body_arrays_ok(out)) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    double* bp[10];
+    body_ptrs(out, bp);
+    for (int k = 0; k < 10; ++k)
+      ck(cudaMemcpyAsync(bp[k], b->body[k], sizeof(double) * b->N, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in) {
+  if (!b || !body_arrays_ok(in)) return SHAPES_E_INVALID_ARG;
+  double* bp[10];
+  body_ptrs(in, bp);
+  for (int k = 0; k < 10; ++k)
+    for (int32_t i = 0; i < b->N; ++i)
+      if (!std::isfinite(bp[k][i])) return SHAPES_E_NAN;
+  return guarded([&]() -> int {
+    for (int k = 0; k < 10; ++k)
+      ck(cudaMemcpyAsync(b->body[k], bp[k], sizeof(double) * b->N, cudaMemcpyHostToDevice, b->stream), "upload");
+    b->pose(0, 0.0);
+    ck(cudaGetLastError(), "launch");
+    ck(cudaStreamSynchronize(b->stream), "upload");
+    b->have_results = false;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_num_worlds(shapes_batch* b, int32_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->W;
+  return SHAPES_OK;
+}
+
+int shapes_batch_num_bodies(shapes_batch* b, int64_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->N;
+  return SHAPES_OK;
+}
+
+int shapes_batch_num_vertices(shapes_batch* b, int64_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->V;
+  return SHAPES_OK;
+}
+
+int shapes_batch_get_shapes(shapes_batch* b, double* world_xy, double* normal_xy) {
+  if (!b || !world_xy || !normal_xy) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    std::vector<double> x(b->V), y(b->V), nx(b->V), ny(b->V);
+    ck(cudaMemcpyAsync(x.data(), b->wx, sizeof(double) * b->V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(y.data(), b->wy, sizeof(double) * b->V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(nx.data(), b->nx, sizeof(double) * b->V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(ny.data(), b->ny, sizeof(double) * b->V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    for (int32_t v = 0; v < b->V; ++v) {
+      world_xy[2 * (size_t)v] = x[v];
+      world_xy[2 * (size_t)v + 1] = y[v];
+      normal_xy[2 * (size_t)v] = nx[v];
+      normal_xy[2 * (size_t)v + 1] = ny[v];
+    }
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_num_pairs(shapes_batch* b, int64_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->have_results ? b->stats.pairs : 0;
+  return SHAPES_OK;
+}
+
+static void world_counts_from(shapes_batch* b, const int32_t* dev_off, int32_t* counts) {
+  std::vector<int32_t> off(b->W + 1);
+  ck(cudaMemcpyAsync(off.data(), dev_off, sizeof(int32_t) * (b->W + 1), cudaMemcpyDeviceToHost, b->stream), "download");
+  ck(cudaStreamSynchronize(b->stream), "download");
+  for (int w = 0; w < b->W; ++w) counts[w] = off[w + 1] - off[w];
+}
+
+int shapes_batch_get_pairs(shapes_batch* b, int32_t* ij, int64_t capacity, int32_t* world_counts) {
+  if (!b || (!ij && capacity > 0)) return SHAPES_E_INVALID_ARG;
+  const int64_t P = b->have_results ? b->stats.pairs : 0;
+  if (capacity < P) return SHAPES_E_BUFFER;
+  return guarded([&]() -> int {
+    std::vector<int32_t> pa(P), pb(P);
+    if (P > 0) {
+      ck(cudaMemcpyAsync(pa.data(), b->pair_a, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaMemcpyAsync(pb.data(), b->pair_b, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    for (int64_t p = 0; p < P; ++p) {
+      const int32_t off = b->h_world_body_off[b->h_body_world[pa[p]]];
+      ij[2 * p] = pa[p] - off;
+      ij[2 * p + 1] = pb[p] - off;
+    }
+    if (world_counts) {
+      if (b->have_results) world_counts_from(b, b->world_pair_off, world_counts);
+      else std::fill(world_counts, world_counts + b->W, 0);
+    }
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_num_contacts(shapes_batch* b, int64_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->have_results ? b->stats.contacts : 0;
+  return SHAPES_OK;
+}
+
+static void decode_key(uint64_t k, int32_t* out4) {
+  out4[0] = (int32_t)(k >> 44);
+  out4[1] = (int32_t)((k >> 24) & 0xfffff);
+  out4[2] = (int32_t)((k >> 12) & 0xfff);
+  out4[3] = (int32_t)(k & 0xfff);
+}
+
+int shapes_batch_get_contacts(shapes_batch* b, int32_t* keys5, double* vals5, int64_t capacity,
+                              int32_t* world_counts) {
+  if (!b || ((!keys5 || !vals5) && capacity > 0)) return SHAPES_E_INVALID_ARG;
+  const int64_t C = b->have_results ? b->stats.contacts : 0;
+  if (capacity < C) return SHAPES_E_BUFFER;
+  return guarded([&]() -> int {
+    std::vector<uint64_t> key(C);
+    std::vector<uint8_t> flip(C);
+    if (C > 0) {
+      ck(cudaMemcpyAsync(key.data(), b->c_key[b->results_buf], sizeof(uint64_t) * C, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaMemcpyAsync(flip.data(), b->c_flip, C, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaMemcpyAsync(vals5, b->c_val, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    for (int64_t c = 0; c < C; ++c) {
+      int32_t k4[4];
+      decode_key(key[c], k4);
+      for (int q = 0; q < 4; ++q) keys5[5 * c + q] = k4[q];
+      keys5[5 * c + 4] = flip[c];
+    }
+    if (world_counts) {
+      if (b->have_results) world_counts_from(b, b->cwo[b->results_buf], world_counts);
+      else std::fill(world_counts, world_counts + b->W, 0);
+    }
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_num_cache(shapes_batch* b, int64_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    int32_t total = 0;
+    ck(cudaMemcpyAsync(&total, b->cwo[b->cache_buf] + b->W, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    *out = total;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_cache(shapes_batch* b, int32_t* keys4, double* lam2, int64_t capacity, int32_t* world_counts) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  int64_t n = 0;
+  int rc = shapes_batch_num_cache(b, &n);
+  if (rc != SHAPES_OK) return rc;
+  if (capacity < n) return SHAPES_E_BUFFER;
+  if (n > 0 && (!keys4 || !lam2)) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    std::vector<uint64_t> key(n);
+    if (n > 0) {
+      ck(cudaMemcpyAsync(key.data(), b->c_key[b->cache_buf], sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaMemcpyAsync(lam2, b->lam[b->cache_buf], sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    for (int64_t c = 0; c < n; ++c) decode_key(key[c], keys4 + 4 * c);
+    if (world_counts) world_counts_from(b, b->cwo[b->cache_buf], world_counts);
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_cache(shapes_batch* b, const int32_t* world_counts, const int32_t* keys4, const double* lam2) {
+  if (!b || !world_counts) return SHAPES_E_INVALID_ARG;
+  std::vector<int32_t> off(b->W + 1, 0);
+  for (int w = 0; w < b->W; ++w) {
+    if (world_counts[w] < 0) return SHAPES_E_INVALID_ARG;
+    off[w + 1] = off[w] + world_counts[w];
+  }
+  const int64_t n = off[b->W];
+  if (n > 0 && (!keys4 || !lam2)) return SHAPES_E_INVALID_ARG;
+  std::vector<uint64_t> key(n);
+  for (int w = 0; w < b->W; ++w) {
+    const int32_t nw = b->h_world_body_off[w + 1] - b->h_world_body_off[w];
+    for (int32_t c = off[w]; c < off[w + 1]; ++c) {
+      const int32_t* k = keys4 + 4 * (size_t)c;
+      if (k[0] < 0 || k[0] >= nw || k[1] < 0 || k[1] >= nw || k[2] < 0 || k[2] >= 4096 || k[3] < 0 || k[3] >= 4096)
+        return SHAPES_E_INVALID_ARG;
+      key[c] = ((uint64_t)k[0] << 44) | ((uint64_t)k[1] << 24) | ((uint64_t)k[2] << 12) | (uint64_t)k[3];
+      if (c > off[w] && !(key[c] < key[c - 1])) return SHAPES_E_INVALID_ARG;
+    }
+  }
+  return guarded([&]() -> int {
+    if (n > b->contact_cap) {
+      const int64_t nc = std::max<int64_t>(n, 2LL * b->contact_cap);
+      if (nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
+      b->alloc_step_buffers(std::max<int32_t>(b->pair_cap, (int32_t)(nc / 2)), (int32_t)nc, 8);
+    }
+    if (n > 0) {
+      ck(cudaMemcpyAsync(b->c_key[b->cache_buf], key.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, b->stream), "upload");
+      ck(cudaMemcpyAsync(b->lam[b->cache_buf], lam2, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, b->stream), "upload");
+    }
+    ck(cudaMemcpyAsync(b->cwo[b->cache_buf], off.data(), sizeof(int32_t) * (b->W + 1), cudaMemcpyHostToDevice, b->stream), "upload");
+    ck(cudaStreamSynchronize(b->stream), "upload");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_stats(shapes_batch* b, shapes_stats* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  *out = b->stats;
+  return SHAPES_OK;
+}
+
+int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : b->own_stream;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_profiling(shapes_batch* b, int32_t enabled) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  b->profiling = enabled != 0;
+  for (int k = 0; k < SHAPES_STAGE_COUNT; ++k) {
+    b->prof_ms[k] = 0.0;
+    b->prof_launches[k] = 0;
+  }
+  return SHAPES_OK;
+}
+
+int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches) {
+  if (!b || !ms || !launches) return SHAPES_E_INVALID_ARG;
+  for (int k = 0; k < SHAPES_STAGE_COUNT; ++k) {
+    ms[k] = b->prof_ms[k];
+    launches[k] = b->prof_launches[k];
+    b->prof_ms[k] = 0.0;
+    b->prof_launches[k] = 0;
+  }
+  return SHAPES_OK;
+}
+
+int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads) {
+  if (!b || target_bodies_per_group < 0 || threads < 0 || threads > 1024 || (threads % 32) != 0)
+    return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    b->target_group_bodies = target_bodies_per_group;
+    b->solve_threads = threads > 0 ? threads : 128;
+    b->make_groups();
+    return SHAPES_OK;
+  });
+}
+
+}  // extern "C"

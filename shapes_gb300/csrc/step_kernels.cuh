@@ -1,0 +1,910 @@
+/*
+ * Device kernels of the GB300 world step.
+ *
+ * Arithmetic contract (shared with the CPU oracle): IEEE binary64, every sum a
+ * left fold in the reference's source order, no contraction (-fmad=false), the
+ * reference's comparison spellings.  Floating-point comparisons whose only job
+ * is ordering (AABB overlap) are done on order-preserving 64-bit integer keys,
+ * which give the same answers as the IEEE comparisons for every non-NaN value;
+ * NaN operands take the IEEE path.  On GB300 the FP64 pipe retires about 0.05
+ * warp-instructions per clock per SM and charges masked-off lanes in full, so
+ * every kernel here keeps warps full across its FP64 work and moves what it
+ * can to the integer pipes.
+ */
+#pragma once
+#include <cstdint>
+
+#include "shapes_sincos.h"
+
+namespace shapes {
+
+constexpr int kMaxVerts = 64;
+constexpr uint32_t kWarmBit = 0x80000000u;
+constexpr uint8_t kFlagStatic = 1;
+constexpr uint8_t kFlagBoxNaN = 2;
+
+/* Per-contact constraint data, built once per step (constraintGen,
+ * Constraints/Contact.hs:60-72) plus the step-invariant factors of the solver:
+ * effective-mass denominators (effMassM2, Constraint.hs:173-179), pairMu
+ * (Friction.hs:46-48) and min bounciness (Restitution.hs:51). */
+struct __align__(16) Con {
+  double jn[6];
+  double jf[6];
+  double bn;
+  double rax, ray, rbx, rby, rnx, rny;
+  double mcn, mcf;
+  double mu;
+  double e;
+  double pad;
+};
+
+/* Device view of a batch; passed by value to every kernel. */
+struct Dev {
+  int32_t n_worlds, n_bodies, n_verts;
+  int32_t pair_cap, contact_cap, item_cap;
+  const int32_t* world_body_off; /* [W+1] */
+  const int32_t* body_world;     /* [N] */
+  const int32_t* vert_off;       /* [N+1] */
+  const double* lx;
+  const double* ly;
+  int32_t* emin;
+  int32_t* emax;
+  double* vx;
+  double* vy;
+  double* w;
+  double* px;
+  double* py;
+  double* th;
+  const double* iml;
+  const double* imr;
+  const double* mu;
+  const double* bounce;
+  double* wx;
+  double* wy;
+  double* nx;
+  double* ny;
+  double* box;      /* [4N] x0 x1 y0 y1 */
+  uint64_t* boxk;   /* [4N] ordered keys of box */
+  uint8_t* flags;   /* [N] */
+  int32_t* row_cnt; /* [N] mirrored per-row pair counts */
+  int32_t* row_off; /* [N+1] scanned */
+  int32_t* pair_a;  /* [pair_cap] global body index, the larger */
+  int32_t* pair_b;  /* [pair_cap] */
+  int32_t* slot_cnt;   /* [pair_cap] contacts per pair (0..2) */
+  int32_t* slot_off;   /* [pair_cap+1] scanned */
+  int32_t* slot_feat;  /* [2*pair_cap] fa | fb<<12 | flip<<24 */
+  double* slot_val;    /* [2*pair_cap*5] nx ny px py depth */
+  uint64_t* c_key;     /* [contact_cap] packed world-local key */
+  int32_t* c_ga;       /* [contact_cap] */
+  int32_t* c_gb;       /* [contact_cap] */
+  uint8_t* c_flip;     /* [contact_cap] */
+  uint8_t* c_hit;      /* [contact_cap] */
+  double* c_val;       /* [contact_cap*5] */
+  Con* con;            /* [contact_cap] */
+  double* lam;         /* [2*contact_cap] this step's cache Lagrangians */
+  const uint64_t* old_key; /* previous cache keys */
+  const double* old_lam;   /* previous cache Lagrangians */
+  const int32_t* old_cwo;  /* [W+1] previous cache world offsets */
+  int32_t* world_pair_off;    /* [W+1] */
+  int32_t* world_contact_off; /* [W+1] */
+  int32_t* last;              /* [N] scheduler scratch */
+  uint32_t* items;            /* [item_cap] */
+  int32_t* ilevel;            /* [item_cap] */
+  uint32_t* isorted;          /* [item_cap] */
+  int32_t* ihist;             /* [item_cap] */
+  int32_t* world_items;       /* [W] */
+  int32_t* group_depth;       /* [G] */
+  const int32_t* group_world_off; /* [G+1] */
+  unsigned long long* counters;   /* [8] see kCnt* */
+};
+
+enum {
+  kCntPairs = 0,
+  kCntContacts = 1,
+  kCntHits = 2,
+  kCntItems = 3,
+  kCntLevels = 4,
+  kCntOverflow = 5,
+};
+
+/* ------------------------------------------------------------------------ */
+/* helpers                                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Order-preserving key of a binary64: for non-NaN a, b,
+ * a < b  <=>  okey(a) < okey(b), and a == b <=> okey(a) == okey(b). */
+__device__ __forceinline__ uint64_t okey(double d) {
+  uint64_t u = (uint64_t)__double_as_longlong(d);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ bool is_nan(double d) { return d != d; }
+
+__device__ __forceinline__ uint64_t pack_key(int i, int j, int fa, int fb) {
+  return ((uint64_t)i << 44) | ((uint64_t)j << 24) | ((uint64_t)fa << 12) | (uint64_t)fb;
+}
+
+/* ------------------------------------------------------------------------ */
+/* A2 pose + A11 integrate                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* listToHull extents (ConvexHull.hs:151-167): for each local edge, the first
+ * strict min / max vertex along its local unit normal (extentAlong',
+ * ConvexHull.hs:81-92).  One thread per edge. */
+__global__ void k_init_extents(Dev d) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < d.n_verts; v += gridDim.x * blockDim.x) {
+    /* find the owning body by binary search over vert_off */
+    int lo = 0, hi = d.n_bodies - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (d.vert_off[mid] <= v) lo = mid; else hi = mid - 1;
+    }
+    const int b0 = d.vert_off[lo], nv = d.vert_off[lo + 1] - b0, e = v - b0;
+    const int n1 = e < nv - 1 ? e + 1 : 0;
+    const double ddx = d.lx[b0 + n1] - d.lx[b0 + e], ddy = d.ly[b0 + n1] - d.ly[b0 + e];
+    const double ex = ddy, ey = -ddx;
+    const double len = sqrt(ex * ex + ey * ey);
+    const double nx = ex / len, ny = ey / len;
+    double lo_d = d.lx[b0] * nx + d.ly[b0] * ny, hi_d = lo_d;
+    int imin = 0, imax = 0;
+    for (int k = 1; k < nv; ++k) {
+      const double t = d.lx[b0 + k] * nx + d.ly[b0 + k] * ny;
+      if (t < lo_d) { lo_d = t; imin = k; }
+      if (t > hi_d) { hi_d = t; imax = k; }
+    }
+    d.emin[v] = imin;
+    d.emax[v] = imax;
+  }
+}
+
+/* advanceObj (Constraint.hs:225-229) when `advance`, then moveShape
+ * (World.hs:132-133): rotation matrix from shapes_sincos, the 3x3 product of
+ * toTransform (Transform.hs:34-38, 73-77; MatrixTemplate.hs:47-67), afmul
+ * (Linear.hs:217-220) per vertex, unitEdgeNormal (ConvexHull.hs:218-226) per
+ * edge, then hullToAabb (Aabb.hs:81-84, 106-110) and its ordered keys.
+ * One thread per body. */
+__global__ void k_integrate_pose(Dev d, double dt, int advance) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    double px = d.px[g], py = d.py[g], th = d.th[g];
+    if (advance) {
+      const double vx = d.vx[g], vy = d.vy[g], w = d.w[g];
+      px = (vx * dt) + px;
+      py = (vy * dt) + py;
+      th = (dt * w) + th;
+      d.px[g] = px;
+      d.py[g] = py;
+      d.th[g] = th;
+    }
+    double s, c;
+    shapes_sincos(th, &s, &c);
+    const double ms = -s;
+    /* rows of translate(px,py) times columns of rotate(c,s) */
+    const double m00 = (1.0 * c + 0.0 * s) + px * 0.0;
+    const double m01 = (1.0 * ms + 0.0 * c) + px * 0.0;
+    const double m02 = (1.0 * 0.0 + 0.0 * 0.0) + px * 1.0;
+    const double m10 = (0.0 * c + 1.0 * s) + py * 0.0;
+    const double m11 = (0.0 * ms + 1.0 * c) + py * 0.0;
+    const double m12 = (0.0 * 0.0 + 1.0 * 0.0) + py * 1.0;
+    const int b0 = d.vert_off[g], nv = d.vert_off[g + 1] - b0;
+    double x0 = 0, y0 = 0, xp = 0, yp = 0;
+    double bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
+    for (int k = 0; k < nv; ++k) {
+      const double lx = d.lx[b0 + k], ly = d.ly[b0 + k];
+      const double x = (m00 * lx + m01 * ly) + m02 * 1.0;
+      const double y = (m10 * lx + m11 * ly) + m12 * 1.0;
+      d.wx[b0 + k] = x;
+      d.wy[b0 + k] = y;
+      if (k == 0) {
+        x0 = x; y0 = y;
+        bx0 = x; bx1 = x; by0 = y; by1 = y;
+      } else {
+        const double ddx = x - xp, ddy = y - yp;
+        const double ex = ddy, ey = -ddx;
+        const double len = sqrt(ex * ex + ey * ey);
+        d.nx[b0 + k - 1] = ex / len;
+        d.ny[b0 + k - 1] = ey / len;
+        bx0 = bx0 < x ? bx0 : x;
+        bx1 = bx1 > x ? bx1 : x;
+        by0 = by0 < y ? by0 : y;
+        by1 = by1 > y ? by1 : y;
+      }
+      xp = x;
+      yp = y;
+    }
+    {
+      const double ddx = x0 - xp, ddy = y0 - yp;
+      const double ex = ddy, ey = -ddx;
+      const double len = sqrt(ex * ex + ey * ey);
+      d.nx[b0 + nv - 1] = ex / len;
+      d.ny[b0 + nv - 1] = ey / len;
+    }
+    d.box[4 * g + 0] = bx0;
+    d.box[4 * g + 1] = bx1;
+    d.box[4 * g + 2] = by0;
+    d.box[4 * g + 3] = by1;
+    d.boxk[4 * g + 0] = okey(bx0);
+    d.boxk[4 * g + 1] = okey(bx1);
+    d.boxk[4 * g + 2] = okey(by0);
+    d.boxk[4 * g + 3] = okey(by1);
+    uint8_t f = 0;
+    if (d.iml[g] == 0.0 && d.imr[g] == 0.0) f |= kFlagStatic;
+    if (is_nan(bx0) || is_nan(bx1) || is_nan(by0) || is_nan(by1)) f |= kFlagBoxNaN;
+    d.flags[g] = f;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* A3 broadphase                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* culledKeys (Aabb.hs:168-183): not both static, and boundsOverlap
+ * (Aabb.hs:69-72) on x and y, i.e. not (c > b || d < a) with (a,b) = box i,
+ * (c,d) = box j. */
+__device__ __forceinline__ bool pair_overlaps(const Dev& d, int gi, int gj, uint8_t fi,
+                                              const uint64_t ki[4]) {
+  const uint8_t fj = d.flags[gj];
+  if ((fi & fj & kFlagStatic)) return false;
+  if ((fi | fj) & kFlagBoxNaN) {
+    const double* a = d.box + 4 * gi;
+    const double* b = d.box + 4 * gj;
+    return !(b[0] > a[1] || b[1] < a[0]) && !(b[2] > a[3] || b[3] < a[2]);
+  }
+  const ulonglong2 kj01 = *reinterpret_cast<const ulonglong2*>(d.boxk + 4 * gj);
+  const ulonglong2 kj23 = *reinterpret_cast<const ulonglong2*>(d.boxk + 4 * gj + 2);
+  return !(kj01.x > ki[1] || kj01.y < ki[0]) && !(kj23.x > ki[3] || kj23.y < ki[2]);
+}
+
+/* One warp per row i (the larger index of a pair): lanes test j = i-1, i-2, ...
+ * 32 at a time, so ballot order is the reference's descending j order.
+ * COUNT: writes the row's pair count at its mirrored position
+ * q = off + (n_w - 1 - i), so that an exclusive scan over q lays rows out in
+ * descending i within each world.  !COUNT: writes the pairs at row_off[q]. */
+template <bool COUNT>
+__global__ void k_broadphase(Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw_total = (gridDim.x * blockDim.x) >> 5;
+  for (int g = wid; g < d.n_bodies; g += nw_total) {
+    const int wld = d.body_world[g];
+    const int off = d.world_body_off[wld];
+    const int n = d.world_body_off[wld + 1] - off;
+    const int i = g - off;
+    const int q = off + (n - 1 - i);
+    const uint8_t fi = d.flags[g];
+    uint64_t ki[4];
+    ki[0] = d.boxk[4 * g + 0];
+    ki[1] = d.boxk[4 * g + 1];
+    ki[2] = d.boxk[4 * g + 2];
+    ki[3] = d.boxk[4 * g + 3];
+    int count = 0;
+    const int base_out = COUNT ? 0 : d.row_off[q];
+    for (int base = 0; base < i; base += 32) {
+      const int jl = i - 1 - base - lane;
+      bool hit = false;
+      if (jl >= 0) hit = pair_overlaps(d, g, off + jl, fi, ki);
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (!COUNT && hit) {
+        const int pos = base_out + count + __popc(m & ((1u << lane) - 1u));
+        if (pos < d.pair_cap) {
+          d.pair_a[pos] = g;
+          d.pair_b[pos] = off + jl;
+        }
+      }
+      count += __popc(m);
+    }
+    if (COUNT && lane == 0) d.row_cnt[q] = count;
+  }
+}
+
+/* world_pair_off[w] = row_off[world_body_off[w]] (first row of the world in
+ * mirrored order); also records the pair total and overflow. */
+__global__ void k_world_pair_offsets(Dev d) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w <= d.n_worlds; w += gridDim.x * blockDim.x) {
+    const int p = d.row_off[d.world_body_off[w]];
+    d.world_pair_off[w] = p;
+    if (w == d.n_worlds) {
+      d.counters[kCntPairs] = (unsigned long long)p;
+      if (p > d.pair_cap) d.counters[kCntOverflow] |= 1ull;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* A5-A7 narrowphase                                                          */
+/* ------------------------------------------------------------------------ */
+
+struct HullView {
+  const double* wx;
+  const double* wy;
+  const double* nx;
+  const double* ny;
+  const int32_t* emin;
+  const int32_t* emax;
+  int nv;
+};
+
+__device__ __forceinline__ HullView hull_view(const Dev& d, int g) {
+  const int b0 = d.vert_off[g];
+  HullView h;
+  h.wx = d.wx + b0;
+  h.wy = d.wy + b0;
+  h.nx = d.nx + b0;
+  h.ny = d.ny + b0;
+  h.emin = d.emin + b0;
+  h.emax = d.emax + b0;
+  h.nv = d.vert_off[g + 1] - b0;
+  return h;
+}
+
+/* overlap (SAT.hs:103-118): extentAlongSelf with the precomputed extent
+ * indices (ConvexHull.hs:111-118), extentAlong over the penetrator
+ * (ConvexHull.hs:81-100), overlapTest/overlapAmount (SAT.hs:74-95). */
+__device__ __forceinline__ bool sat_axis(const HullView& se, int e, const HullView& sp,
+                                         double* depth, int* pen) {
+  const double dx = se.nx[e], dy = se.ny[e];
+  const int mi = se.emin[e], ma = se.emax[e];
+  const double sa = se.wx[mi] * dx + se.wy[mi] * dy;
+  const double sb = se.wx[ma] * dx + se.wy[ma] * dy;
+  double lo = sp.wx[0] * dx + sp.wy[0] * dy, hi = lo;
+  int pmin = 0;
+  for (int k = 1; k < sp.nv; ++k) {
+    const double t = sp.wx[k] * dx + sp.wy[k] * dy;
+    if (t < lo) { lo = t; pmin = k; }
+    if (t > hi) { hi = t; }
+  }
+  *pen = pmin;
+  if (lo > sb || hi < sa) return false; /* Separated */
+  *depth = sb - lo;
+  return true;
+}
+
+/* minOverlap (SAT.hs:121-138): first Separated axis, else first strict
+ * minimum depth.  Returns false when separated. */
+__device__ __forceinline__ bool min_overlap(const HullView& se, const HullView& sp, int* edge,
+                                            double* depth, int* pen) {
+  double best = 0.0;
+  int be = 0, bp = 0;
+  for (int e = 0; e < se.nv; ++e) {
+    double dep;
+    int p;
+    if (!sat_axis(se, e, sp, &dep, &p)) return false;
+    if (e == 0 || dep < best) { best = dep; be = e; bp = p; }
+  }
+  *edge = be;
+  *depth = best;
+  *pen = bp;
+  return true;
+}
+
+enum { kClipNone = 0, kClipLeft = 1, kClipRight = 2, kClipBoth = 3 };
+
+/* clipSegment (Linear.hs:327-343), intersect2 (Linear.hs:244-251),
+ * invM2x2 (Linear.hs:194-199). */
+__device__ __forceinline__ int clip_segment(double bpx, double bpy, double bnx, double bny,
+                                            double ipx, double ipy, double inx, double iny,
+                                            double ax, double ay, double bx, double by,
+                                            double* cx, double* cy) {
+  const double b0 = bpx * bnx + bpy * bny;
+  const double b1 = ipx * inx + ipy * iny;
+  const double det = bnx * iny - bny * inx;
+  const double inv = 1.0 / det;
+  const double m00 = iny * inv, m01 = (-bny) * inv, m10 = (-inx) * inv, m11 = bnx * inv;
+  const double x = m00 * b0 + m01 * b1;
+  const double y = m10 * b0 + m11 * b1;
+  *cx = x;
+  *cy = y;
+  const double a_ = ax * bnx + ay * bny;
+  const double b_ = bx * bnx + by * bny;
+  const double c_ = x * bnx + y * bny;
+  if (a_ < c_) return b_ < c_ ? kClipBoth : kClipLeft;
+  if (b_ < c_) return kClipRight;
+  return kClipNone;
+}
+
+/* contact_ (SAT.hs:261-267): penetratingEdge (SAT.hs:152-166), clipEdge
+ * (SAT.hs:190-218) and flattenContactPoints (SAT.hs:181-187).  Writes up to
+ * two (index, x, y) points, descending index. */
+__device__ __forceinline__ int manifold(const HullView& se, int e, const HullView& sp, int pen,
+                                        int idx[2], double xs[2], double ys[2]) {
+  const int ne = e < se.nv - 1 ? e + 1 : 0;
+  const double ax = se.wx[e], ay = se.wy[e], bx = se.wx[ne], by = se.wy[ne];
+  const double nx = se.nx[e], ny = se.ny[e];
+  const int vb = pen, vc = pen < sp.nv - 1 ? pen + 1 : 0, va = pen > 0 ? pen - 1 : sp.nv - 1;
+  const double abn = fabs((sp.wx[vb] - sp.wx[va]) * nx + (sp.wy[vb] - sp.wy[va]) * ny);
+  const double bcn = fabs((sp.wx[vc] - sp.wx[vb]) * nx + (sp.wy[vc] - sp.wy[vb]) * ny);
+  int ci, di;
+  if (bcn < abn) { ci = vb; di = vc; } else { ci = va; di = vb; }
+  double cx = sp.wx[ci], cy = sp.wy[ci], dx = sp.wx[di], dy = sp.wy[di];
+  const double lpx = cx, lpy = cy;
+  const double lnx = dy - cy, lny = -(dx - cx);
+  double qx, qy;
+  int k = clip_segment(ax, ay, bx - ax, by - ay, lpx, lpy, lnx, lny, cx, cy, dx, dy, &qx, &qy);
+  if (k == kClipBoth) return 0;
+  if (k == kClipLeft) { cx = qx; cy = qy; }
+  if (k == kClipRight) { dx = qx; dy = qy; }
+  k = clip_segment(bx, by, ax - bx, ay - by, lpx, lpy, lnx, lny, cx, cy, dx, dy, &qx, &qy);
+  if (k == kClipBoth) return 0;
+  if (k == kClipLeft) { cx = qx; cy = qy; }
+  if (k == kClipRight) { dx = qx; dy = qy; }
+  k = clip_segment(ax, ay, -nx, -ny, lpx, lpy, lnx, lny, cx, cy, dx, dy, &qx, &qy);
+  if (k == kClipBoth) return 0;
+  if (k == kClipLeft) { idx[0] = di; xs[0] = dx; ys[0] = dy; return 1; }
+  if (k == kClipRight) { idx[0] = ci; xs[0] = cx; ys[0] = cy; return 1; }
+  if (ci > di) {
+    idx[0] = ci; xs[0] = cx; ys[0] = cy;
+    idx[1] = di; xs[1] = dx; ys[1] = dy;
+  } else {
+    idx[0] = di; xs[0] = dx; ys[0] = dy;
+    idx[1] = ci; xs[1] = cx; ys[1] = cy;
+  }
+  return 2;
+}
+
+/* HullVsHull.generateContacts (HullVsHull.hs:54-90) over SAT.contact
+ * (SAT.hs:238-258) for every broadphase pair.  One thread per pair; results
+ * go to two fixed slots per pair and are compacted after a scan. */
+__global__ void k_narrowphase(Dev d) {
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const int ga = d.pair_a[p], gb = d.pair_b[p];
+    const HullView a = hull_view(d, ga), b = hull_view(d, gb);
+    int cnt = 0;
+    int e_ab, pen_ab, e_ba, pen_ba;
+    double dep_ab, dep_ba;
+    if (min_overlap(a, b, &e_ab, &dep_ab, &pen_ab) && min_overlap(b, a, &e_ba, &dep_ba, &pen_ba)) {
+      const bool flip = !(dep_ab < dep_ba);
+      const HullView& se = flip ? b : a;
+      const HullView& sp = flip ? a : b;
+      const int e = flip ? e_ba : e_ab;
+      const int pen = flip ? pen_ba : pen_ab;
+      int idx[2];
+      double xs[2], ys[2];
+      cnt = manifold(se, e, sp, pen, idx, xs, ys);
+      const double nx = se.nx[e], ny = se.ny[e];
+      const double vdot = se.wx[e] * nx + se.wy[e] * ny;
+      for (int q = 0; q < cnt; ++q) {
+        const int fa = flip ? idx[q] : e;
+        const int fb = flip ? e : idx[q];
+        d.slot_feat[2 * p + q] = fa | (fb << 12) | ((flip ? 1 : 0) << 24);
+        double* v = d.slot_val + 5 * (2 * (size_t)p + q);
+        v[0] = nx;
+        v[1] = ny;
+        v[2] = xs[q];
+        v[3] = ys[q];
+        v[4] = vdot - (xs[q] * nx + ys[q] * ny);
+      }
+    }
+    d.slot_cnt[p] = cnt;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* A8-A9 constraint build + warm-start lookup                                 */
+/* ------------------------------------------------------------------------ */
+
+__device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) {
+  return ax * by - ay * bx;
+}
+
+/* world_contact_off[w] = slot_off[world_pair_off[w]]; totals + overflow. */
+__global__ void k_world_contact_offsets(Dev d) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w <= d.n_worlds; w += gridDim.x * blockDim.x) {
+    const int p = min(d.world_pair_off[w], d.pair_cap);
+    const int c = d.slot_off[p];
+    d.world_contact_off[w] = c;
+    if (w == d.n_worlds) {
+      d.counters[kCntContacts] = (unsigned long long)c;
+      if (c > d.contact_cap) d.counters[kCntOverflow] |= 2ull;
+    }
+  }
+}
+
+/* One thread per contact slot.  Compacts the contact, builds its
+ * ContactConstraint (NonPenetration.hs:16-56, Friction.hs:18-44,
+ * Restitution.hs:21-31, flip handling Utils.hs:175-215 / Constraint.hs:96-98),
+ * the step-invariant solver factors, and looks the key up in the previous
+ * cache: descZipVector (Utils/Descending.hs:47-71) over two strictly
+ * descending key lists pairs each new key with an equal old key exactly when
+ * one exists, which a binary search over the world's old entries finds.
+ * `build_solver` = 0 compacts contacts only (collide). */
+__global__ void k_build(Dev d, double dt, double beta, double slop, int warm_start, int build_solver) {
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  const int C = (int)d.counters[kCntContacts];
+  if (C > d.contact_cap) return;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * P; t += gridDim.x * blockDim.x) {
+    const int p = t >> 1, s = t & 1;
+    if (s >= d.slot_cnt[p]) continue;
+    const int c = d.slot_off[p] + s;
+    const int ga = d.pair_a[p], gb = d.pair_b[p];
+    const int wld = d.body_world[ga];
+    const int off = d.world_body_off[wld];
+    const int feat = d.slot_feat[t];
+    const int fa = feat & 0xfff, fb = (feat >> 12) & 0xfff, flip = (feat >> 24) & 1;
+    const double* v = d.slot_val + 5 * (size_t)t;
+    const double nx = v[0], ny = v[1], px = v[2], py = v[3], depth = v[4];
+    const uint64_t key = pack_key(ga - off, gb - off, fa, fb);
+    d.c_key[c] = key;
+    d.c_ga[c] = ga;
+    d.c_gb[c] = gb;
+    d.c_flip[c] = (uint8_t)flip;
+    double* cv = d.c_val + 5 * (size_t)c;
+    cv[0] = nx;
+    cv[1] = ny;
+    cv[2] = px;
+    cv[3] = py;
+    cv[4] = depth;
+    if (!build_solver) continue;
+    /* constraintGen: positions of (a, b) = (i, j); a Flip contact is built
+     * with the bodies swapped, then its Jacobian halves are swapped back. */
+    const double xi = d.px[ga], yi = d.py[ga], xj = d.px[gb], yj = d.py[gb];
+    const double xa = flip ? xj : xi, ya = flip ? yj : yi;
+    const double xb = flip ? xi : xj, yb = flip ? yi : yj;
+    double jn[6], jf[6];
+    jn[0] = -nx;
+    jn[1] = -ny;
+    jn[2] = cross2(xa - px, ya - py, nx, ny);
+    jn[3] = nx;
+    jn[4] = ny;
+    jn[5] = cross2(px - xb, py - yb, nx, ny);
+    const double tbx = ny, tby = -nx;
+    const double tax = -tbx, tay = -tby;
+    jf[0] = tax;
+    jf[1] = tay;
+    jf[2] = cross2(px - xa, py - ya, tax, tay);
+    jf[3] = tbx;
+    jf[4] = tby;
+    jf[5] = cross2(px - xb, py - yb, tbx, tby);
+    Con cc;
+    for (int k = 0; k < 3; ++k) {
+      cc.jn[k] = flip ? jn[k + 3] : jn[k];
+      cc.jn[k + 3] = flip ? jn[k] : jn[k + 3];
+      cc.jf[k] = flip ? jf[k + 3] : jf[k];
+      cc.jf[k + 3] = flip ? jf[k] : jf[k + 3];
+    }
+    cc.bn = depth > slop ? (beta / dt) * (slop - depth) : 0.0;
+    cc.rax = px - xi;
+    cc.ray = py - yi;
+    cc.rbx = px - xj;
+    cc.rby = py - yj;
+    cc.rnx = flip ? -nx : nx;
+    cc.rny = flip ? -ny : ny;
+    const double ima = d.iml[ga], ira = d.imr[ga], imb = d.iml[gb], irb = d.imr[gb];
+    const double m[6] = {ima, ima, ira, imb, imb, irb};
+    double mcn = (cc.jn[0] * m[0]) * cc.jn[0];
+    double mcf = (cc.jf[0] * m[0]) * cc.jf[0];
+    for (int k = 1; k < 6; ++k) {
+      mcn = mcn + (cc.jn[k] * m[k]) * cc.jn[k];
+      mcf = mcf + (cc.jf[k] * m[k]) * cc.jf[k];
+    }
+    cc.mcn = mcn;
+    cc.mcf = mcf;
+    cc.mu = (d.mu[ga] + d.mu[gb]) / 2.0;
+    const double ea = d.bounce[ga], eb = d.bounce[gb];
+    cc.e = ea <= eb ? ea : eb;
+    cc.pad = 0.0;
+    d.con[c] = cc;
+    /* warm-start lookup */
+    double l0 = 0.0, l1 = 0.0;
+    uint8_t hit = 0;
+    if (warm_start) {
+      int lo = d.old_cwo[wld], hi = d.old_cwo[wld + 1] - 1;
+      while (lo <= hi) { /* keys strictly descending */
+        const int mid = (lo + hi) >> 1;
+        const uint64_t k = d.old_key[mid];
+        if (k == key) {
+          hit = 1;
+          l0 = d.old_lam[2 * mid];
+          l1 = d.old_lam[2 * mid + 1];
+          break;
+        }
+        if (k > key) lo = mid + 1; else hi = mid - 1;
+      }
+    }
+    d.c_hit[c] = hit;
+    d.lam[2 * c] = l0;
+    d.lam[2 * c + 1] = l1;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* A9-A10 dependency-level schedule                                           */
+/* ------------------------------------------------------------------------ */
+
+/* Block-wide exclusive scan of in-place int array a[0..n), returns total. */
+__device__ int block_exclusive_scan(int32_t* a, int n, int32_t* smem /* >= 32 */) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, wid = tid >> 5, nwarp = (nt + 31) >> 5;
+  int carry = 0;
+  for (int base = 0; base < n; base += nt) {
+    const int idx = base + tid;
+    const int x = idx < n ? a[idx] : 0;
+    int incl = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) smem[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      int ws = lane < nwarp ? smem[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, ws, o);
+        if (lane >= o) ws += y;
+      }
+      if (lane < nwarp) smem[lane] = ws; /* inclusive warp sums */
+    }
+    __syncthreads();
+    const int wprefix = wid > 0 ? smem[wid - 1] : 0;
+    const int chunk_total = smem[nwarp - 1];
+    if (idx < n) a[idx] = carry + wprefix + incl - x;
+    carry += chunk_total;
+    __syncthreads();
+  }
+  return carry;
+}
+
+/* The reference applies warm starts then `iterations` sweeps strictly in
+ * contact order (Solvers/Contact.hs:74-157).  Each update reads and writes only
+ * its two bodies' velocities and its own Lagrangians, so running update u after
+ * every earlier update that shares a non-static body with it reproduces the
+ * sequential result bit for bit.  Static bodies are read-only in the step.
+ * level(u) = 1 + max(level of the last earlier update on each of its dynamic
+ * bodies); updates of one level touch disjoint bodies.  Levels pipeline the
+ * sweeps: sweep s+1 starts on a body as soon as sweep s is done with it.
+ * One CTA per solver group (a contiguous run of worlds): warp 0 scans its worlds
+ * (lane = world), then the block counting-sorts the group's updates by level. */
+__global__ void k_schedule(Dev d, int iterations, int warm_start) {
+  __shared__ int32_t s_scan[32];
+  __shared__ int32_t s_depth;
+  if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
+  const int grp = blockIdx.x;
+  const int w0 = d.group_world_off[grp], w1 = d.group_world_off[grp + 1];
+  const int stride = iterations + 1;
+  const int c_base = d.world_contact_off[w0];
+  const size_t ibase = (size_t)stride * c_base;
+  if (threadIdx.x == 0) s_depth = 0;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int depth = 0;
+    for (int wld = w0 + (int)threadIdx.x; wld < w1; wld += 32) {
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int b = b0; b < b1; ++b) d.last[b] = 0;
+      const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+      size_t out = (size_t)stride * c0;
+      int n_items = 0;
+      for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
+        for (int c = c0; c < c1; ++c) {
+          if (pass == 0 && !d.c_hit[c]) continue;
+          const int ga = d.c_ga[c], gb = d.c_gb[c];
+          const bool da = !(d.flags[ga] & kFlagStatic), db = !(d.flags[gb] & kFlagStatic);
+          const int la = da ? d.last[ga] : 0, lb = db ? d.last[gb] : 0;
+          const int lvl = (la > lb ? la : lb) + 1;
+          if (da) d.last[ga] = lvl;
+          if (db) d.last[gb] = lvl;
+          d.items[out + n_items] = (uint32_t)c | (pass == 0 ? kWarmBit : 0u);
+          d.ilevel[out + n_items] = lvl;
+          ++n_items;
+          depth = lvl > depth ? lvl : depth;
+        }
+      }
+      d.world_items[wld] = n_items;
+      if (warm_start) atomicAdd(&d.counters[kCntHits], (unsigned long long)(n_items - iterations * (c1 - c0)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const int y = __shfl_xor_sync(0xffffffffu, depth, o);
+      depth = y > depth ? y : depth;
+    }
+    if (threadIdx.x == 0) s_depth = depth;
+  }
+  __syncthreads();
+  const int depth = s_depth;
+  if (threadIdx.x == 0) {
+    d.group_depth[grp] = depth;
+    atomicAdd(&d.counters[kCntLevels], (unsigned long long)depth);
+  }
+  if (depth == 0) return;
+  int32_t* hist = d.ihist + ibase;
+  for (int k = threadIdx.x; k < depth; k += blockDim.x) hist[k] = 0;
+  __syncthreads();
+  int total = 0;
+  for (int wld = w0; wld < w1; ++wld) {
+    const size_t o = (size_t)stride * d.world_contact_off[wld];
+    const int n_items = d.world_items[wld];
+    for (int k = threadIdx.x; k < n_items; k += blockDim.x) atomicAdd(&hist[d.ilevel[o + k] - 1], 1);
+    total += n_items;
+  }
+  __syncthreads();
+  block_exclusive_scan(hist, depth, s_scan);
+  __syncthreads();
+  for (int wld = w0; wld < w1; ++wld) {
+    const size_t o = (size_t)stride * d.world_contact_off[wld];
+    const int n_items = d.world_items[wld];
+    for (int k = threadIdx.x; k < n_items; k += blockDim.x) {
+      const int pos = atomicAdd(&hist[d.ilevel[o + k] - 1], 1);
+      d.isorted[ibase + pos] = d.items[o + k];
+    }
+  }
+  if (threadIdx.x == 0) atomicAdd(&d.counters[kCntItems], (unsigned long long)total);
+}
+
+/* ------------------------------------------------------------------------ */
+/* A9-A10 solver                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* applyLagrangian2 (Constraint.hs:197-204): v += (J * lambda) * invMass. */
+__device__ __forceinline__ void apply_impulse(const double j[6], double l, double v[6],
+                                              const double m[6]) {
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = v[k] + (j[k] * l) * m[k];
+}
+
+__device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
+  double s = j[0] * v[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) s = s + j[k] * v[k];
+  return s;
+}
+
+/* One dependency level's update.  Warm: applySln of the cached Lagrangians
+ * (Solvers/Contact.hs:105-113).  Otherwise improveContactSln
+ * (Solvers/Contact.hs:124-143): both new Lagrangians from the same velocities
+ * (contactLagrangian, Constraints/Contact.hs:86-95; bounceB,
+ * Restitution.hs:34-51; lagrangian2, Constraint.hs:164-169), then positive /
+ * clampAbs (SolutionProcessors.hs:33-53) and applySln (non-penetration first). */
+__device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
+  const int c = (int)(item & ~kWarmBit);
+  const int ga = d.c_ga[c], gb = d.c_gb[c];
+  const Con& cc = d.con[c];
+  double j_n[6], j_f[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) { j_n[k] = cc.jn[k]; j_f[k] = cc.jf[k]; }
+  double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
+  const double ima = d.iml[ga], ira = d.imr[ga], imb = d.iml[gb], irb = d.imr[gb];
+  const double m[6] = {ima, ima, ira, imb, imb, irb};
+  double ln_apply, lf_apply;
+  if (item & kWarmBit) {
+    ln_apply = d.lam[2 * c];
+    lf_apply = d.lam[2 * c + 1];
+  } else {
+    const double cn = d.lam[2 * c], cf = d.lam[2 * c + 1];
+    /* bounceB: closing velocity ((-va + (-wa) z× ra) + vb) + wb z× rb */
+    const double nwa = -v[2];
+    const double cvx = ((-v[0] + (-(nwa * cc.ray))) + v[3]) + (-(v[5] * cc.rby));
+    const double cvy = ((-v[1] + nwa * cc.rax) + v[4]) + v[5] * cc.rbx;
+    const double tb = cc.e * (cvx * cc.rnx + cvy * cc.rny);
+    const double bounce = 0.0 <= tb ? 0.0 : tb;
+    const double ln_new = (-(dot6(j_n, v) + (cc.bn + bounce))) / cc.mcn;
+    const double lf_new = (-(dot6(j_f, v) + 0.0)) / cc.mcf;
+    const double neg_cn = -cn;
+    ln_apply = ln_new <= neg_cn ? neg_cn : ln_new;
+    const double ln_cache = cn + ln_apply;
+    const double thr = ln_cache * cc.mu;
+    const double acc = cf + lf_new;
+    const double acc2 = acc > thr ? thr : (acc < -thr ? -thr : acc);
+    lf_apply = acc2 - cf;
+    d.lam[2 * c] = ln_cache;
+    d.lam[2 * c + 1] = acc2;
+  }
+  apply_impulse(j_n, ln_apply, v, m);
+  apply_impulse(j_f, lf_apply, v, m);
+  if (!(d.flags[ga] & kFlagStatic)) {
+    d.vx[ga] = v[0];
+    d.vy[ga] = v[1];
+    d.w[ga] = v[2];
+  }
+  if (!(d.flags[gb] & kFlagStatic)) {
+    d.vx[gb] = v[3];
+    d.vy[gb] = v[4];
+    d.w[gb] = v[5];
+  }
+}
+
+/* One CTA per solver group: applyExternal (World.hs:156-158, constantAccel
+ * External.hs:23-28) on the group's bodies, then every dependency level in
+ * order with a block barrier between levels. */
+__global__ void k_solve(Dev d, int iterations, int external, double ax, double ay, double dt) {
+  if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
+  const int grp = blockIdx.x;
+  const int w0 = d.group_world_off[grp], w1 = d.group_world_off[grp + 1];
+  if (external) {
+    const int b0 = d.world_body_off[w0], b1 = d.world_body_off[w1];
+    for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
+      if (!(0.0 == d.iml[g])) {
+        d.vx[g] = d.vx[g] + ax * dt;
+        d.vy[g] = d.vy[g] + ay * dt;
+      }
+    }
+  }
+  __syncthreads();
+  const int depth = d.group_depth[grp];
+  if (depth == 0) return;
+  const size_t ibase = (size_t)(iterations + 1) * d.world_contact_off[w0];
+  const int32_t* ends = d.ihist + ibase;
+  const uint32_t* items = d.isorted + ibase;
+  int lo = 0;
+  for (int lvl = 0; lvl < depth; ++lvl) {
+    const int hi = ends[lvl];
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) solve_item(d, items[k]);
+    lo = hi;
+    __syncthreads();
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* scans                                                                      */
+/* ------------------------------------------------------------------------ */
+
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 8;
+constexpr int kScanTile = kScanThreads * kScanPerThread;
+
+/* Tile sums of in[0..n) (n read from *n_dev when non-null, capped at n_cap). */
+__global__ void k_scan_tiles(const int32_t* in, int n_cap, const unsigned long long* n_dev,
+                             int32_t* tile_sums) {
+  __shared__ int32_t s[32];
+  const int n = n_dev ? (int)min((unsigned long long)n_cap, *n_dev) : n_cap;
+  const int base = blockIdx.x * kScanTile;
+  int sum = 0;
+  for (int k = 0; k < kScanPerThread; ++k) {
+    const int idx = base + k * kScanThreads + threadIdx.x;
+    if (idx < n) sum += in[idx];
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int k = 0; k < kScanThreads / 32; ++k) t += s[k];
+    tile_sums[blockIdx.x] = t;
+  }
+}
+
+/* Exclusive scan of the tile sums (one block). */
+__global__ void k_scan_tile_sums(int32_t* tile_sums, int n_tiles) {
+  __shared__ int32_t s[32];
+  block_exclusive_scan(tile_sums, n_tiles, s);
+}
+
+/* out[k] = exclusive prefix of in; out[n] = total. */
+__global__ void k_scan_apply(const int32_t* in, int n_cap, const unsigned long long* n_dev,
+                             const int32_t* tile_sums, int32_t* out) {
+  __shared__ int32_t s_vals[kScanTile];
+  __shared__ int32_t s_scan[32];
+  const int n = n_dev ? (int)min((unsigned long long)n_cap, *n_dev) : n_cap;
+  const int base = blockIdx.x * kScanTile;
+  for (int k = threadIdx.x; k < kScanTile; k += kScanThreads) {
+    const int idx = base + k;
+    s_vals[k] = idx < n ? in[idx] : 0;
+  }
+  __syncthreads();
+  /* per-thread serial over a contiguous run, then block scan of run totals */
+  const int r0 = threadIdx.x * kScanPerThread;
+  int run = 0;
+  for (int k = 0; k < kScanPerThread; ++k) run += s_vals[r0 + k];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_scan[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int ws = lane < kScanThreads / 32 ? s_scan[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < kScanThreads / 32) s_scan[lane] = ws;
+  }
+  __syncthreads();
+  int prefix = tile_sums[blockIdx.x] + (wid > 0 ? s_scan[wid - 1] : 0) + incl - run;
+  for (int k = 0; k < kScanPerThread; ++k) {
+    const int idx = base + r0 + k;
+    if (idx <= n) out[idx] = prefix;
+    prefix += s_vals[r0 + k];
+  }
+}
+
+}  // namespace shapes

@@ -1,0 +1,262 @@
+"""Seeded synthetic scenes for the workloads the step is measured and tested on.
+
+The reference ships demo scenes (shapes/src/Physics/Scenes/Stacks.hs) but no
+benchmark dataset; these generators build worlds with the body counts, shapes
+and parameter ranges of the five workload definitions.  Where a definition is
+silent the reference's own scene defaults are used: friction 0.2, bounce 0
+(Scenes/Stacks.hs:22-28) and ContactBehavior (baumgarte 0.01, slop 0.02)
+(Scenes/Stacks.hs:87-88).  Every generator takes a seed for
+``numpy.random.default_rng`` (PCG64).
+
+A scene is a dict with
+  world_body_offsets  int32[W+1]
+  bodies              dict of ten float64[N] arrays (shapes_bodies fields)
+  vert_offsets        int32[N+1]
+  local_xy            float64[V, 2]  (counter-clockwise hull vertices)
+  config              dict(dt, baumgarte, slop, accel, iterations, steps)
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from ._lib import BODY_FIELDS
+
+DEFAULT_MU = 0.2
+DEFAULT_BOUNCE = 0.0
+DEFAULT_BAUMGARTE = 0.01
+DEFAULT_SLOP = 0.02
+
+
+def to_inv_mass(m: float) -> float:
+    """toInvMass2 (Constraint.hs:79-83): 0 stays 0 (infinite mass)."""
+    return 0.0 if m == 0.0 else 1.0 / m
+
+
+def rectangle_vertices(w: float, h: float) -> np.ndarray:
+    """rectangleVertices (ConvexHull.hs:135-145): CCW from (+w/2, +h/2)."""
+    w2, h2 = w / 2.0, h / 2.0
+    return np.array([[w2, h2], [-w2, h2], [-w2, -h2], [w2, -h2]], dtype=np.float64)
+
+
+def polygon_mass(xy: np.ndarray, density: float = 1.0) -> tuple[float, float]:
+    """Area and polar moment about the local origin of a CCW polygon."""
+    x, y = xy[:, 0], xy[:, 1]
+    x1, y1 = np.roll(x, -1), np.roll(y, -1)
+    cr = x * y1 - x1 * y
+    area = 0.5 * cr.sum()
+    inertia = (cr * (x * x + x * x1 + x1 * x1 + y * y + y * y1 + y1 * y1)).sum() / 12.0
+    return float(density * area), float(density * inertia)
+
+
+def perturbed_polygon(rng, nv: int, radius: float, jitter: float = 0.1) -> np.ndarray:
+    """Regular polygon with each vertex radius scaled by U[1-jitter, 1+jitter]."""
+    ang = 2.0 * np.pi * np.arange(nv) / nv
+    r = radius * rng.uniform(1.0 - jitter, 1.0 + jitter, size=nv)
+    return np.stack([r * np.cos(ang), r * np.sin(ang)], axis=1)
+
+
+class SceneBuilder:
+    """Accumulates worlds of hull bodies into flat SoA arrays."""
+
+    def __init__(self):
+        self.rows = {f: [] for f in BODY_FIELDS}
+        self.verts: list[np.ndarray] = []
+        self.world_off = [0]
+
+    def add(self, xy, pos, rot=0.0, vel=(0.0, 0.0), rot_vel=0.0, mass=None, inertia=None,
+            mu=DEFAULT_MU, bounce=DEFAULT_BOUNCE, static=False):
+        xy = np.asarray(xy, dtype=np.float64)
+        if static:
+            iml = imr = 0.0
+        else:
+            m, i = polygon_mass(xy)
+            if mass is not None:
+                m = mass
+            if inertia is not None:
+                i = inertia
+            iml, imr = to_inv_mass(m), to_inv_mass(i)
+        vals = dict(vel_x=vel[0], vel_y=vel[1], rot_vel=rot_vel, pos_x=pos[0], pos_y=pos[1], rot=rot,
+                    inv_mass_lin=iml, inv_mass_rot=imr, mu=mu, bounce=bounce)
+        for f in BODY_FIELDS:
+            self.rows[f].append(float(vals[f]))
+        self.verts.append(xy)
+
+    def end_world(self):
+        self.world_off.append(len(self.verts))
+
+    def build(self, **config) -> dict:
+        if self.world_off[-1] != len(self.verts):
+            self.end_world()
+        vo = np.zeros(len(self.verts) + 1, dtype=np.int32)
+        vo[1:] = np.cumsum([len(v) for v in self.verts])
+        return dict(
+            world_body_offsets=np.asarray(self.world_off, dtype=np.int32),
+            bodies={f: np.asarray(v, dtype=np.float64) for f, v in self.rows.items()},
+            vert_offsets=vo,
+            local_xy=np.concatenate(self.verts, axis=0),
+            config=config,
+        )
+
+
+def box_grid_world(b: SceneBuilder, rng, cols=20, rows=20, spacing=1.05, bottom=0.55, jitter=0.05,
+                   rot_jitter=0.1, slab=(100.0, 1.0), slab_y=-0.5):
+    """A static slab then cols x rows unit squares (mass 1, I = 1/6), column by
+    column bottom to top like Stacks.stacks (Scenes/Stacks.hs:46-56)."""
+    b.add(rectangle_vertices(*slab), (0.0, slab_y), static=True)
+    left = -spacing * (cols - 1) / 2.0
+    sq = rectangle_vertices(1.0, 1.0)
+    for c in range(cols):
+        for r in range(rows):
+            x = left + c * spacing + rng.uniform(-jitter, jitter)
+            y = bottom + r * spacing + rng.uniform(-jitter, jitter)
+            th = rng.uniform(-rot_jitter, rot_jitter)
+            b.add(sq, (x, y), th, mass=1.0, inertia=1.0 / 6.0)
+    b.end_world()
+
+
+def single_world_boxes(seed: int = 0, cols: int = 20, rows: int = 20, steps: int = 600) -> dict:
+    """Single world: static 100x1 slab + 20x20 unit squares at spacing 1.05,
+    jitter +-0.05, rotation +-0.1 rad; g = (0,-9.8), dt = 1/60, 4 sweeps."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    box_grid_world(b, rng, cols, rows)
+    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
+                   iterations=4, steps=steps)
+
+
+def polygon_field(seed: int = 1, n: int = 65536, extent: float = 512.0, rmin=0.3, rmax=1.0) -> dict:
+    """Single world of n convex polygons (3-8 vertices, radius U[rmin,rmax],
+    vertex radii +-10%, random rotation) with centres uniform in extent^2.
+    Contact generation only."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    nvs = rng.integers(3, 9, size=n)
+    rs = rng.uniform(rmin, rmax, size=n)
+    ths = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    cs = rng.uniform(0.0, extent, size=(n, 2))
+    for k in range(n):
+        xy = perturbed_polygon(rng, int(nvs[k]), float(rs[k]))
+        b.add(xy, (cs[k, 0], cs[k, 1]), ths[k])
+    b.end_world()
+    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
+                   iterations=0, steps=1)
+
+
+def column_world(b: SceneBuilder, rng, n_bodies: int, gap=0.05, x_jitter=0.05, rot_jitter=0.02,
+                 slab=(40.0, 1.0)):
+    """Static slab, then n_bodies-1 square boxes of side U[0.5, 2] stacked in a
+    column with a small gap and seeded jitter."""
+    b.add(rectangle_vertices(*slab), (0.0, -slab[1] / 2.0), static=True)
+    y = gap
+    for _ in range(n_bodies - 1):
+        s = rng.uniform(0.5, 2.0)
+        m = s * s
+        b.add(rectangle_vertices(s, s), (rng.uniform(-x_jitter, x_jitter), y + s / 2.0),
+              rng.uniform(-rot_jitter, rot_jitter), mass=m, inertia=m * s * s / 6.0)
+        y += s + gap
+    b.end_world()
+
+
+def batched_columns(seed: int = 2, n_worlds: int = 4096, nmin: int = 8, nmax: int = 512, steps: int = 300) -> dict:
+    """n_worlds independent worlds, body count log-uniform in [nmin, nmax]
+    (slab included), boxes of side U[0.5,2] dropped in a column; dt = 1/60,
+    8 sweeps, 300 steps."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    counts = np.rint(np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=n_worlds))).astype(int)
+    for nb in counts:
+        column_world(b, rng, int(nb))
+    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
+                   iterations=8, steps=steps)
+
+
+def mixed_pile_world(b: SceneBuilder, rng, n_bodies: int, cols: int = 16, size=(0.4, 1.5), mu=(0.2, 0.8),
+                     slab_w: float = 60.0):
+    """Static slab, then n_bodies-1 boxes and 3-8 vertex polygons of size
+    U[size] and friction U[mu], dropped from a jittered grid."""
+    b.add(rectangle_vertices(slab_w, 1.0), (0.0, -0.5), static=True)
+    pitch = 2.0 * size[1] + 0.1
+    left = -pitch * (cols - 1) / 2.0
+    for k in range(n_bodies - 1):
+        c, r = k % cols, k // cols
+        s = rng.uniform(*size)
+        if rng.uniform() < 0.5:
+            xy = rectangle_vertices(s, s * rng.uniform(0.6, 1.0))
+        else:
+            xy = perturbed_polygon(rng, int(rng.integers(3, 9)), s / 2.0 * 1.2)
+        pos = (left + c * pitch + rng.uniform(-0.1, 0.1), pitch * (r + 0.5) + rng.uniform(-0.1, 0.1))
+        b.add(xy, pos, rng.uniform(0.0, 2.0 * np.pi), mu=rng.uniform(*mu))
+    b.end_world()
+
+
+def batched_mixed(seed: int = 3, n_worlds: int = 1024, n_bodies: int = 256, steps: int = 300) -> dict:
+    """n_worlds worlds of n_bodies mixed boxes and polygons (sizes U[0.4,1.5],
+    friction U[0.2,0.8])."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    for _ in range(n_worlds):
+        mixed_pile_world(b, rng, n_bodies)
+    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
+                   iterations=8, steps=steps)
+
+
+def container_world(seed: int = 4, n: int = 262144, width: float = 1024.0, rmin=0.3, rmax=1.0,
+                    steps: int = 2000) -> dict:
+    """One world: a static U container `width` wide (floor + two walls) holding
+    n mixed convex polygons (3-8 vertices, radius U[rmin,rmax]) dropped from a
+    jittered grid; dt = 1/120."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    b.add(rectangle_vertices(width + 4.0, 2.0), (0.0, -1.0), static=True)
+    wall_h = 2.0 * (2.2 * rmax) * n / (width / (2.2 * rmax)) + 20.0
+    b.add(rectangle_vertices(2.0, wall_h), (-(width / 2.0 + 1.0), wall_h / 2.0), static=True)
+    b.add(rectangle_vertices(2.0, wall_h), (width / 2.0 + 1.0, wall_h / 2.0), static=True)
+    pitch = 2.2 * rmax + 0.05
+    cols = int(width // pitch)
+    left = -pitch * (cols - 1) / 2.0
+    for k in range(n - 3):
+        c, r = k % cols, k // cols
+        xy = perturbed_polygon(rng, int(rng.integers(3, 9)), float(rng.uniform(rmin, rmax)))
+        b.add(xy, (left + c * pitch + rng.uniform(-0.02, 0.02), pitch * (r + 0.5)), rng.uniform(0, 2 * np.pi))
+    b.end_world()
+    return b.build(dt=1.0 / 120.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
+                   iterations=4, steps=steps)
+
+
+def stacks_make_scene(dims=(30, 30), spacing=0.0) -> dict:
+    """Stacks.makeScene (Scenes/Stacks.hs:110-113): the reference's own bench
+    scene - an 18x1 static floor at (0,-6) then dims[0] columns of dims[1]
+    0.2x0.2 boxes (mass 2, inertia 1), friction 0.2, bounce 0, gravity (0,-2),
+    contactBehavior (0.01, 0.02), run at dt 0.01 (shapes/bench/Main.hs:19-22)."""
+    b = SceneBuilder()
+    b.add(rectangle_vertices(18.0, 1.0), (0.0, -6.0), static=True)
+    w, h = 0.2, 0.2
+    n_w, n_h = dims
+    leftmost = 0.0 - (w * float(n_w - 1) / 2.0)
+    left = leftmost
+    for _ in range(n_w):
+        y = -4.5
+        for _ in range(n_h):
+            b.add(rectangle_vertices(w, h), (left, y), mass=2.0, inertia=1.0)
+            y = y + (h + spacing)
+        left = left + w
+    b.end_world()
+    return b.build(dt=0.01, baumgarte=0.01, slop=0.02, accel=(0.0, -2.0), iterations=2, steps=10)
+
+
+def subset_worlds(scene: dict, worlds) -> dict:
+    """A scene holding only the given worlds of `scene` (in the given order)."""
+    off = scene["world_body_offsets"]
+    vo = scene["vert_offsets"]
+    b_idx = np.concatenate([np.arange(off[w], off[w + 1]) for w in worlds])
+    new_off = np.zeros(len(worlds) + 1, dtype=np.int32)
+    new_off[1:] = np.cumsum([off[w + 1] - off[w] for w in worlds])
+    counts = vo[b_idx + 1] - vo[b_idx]
+    new_vo = np.zeros(len(b_idx) + 1, dtype=np.int32)
+    new_vo[1:] = np.cumsum(counts)
+    xy = np.concatenate([scene["local_xy"][vo[b]:vo[b + 1]] for b in b_idx], axis=0)
+    return dict(world_body_offsets=new_off,
+                bodies={f: scene["bodies"][f][b_idx].copy() for f in BODY_FIELDS},
+                vert_offsets=new_vo, local_xy=xy, config=dict(scene["config"]))

@@ -1,0 +1,274 @@
+"""CUDA step vs the CPU oracle, through the C ABI, on seeded scenes.
+
+Contract: pairs and contact keys identical; every binary64 result (poses,
+contact points/normals/depths, velocities, positions, Lagrangians)
+bit-identical.  The workload definitions ask for 1e-12 (manifolds) and 1e-9
+relative (trajectories); bit identity is stronger and is what is asserted,
+with the relative error also checked against 1e-9 for the long run.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from shapes_gb300 import _lib, scenes
+from tests.parity import (STATE_FIELDS, assert_bits_equal, batch_from_scene, compare_bodies, compare_collision,
+                          config_of, max_rel_err, oracle_worlds, step_oracles)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build(built):
+    import torch
+
+    torch.cuda.set_device(0)
+
+
+def test_pose_bit_exact():
+    for sc in (scenes.single_world_boxes(), scenes.stacks_make_scene(), scenes.polygon_field(n=3000, extent=60.0)):
+        b = batch_from_scene(sc)
+        xy, nxy = b.get_shapes()
+        ow = O.world_from_scene(sc)
+        wxy, wnxy = ow.shapes()
+        assert_bits_equal(xy, wxy, "world vertices")
+        assert_bits_equal(nxy, wnxy, "edge normals")
+        b.close()
+
+
+@pytest.mark.parametrize("name", ["boxes", "stacks", "polygons"])
+def test_collide_matches_oracle(name):
+    sc = {"boxes": lambda: scenes.single_world_boxes(),
+          "stacks": lambda: scenes.stacks_make_scene(),
+          "polygons": lambda: scenes.polygon_field(n=4096, extent=64.0)}[name]()
+    b = batch_from_scene(sc)
+    b.collide()
+    ow = O.world_from_scene(sc)
+    ow.collide()
+    compare_collision(b, [ow], name)
+    assert b.stats()["contacts"] > 0
+    b.close()
+
+
+def test_collide_65536_polygons():
+    """Broadphase + SAT at scale: 65,536 polygons in a 512x512 box."""
+    sc = scenes.polygon_field()
+    b = batch_from_scene(sc)
+    b.collide()
+    ow = O.world_from_scene(sc)
+    ow.collide()
+    compare_collision(b, [ow], "65536 polygons")
+    st = b.stats()
+    assert st["pairs"] > 10000 and st["contacts"] > 10000, st
+    b.close()
+
+
+def test_single_world_boxes_trajectory():
+    """400 boxes + slab, 4 sweeps, 600 steps: bit-identical to the oracle."""
+    sc = scenes.single_world_boxes()
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    for chunk in (1, 49, 150, 400):
+        b.step(cfg, chunk)
+        step_oracles(ow, sc, chunk)
+        compare_bodies(b, ow, sc, f"after chunk {chunk}")
+    compare_collision(b, ow, "last step")
+    got = b.get_bodies()
+    want = ow[0].bodies()
+    for f in STATE_FIELDS:
+        assert max_rel_err(got[f], want[f]) <= 1e-9
+    gk, gl, _ = b.get_cache()
+    wk, wl = ow[0].cache()
+    assert np.array_equal(gk, wk)
+    assert_bits_equal(gl, wl, "cache lagrangians")
+    b.close()
+
+
+def test_reference_bench_scene():
+    """Stacks.makeScene (30,30) 0 at dt 0.01, 2 sweeps (shapes/bench/Main.hs:19-22)."""
+    sc = scenes.stacks_make_scene()
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 10)
+    step_oracles(ow, sc, 10)
+    compare_bodies(b, ow, sc, "stacks 10 steps")
+    b.step(cfg, 150)
+    step_oracles(ow, sc, 150)
+    compare_bodies(b, ow, sc, "stacks 160 steps")
+    compare_collision(b, ow, "stacks")
+    b.close()
+
+
+def test_batched_worlds_match_single_world_runs():
+    big = scenes.batched_columns(n_worlds=256)
+    rng = np.random.default_rng(5)
+    pick = sorted(rng.choice(256, size=40, replace=False).tolist())
+    sc = scenes.subset_worlds(big, pick)
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 30)
+    step_oracles(ow, sc, 30)
+    compare_bodies(b, ow, sc, "batched 30")
+    b.step(cfg, 90)
+    step_oracles(ow, sc, 90)
+    compare_bodies(b, ow, sc, "batched 120")
+    compare_collision(b, ow, "batched")
+    b.close()
+
+
+def test_mixed_polygon_worlds():
+    sc = scenes.batched_mixed(n_worlds=6, n_bodies=96)
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 120)
+    step_oracles(ow, sc, 120)
+    compare_bodies(b, ow, sc, "mixed")
+    compare_collision(b, ow, "mixed")
+    b.close()
+
+
+@pytest.mark.parametrize("target,threads", [(1, 32), (64, 64), (100000, 256)])
+def test_solver_packing_does_not_change_results(target, threads):
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
+    b = batch_from_scene(sc)
+    b.set_launch(target, threads)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 40)
+    step_oracles(ow, sc, 40)
+    compare_bodies(b, ow, sc, f"packing {target}/{threads}")
+    b.close()
+
+
+def test_cache_checkpoint_resume():
+    sc = scenes.stacks_make_scene((8, 8))
+    cfg = config_of(sc)
+    a = batch_from_scene(sc)
+    a.step(cfg, 140)
+    b = batch_from_scene(sc)
+    b.step(cfg, 120)
+    keys, lam, wc = b.get_cache()
+    st = b.get_bodies()
+    c = _lib.Batch(sc["world_body_offsets"], st, sc["vert_offsets"], sc["local_xy"])
+    c.set_cache(keys, lam, wc)
+    c.step(cfg, 20)
+    ga, gc = a.get_bodies(), c.get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(ga[f], gc[f], f"resume {f}")
+    for h in (a, b, c):
+        h.close()
+
+
+def test_warm_start_off_and_no_gravity():
+    sc = scenes.stacks_make_scene((6, 6))
+    for warm, ext in ((False, True), (True, False)):
+        b = batch_from_scene(sc)
+        ow = oracle_worlds(sc)
+        b.step(config_of(sc, warm_start=warm, external=ext), 130)
+        step_oracles(ow, sc, 130, warm_start=warm, external=ext)
+        compare_bodies(b, ow, sc, f"warm={warm} ext={ext}")
+        b.close()
+
+
+def test_iteration_counts():
+    sc = scenes.stacks_make_scene((5, 5))
+    for it in (0, 1, 3, 8):
+        b = batch_from_scene(sc)
+        ow = oracle_worlds(sc)
+        b.step(config_of(sc, iterations=it), 130)
+        step_oracles(ow, sc, 130, iterations=it)
+        compare_bodies(b, ow, sc, f"iterations={it}")
+        b.close()
+
+
+def test_buffer_regrowth_is_exact():
+    """60 overlapping bodies: more pairs than the initial capacity; the call
+    retries with larger buffers and still matches the oracle."""
+    rng = np.random.default_rng(3)
+    bld = scenes.SceneBuilder()
+    bld.add(scenes.rectangle_vertices(20.0, 1.0), (0.0, -0.5), static=True)
+    for _ in range(60):
+        bld.add(scenes.perturbed_polygon(rng, 6, 1.0), tuple(rng.uniform(-0.3, 0.3, 2) + [0, 2.0]),
+                rng.uniform(0, 6.28))
+    sc = bld.build(dt=1 / 60, baumgarte=0.01, slop=0.02, accel=(0, -9.8), iterations=4, steps=1)
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    b.step(config_of(sc), 3)
+    step_oracles(ow, sc, 3)
+    assert b.stats()["retries"] >= 1 or b.stats()["pairs"] <= 1024
+    compare_bodies(b, ow, sc, "regrowth")
+    compare_collision(b, ow, "regrowth")
+    b.close()
+
+
+def test_determinism():
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=32), list(range(32)))
+    out = []
+    for _ in range(2):
+        b = batch_from_scene(sc)
+        b.step(config_of(sc), 50)
+        out.append(b.get_bodies())
+        b.close()
+    for f in STATE_FIELDS:
+        assert_bits_equal(out[0][f], out[1][f], f)
+
+
+def test_invalid_inputs_are_rejected():
+    sc = scenes.single_world_boxes(cols=2, rows=2)
+    bad = dict(sc)
+    xy = sc["local_xy"].copy()
+    xy[4:8] = xy[4:8][::-1]  # second body clockwise
+    with pytest.raises(_lib.ShapesError) as e:
+        _lib.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], xy)
+    assert e.value.status == _lib.SHAPES_E_NONCONVEX
+    bodies = {k: v.copy() for k, v in sc["bodies"].items()}
+    bodies["pos_x"][1] = np.nan
+    with pytest.raises(_lib.ShapesError) as e:
+        _lib.Batch(sc["world_body_offsets"], bodies, sc["vert_offsets"], sc["local_xy"])
+    assert e.value.status == _lib.SHAPES_E_NAN
+    kinds = np.zeros(len(sc["bodies"]["pos_x"]), dtype=np.uint8)
+    kinds[2] = 1
+    with pytest.raises(_lib.ShapesError) as e:
+        _lib.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], sc["local_xy"], kinds)
+    assert e.value.status == _lib.SHAPES_E_UNSUPPORTED
+    b = batch_from_scene(bad)
+    cfg = config_of(sc)
+    cfg.iterations = -1
+    with pytest.raises(_lib.ShapesError):
+        b.step(cfg, 1)
+    b.close()
+
+
+def test_engine_api_mirror():
+    """The Physics.Engine.Main mirror API (init_engine / step_world) on a
+    hand-built world equals the oracle."""
+    import shapes_gb300 as S
+
+    objs = [S.make_world_obj(S.make_physical_obj((0, 0), 0, (0, -6), 0, (0, 0)), 0.2, 0, S.make_rectangle_hull(18, 1))]
+    for k in range(5):
+        objs.append(S.make_world_obj(S.make_physical_obj((-1, 0), 0, (8, -4.5 + 2 * k), 0, (2, 1)), 0.2, 0,
+                                     S.make_rectangle_hull(2, 2)))
+    world = S.make_world(objs)
+    scene = S.engine.Scene(world, S.make_constant_accel((0, -2)), S.ContactBehavior(0.01, 0.02))
+    st = S.init_engine(scene)
+    cfg = S.EngineConfig(0.01, scene.contact_beh)
+    S.step_world(st, cfg, 200)
+    got = st.batch.get_bodies()
+    n = len(objs)
+    bodies = {f: np.zeros(n) for f in _lib.BODY_FIELDS}
+    vo = [0]
+    for k, o in enumerate(objs):
+        p = o.phys_obj
+        for f, v in zip(_lib.BODY_FIELDS, (p.vel[0], p.vel[1], p.rot_vel, p.pos[0], p.pos[1], p.rot, p.inv_mass[0],
+                                            p.inv_mass[1], o.mu, o.bounce)):
+            bodies[f][k] = v
+        vo.append(vo[-1] + 4)
+    ow = O.OracleWorld(bodies, np.array(vo), np.concatenate([o.shape.vertices for o in objs]))
+    ow.step(0.01, 0.01, 0.02, (0, -2), 2, nsteps=200)
+    want = ow.bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(got[f], want[f], f)
+    st.batch.close()

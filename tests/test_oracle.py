@@ -1,0 +1,190 @@
+"""The oracle pinned against the reference's fixtures (CPU only).
+
+K1/K2/K3 are known answers for the reference's own bench/test fixtures
+(tests/golden/kat.json, derived by hand from the reference source); the Grid
+restatement checks that the step's Grid broadphase (Grid.hs) and the Aabb
+pair list the oracle produces are the same list.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from shapes_gb300 import scenes
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib
+
+
+def kat():
+    return json.loads((GOLDEN / "kat.json").read_text())
+
+
+def box(center, size):
+    v = scenes.rectangle_vertices(*size)
+    return v + np.asarray(center)
+
+
+def test_k1_solve_constraint(O):
+    k = kat()["K1"]
+    a, b = O.solve_constraint(k["j"], k["b"], k["a"], k["b_obj"])
+    assert list(a[:3]) == k["a_after"]
+    assert list(b[:3]) == k["b_after"]
+
+
+def test_k2_box_contact(O):
+    k = kat()["K2"]
+    keys, vals = O.hull_contacts(box(**k["a"]), box(**k["b"]))
+    assert len(keys) == len(k["contacts"])
+    for got_k, got_v, want in zip(keys, vals, k["contacts"]):
+        assert list(got_k[:2]) == want["features"]
+        assert got_k[2] == want["flip"]
+        assert list(got_v[:2]) == want["normal"]
+        assert list(got_v[2:4]) == want["point"]
+        assert got_v[4] == want["depth"]
+
+
+def test_k3_unordered_pairs_count(O):
+    for n in range(0, kat()["K3"]["n_max"] + 1):
+        assert O.unordered_pairs_count(n) == n * (n - 1) // 2
+
+
+def test_rectangle_is_ccw():
+    v = scenes.rectangle_vertices(2.0, 1.0)
+    x, y = v[:, 0], v[:, 1]
+    area2 = np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y)
+    assert area2 > 0
+
+
+def _ulp_err(got, want):
+    return abs(got - want) / math.ulp(abs(want)) if want != 0 else abs(got)
+
+
+def test_sincos_accuracy(O):
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(-4, 4, 20000), rng.uniform(-1e4, 1e4, 20000),
+                         rng.uniform(-1e-6, 1e-6, 2000), [0.0, -0.0, math.pi / 2, math.pi, 1e6]])
+    s, c = O.sincos(xs)
+    worst = 0.0
+    same = 0
+    for x, si, ci in zip(xs, s, c):
+        ws, wc = math.sin(x), math.cos(x)
+        worst = max(worst, _ulp_err(si, ws), _ulp_err(ci, wc))
+        same += int(si == ws) + int(ci == wc)
+    assert worst <= 1.0, worst
+    assert same / (2 * len(xs)) > 0.95
+    assert math.copysign(1.0, O.sincos(np.array([-0.0]))[0][0]) == -1.0
+    s, c = O.sincos(np.array([math.inf, math.nan, 1e300]))
+    assert np.isnan(s).all() and np.isnan(c).all()
+
+
+def grid_culled_keys(world_xy, vert_off, static):
+    """Grid.toGrid + Grid.culledKeys (Broadphase/Grid.hs:67-110) restated:
+    gridAxes = GridAxis 20 1 (-10) on both axes (Engine/Main.hs:40-41)."""
+    n = len(vert_off) - 1
+    boxes = []
+    for i in range(n):
+        pts = world_xy[vert_off[i]:vert_off[i + 1]]
+        x0 = x1 = pts[0, 0]
+        y0 = y1 = pts[0, 1]
+        for x, y in pts[1:]:
+            x0 = x0 if x0 < x else x
+            x1 = x1 if x1 > x else x
+            y0 = y0 if y0 < y else y
+            y1 = y1 if y1 > y else y
+        boxes.append((x0, x1, y0, y1))
+
+    def axial(v):
+        return math.floor((v - (-10.0)) / 1.0)
+
+    cells = {}
+    for key, (x0, x1, y0, y1) in enumerate(boxes):
+        for cx in range(axial(x0), axial(x1) + 1):
+            for cy in range(axial(y0), axial(y1) + 1):
+                cells.setdefault(cx + cy * 20, {})[key] = (static[key], boxes[key])
+    out = []
+    for sq in cells.values():
+        desc = sorted(sq.items(), key=lambda kv: -kv[0])
+        for a in range(len(desc)):
+            for b in range(a + 1, len(desc)):
+                (ka, (sa, ba)), (kb, (sb, bb)) = desc[a], desc[b]
+                if sa and sb:
+                    continue
+                if not (bb[0] > ba[1] or bb[1] < ba[0]) and not (bb[2] > ba[3] or bb[3] < ba[2]):
+                    out.append((ka, kb))
+    return sorted(set(out), reverse=True)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_grid_broadphase_equals_aabb_pairs(O, seed):
+    rng = np.random.default_rng(seed)
+    b = scenes.SceneBuilder()
+    b.add(scenes.rectangle_vertices(30.0, 1.0), (0.0, -5.0), static=True)
+    b.add(scenes.rectangle_vertices(1.0, 12.0), (-9.0, 0.0), static=True)
+    for _ in range(150):
+        xy = scenes.perturbed_polygon(rng, int(rng.integers(3, 9)), float(rng.uniform(0.3, 1.5)))
+        b.add(xy, tuple(rng.uniform(-14.0, 14.0, 2)), rng.uniform(0, 2 * np.pi))
+    sc = b.build()
+    w = O.world_from_scene(sc)
+    w.collide()
+    got = [tuple(p) for p in w.pairs()]
+    xy, _ = w.shapes()
+    static = [(sc["bodies"]["inv_mass_lin"][i] == 0 and sc["bodies"]["inv_mass_rot"][i] == 0)
+              for i in range(len(sc["bodies"]["pos_x"]))]
+    want = grid_culled_keys(xy, sc["vert_offsets"], static)
+    assert got == want
+    assert len(got) > 50
+
+
+def test_pairs_descending_and_contacts_descending(O):
+    sc = scenes.stacks_make_scene((6, 6))
+    w = O.world_from_scene(sc)
+    cfg = sc["config"]
+    w.step(cfg["dt"], cfg["baumgarte"], cfg["slop"], cfg["accel"], cfg["iterations"], nsteps=3)
+    w.collide()
+    p = [tuple(x) for x in w.pairs()]
+    assert p == sorted(p, reverse=True) and all(i > j for i, j in p)
+    k, _ = w.contacts()
+    keys = [tuple(x[:4]) for x in k]
+    assert keys == sorted(keys, reverse=True) and len(set(keys)) == len(keys)
+    ck, _ = w.cache()
+    assert [tuple(x) for x in ck] == sorted([tuple(x) for x in ck], reverse=True)
+
+
+def test_oracle_iterations_two_is_reference_count(O):
+    """N=2 sweeps is the reference's hard-coded count; more sweeps differ."""
+    sc = scenes.stacks_make_scene((4, 4))
+    cfg = sc["config"]
+    runs = []
+    for it in (2, 2, 3):
+        w = O.world_from_scene(sc)
+        w.step(cfg["dt"], cfg["baumgarte"], cfg["slop"], cfg["accel"], it, nsteps=150)
+        runs.append(w.bodies()["vel_y"])
+    assert np.array_equal(runs[0], runs[1])
+    assert not np.array_equal(runs[0], runs[2])
+
+
+def test_warm_start_off_differs_and_cache_roundtrip(O):
+    sc = scenes.stacks_make_scene((5, 5))
+    cfg = sc["config"]
+    args = (cfg["dt"], cfg["baumgarte"], cfg["slop"], cfg["accel"], cfg["iterations"])
+    a = O.world_from_scene(sc)
+    a.step(*args, nsteps=140)
+    b = O.world_from_scene(sc)
+    b.step(*args, nsteps=120)
+    k, lam = b.cache()
+    st = b.bodies()
+    c = O.OracleWorld(st, sc["vert_offsets"], sc["local_xy"])
+    c.set_cache(k, lam)
+    c.step(*args, nsteps=20)
+    for f in ("pos_x", "pos_y", "rot", "vel_x", "vel_y", "rot_vel"):
+        assert np.array_equal(a.bodies()[f], c.bodies()[f])
+    d = O.world_from_scene(sc)
+    d.step(*args, warm_start=False, nsteps=140)
+    assert not np.array_equal(a.bodies()["vel_y"], d.bodies()["vel_y"])
