@@ -82,13 +82,15 @@ typedef struct shapes_config {
   int32_t reserved;   /* must be 0 */
 } shapes_config;
 
-/* Counters of the most recent step or collide call, summed over worlds. */
+/* Counters of the most recent step or collide call, summed over worlds.
+ * pairs and contacts are those of the call's last step; cache_hits,
+ * solver_items and solver_levels are summed over all steps of the call. */
 typedef struct shapes_stats {
   int64_t pairs;
   int64_t contacts;
   int64_t cache_hits;
   int64_t solver_items;  /* warm-start applications + sweep updates */
-  int64_t solver_levels; /* sum over solver groups of dependency levels */
+  int64_t solver_levels; /* sum over steps and solver groups of dependency levels */
   int64_t retries;       /* buffer regrowths during the last call */
 } shapes_stats;
 
@@ -122,7 +124,8 @@ int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps)
  * does (shapes-demo/src/Physics/Demo/IOWorld.hs:74-81). */
 int shapes_batch_collide(shapes_batch* b);
 
-/* Body state read/write.  set re-poses the shapes and keeps the cache.
+/* Body state read/write.  set validates on the device (SHAPES_E_NAN leaves the
+ * state untouched), re-poses the shapes and keeps the cache.
  * Replaces: readPhysObj / updatePhysObj (World.hs:93-97). */
 int shapes_batch_get_bodies(shapes_batch* b, shapes_bodies* out);
 int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in);
@@ -166,7 +169,11 @@ int shapes_batch_set_cache(shapes_batch* b, const int32_t* world_counts, const i
 
 int shapes_batch_get_stats(shapes_batch* b, shapes_stats* out);
 
-/* Solver packing: worlds per solver CTA and CTA size.  0 = automatic. */
+/* Solver packing.  Worlds are sorted by size and packed into groups, one warp
+ * per group; target_bodies_per_group > 0 closes a group once it holds that many
+ * bodies (0 = automatic: about one warp of updates per dependency level);
+ * threads = warps per CTA x 32, at most 256 (0 = 128).  Results do not depend
+ * on the packing. */
 int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads);
 
 /* Run this handle's device work on a caller-owned CUDA stream (a

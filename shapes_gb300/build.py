@@ -17,13 +17,15 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "libshapes_gpu.so"
+PROBE_LIB = OUT_DIR / "libshapes_probe.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-shared"]
 
 SOURCES = [CSRC / "shapes_gpu.cu"]
-HEADERS = [CSRC / "step_kernels.cuh", CSRC / "shapes_sincos.h", HERE.parent / "include" / "shapes_gpu.h"]
+HEADERS = [CSRC / "step_kernels.cuh", CSRC / "fp64_ops.cuh", CSRC / "shapes_sincos.h",
+           HERE.parent / "include" / "shapes_gpu.h"]
 
 
 def nvcc() -> str:
@@ -33,23 +35,34 @@ def nvcc() -> str:
     return cand
 
 
-def needs_build() -> bool:
-    if not LIB.exists():
+def needs_build(lib: Path, sources) -> bool:
+    if not lib.exists():
         return True
-    t = LIB.stat().st_mtime
-    return any(p.stat().st_mtime > t for p in SOURCES + HEADERS + [Path(__file__)])
+    t = lib.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in list(sources) + [Path(__file__)])
+
+
+def _compile(lib: Path, sources, verbose: bool):
+    tmp = lib.with_suffix(".so.tmp")
+    cmd = [nvcc(), *NVCC_FLAGS, "-o", str(tmp), *map(str, sources)]
+    if verbose:
+        print(" ".join(cmd))
+    return subprocess.Popen(cmd), tmp, lib
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compiles the step library and the FP64 probe (in parallel) if stale."""
     OUT_DIR.mkdir(parents=True, exist_ok=True)
-    if not force and not needs_build():
-        return LIB
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *NVCC_FLAGS, "-o", str(tmp), *map(str, SOURCES)]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
+    jobs = []
+    if force or needs_build(LIB, SOURCES + HEADERS):
+        jobs.append(_compile(LIB, SOURCES, verbose))
+    probe_src = [CSRC / "fp64_probe.cu"]
+    if force or needs_build(PROBE_LIB, probe_src + [CSRC / "fp64_ops.cuh"]):
+        jobs.append(_compile(PROBE_LIB, probe_src, verbose))
+    for proc, tmp, lib in jobs:
+        if proc.wait() != 0:
+            raise RuntimeError(f"nvcc failed building {lib.name}")
+        os.replace(tmp, lib)
     return LIB
 
 

@@ -1,0 +1,81 @@
+/*
+ * Exact binary64 helpers that keep work off GB300's narrow FP64 pipe.
+ *
+ * The FP64 pipe retires about 0.05 warp-instructions per clock per SM and
+ * each FP64 instruction (including DSETP comparisons) is charged for all 32
+ * lanes, while integer instructions issue roughly a hundred times faster.
+ * Every helper here returns exactly what the plain IEEE-754 operation it
+ * replaces returns, for every input.
+ */
+#pragma once
+#include <cstdint>
+
+namespace shapes {
+
+/* Order-preserving key of a binary64: for non-NaN a, b,
+ * a < b  <=>  okey(a) < okey(b), and a == b <=> okey(a) == okey(b)
+ * (-0 and +0 map to the same key). */
+__device__ __forceinline__ uint64_t okey(double d) {
+  uint64_t u = (uint64_t)__double_as_longlong(d);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ bool nan_bits(double x) {
+  return ((uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+
+/* a <= b and a < b as IEEE comparisons (false when either is NaN). */
+__device__ __forceinline__ bool f_le(double a, double b) {
+  return !nan_bits(a) && !nan_bits(b) && okey(a) <= okey(b);
+}
+__device__ __forceinline__ bool f_lt(double a, double b) {
+  return !nan_bits(a) && !nan_bits(b) && okey(a) < okey(b);
+}
+
+/* x + 0.0: only -0 changes (to +0); NaN stays NaN. */
+__device__ __forceinline__ double plus_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)(((uint64_t)__double_as_longlong(x) >> 52) & 0x7ff);
+}
+
+/* |x| < 2^500: finite and far from overflow. */
+__device__ __forceinline__ bool small_mag(double x) { return exp_field(x) < 1523; }
+
+/* |x| < 2. */
+__device__ __forceinline__ bool below_two(double x) { return exp_field(x) < 1024; }
+
+/* 2^-500 <= |b| < 2^500: denominators whose reciprocal is used by div_rn. */
+__device__ __forceinline__ bool recip_ok(double b) {
+  const int e = exp_field(b);
+  return e >= 523 && e < 1523;
+}
+
+/* a / b, correctly rounded (round to nearest even), given y = RN(1/b) and
+ * recip_ok(b).  Markstein's theorem (P. Markstein, "IA-64 and Elementary
+ * Functions", 2000, Thm 8.10; the basis of the IA-64 division sequences): if
+ * y is within half an ulp of 1/b and q is within one ulp of a/b, then
+ * r = a - b q is exact when computed with one fused multiply-add, and
+ * RN(q + r y) is the correctly rounded quotient.  q0 = RN(a y) is within one
+ * ulp of a/b.  The fast path is taken when a is a normal number with
+ * 2^-400 <= |a| < 2^400, so nothing overflows or underflows (|q| stays
+ * within 2^+-900 and |r| above 2^-460); zeros, NaN, infinities and extreme
+ * magnitudes use the hardware division, and so does any b outside
+ * recip_ok (signalled by y == 0).  Three dependent FP64 instructions
+ * replace the division's longer sequence.  Explicit __fma_rn: the fused
+ * operations here are part of this algorithm, not contractions of the
+ * reference's expressions. */
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+  const int ea = exp_field(a);
+  if (ea >= 623 && ea < 1423 && __double_as_longlong(y) != 0) {
+    const double q0 = __dmul_rn(a, y);
+    const double r = __fma_rn(-q0, b, a);
+    return __fma_rn(r, y, q0);
+  }
+  return a / b;
+}
+
+}  // namespace shapes

@@ -1,0 +1,151 @@
+/*
+ * FP64 pipe throughput probe, used by bench.py as the denominator of the FP64
+ * roofline (the measured-peaks file has HBM and bf16 figures only).  Eight
+ * independent add/multiply chains per thread, 16 warps per SM, timed with CUDA
+ * events; reports binary64 add/multiply lane-operations per second.
+ */
+#include <cuda_runtime.h>
+
+__global__ void k_fp64_chains(double* out, int iters) {
+  double a0 = threadIdx.x * 1e-3 + 1.0, a1 = a0 + 0.1, a2 = a0 + 0.2, a3 = a0 + 0.3;
+  double a4 = a0 + 0.4, a5 = a0 + 0.5, a6 = a0 + 0.6, a7 = a0 + 0.7;
+  const double b = 1.0000001, c = 0.9999999;
+  for (int i = 0; i < iters; ++i) {
+    a0 = __dadd_rn(a0, b); a1 = __dmul_rn(a1, c); a2 = __dadd_rn(a2, c); a3 = __dmul_rn(a3, b);
+    a4 = __dadd_rn(a4, b); a5 = __dmul_rn(a5, c); a6 = __dadd_rn(a6, c); a7 = __dmul_rn(a7, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+extern "C" int shapes_probe_fp64(double* lane_ops_per_s) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -5;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -5;
+  const int threads = 256, blocks = sms * 2, iters = 20000;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * threads * blocks) != cudaSuccess) return -5;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_chains<<<blocks, threads>>>(d, 64);
+  cudaEventRecord(e0);
+  k_fp64_chains<<<blocks, threads>>>(d, iters);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (err != cudaSuccess || ms <= 0.f) return -5;
+  *lane_ops_per_s = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+  return 0;
+}
+
+/*
+ * Self-checks of the exact binary64 helpers (fp64_ops.cuh) against the
+ * hardware IEEE operations they replace; used by the test suite.
+ */
+#include "fp64_ops.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  /* splitmix64 finaliser (Steele, Lea, Flood 2014) */
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double make_double(unsigned long long sign, int exp, unsigned long long mant) {
+  return __longlong_as_double((long long)((sign << 63) | ((unsigned long long)exp << 52) | (mant & 0xfffffffffffffull)));
+}
+
+/* Operand classes: random mantissas over the whole fast range and beyond it,
+ * all-ones and all-zeros mantissas, mantissas of the form 2^k +- 1, and
+ * numerators built as b * q with short-mantissa q (quotients near exact). */
+__device__ void div_operands(unsigned long long k, unsigned long long seed, double* a, double* b) {
+  const unsigned long long r0 = mix64(k ^ seed), r1 = mix64(r0), r2 = mix64(r1), r3 = mix64(r2);
+  const int cls = (int)(r3 % 6);
+  const int eb = 523 + (int)(r1 % 1000);   /* recip_ok range */
+  int ea = 600 + (int)(r2 % 850);          /* straddles the fast range */
+  unsigned long long mb = r0, ma = r2 >> 3;
+  if (cls == 1) mb = 0xfffffffffffffull;
+  if (cls == 2) mb = 0;
+  if (cls == 3) mb = (1ull << (r1 % 52)) + ((r0 & 1) ? 1ull : 0xfffffffffffffull);
+  if (cls == 4) ma = 0xfffffffffffffull;
+  *b = make_double(r1 >> 63, eb, mb);
+  if (cls == 5) {
+    const double q = make_double(r2 >> 63, 1023 + (int)(r0 % 64) - 32, (r1 >> 12) & 0xfff0000000000ull);
+    *a = *b * q;
+  } else {
+    *a = make_double(r0 >> 63, ea, ma);
+  }
+}
+
+__global__ void k_div_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                            double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    double a, b;
+    div_operands(k, seed, &a, &b);
+    const double y = shapes::recip_ok(b) ? 1.0 / b : 0.0;
+    const double q = shapes::div_rn(a, b, y);
+    const double ref = a / b;
+    if (__double_as_longlong(q) != __double_as_longlong(ref)) {
+      if (atomicAdd(bad, 1ull) == 0) {
+        first[0] = a;
+        first[1] = b;
+      }
+    }
+  }
+}
+
+__global__ void k_cmp_check(const double* v, int n, unsigned long long* bad) {
+  const int i = blockIdx.x, j = threadIdx.x;
+  if (i >= n || j >= n) return;
+  const double a = v[i], b = v[j];
+  bool ok = shapes::f_le(a, b) == (a <= b) && shapes::f_lt(a, b) == (a < b);
+  const double pz = shapes::plus_zero(a), ref = a + 0.0;
+  ok = ok && ((__double_as_longlong(pz) == __double_as_longlong(ref)) || (pz != pz && ref != ref));
+  if (!ok) atomicAdd(bad, 1ull);
+}
+
+}  // namespace
+
+/* Compares div_rn with IEEE division on n generated operand pairs. */
+extern "C" int shapes_probe_div_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                                      double* first_ab) {
+  unsigned long long* d_bad = nullptr;
+  double* d_first = nullptr;
+  if (cudaMalloc(&d_bad, sizeof(unsigned long long)) != cudaSuccess) return -5;
+  if (cudaMalloc(&d_first, 2 * sizeof(double)) != cudaSuccess) return -5;
+  cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  cudaMemset(d_first, 0, 2 * sizeof(double));
+  k_div_check<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaMemcpy(first_ab, d_first, 2 * sizeof(double), cudaMemcpyDeviceToHost);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  return err == cudaSuccess ? 0 : -5;
+}
+
+/* Compares f_le/f_lt/plus_zero with IEEE on all ordered pairs of n values. */
+extern "C" int shapes_probe_cmp_check(const double* host_vals, int n, unsigned long long* bad) {
+  if (n <= 0 || n > 1024) return -1;
+  double* d_v = nullptr;
+  unsigned long long* d_bad = nullptr;
+  if (cudaMalloc(&d_v, n * sizeof(double)) != cudaSuccess) return -5;
+  if (cudaMalloc(&d_bad, sizeof(unsigned long long)) != cudaSuccess) return -5;
+  cudaMemcpy(d_v, host_vals, n * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  k_cmp_check<<<n, n>>>(d_v, n, d_bad);
+  cudaMemcpy(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(d_v);
+  cudaFree(d_bad);
+  return err == cudaSuccess ? 0 : -5;
+}

@@ -80,6 +80,7 @@ struct shapes_batch {
   int32_t* emax = nullptr;
   /* state */
   double* body[10] = {nullptr};
+  double* body_stage[10] = {nullptr}; /* set_bodies uploads here, validated, then swapped in */
   double* wx = nullptr;
   double* wy = nullptr;
   double* nx = nullptr;
@@ -92,6 +93,22 @@ struct shapes_batch {
   int64_t item_cap = 0;
   int32_t* row_cnt = nullptr;
   int32_t* row_off = nullptr;
+  /* grid broadphase */
+  int32_t grid_min_bodies = 64;
+  bool any_grid = false;
+  int32_t n_buckets = 0;
+  int32_t* grid_T = nullptr;
+  int32_t* grid_base = nullptr;
+  double* grid_inv_s = nullptr;
+  double* grid_lim = nullptr;
+  int32_t* bucket_cnt = nullptr;
+  int32_t* bucket_off = nullptr;
+  int32_t* grid_ids = nullptr;
+  int32_t* cell_x = nullptr;
+  int32_t* cell_y = nullptr;
+  uint8_t* row_mode = nullptr;
+  int32_t* large_cnt = nullptr;
+  int32_t* large_ids = nullptr;
   int32_t* pair_a = nullptr;
   int32_t* pair_b = nullptr;
   int32_t* slot_cnt = nullptr;
@@ -122,7 +139,11 @@ struct shapes_batch {
   int32_t* world_items = nullptr;
   int32_t* group_depth = nullptr;
   int32_t* group_world_off = nullptr;
+  int32_t* group_worlds = nullptr;
   std::vector<int32_t> h_group_world_off;
+  std::vector<int32_t> h_group_worlds;
+  int32_t grouped_iterations = -1;
+  int32_t worlds_per_group_override = 0;
   int32_t target_group_bodies = 0;
   int32_t solve_threads = 128;
   /* scans */
@@ -213,6 +234,19 @@ struct shapes_batch {
     d.box = box;
     d.boxk = boxk;
     d.flags = flags;
+    d.grid_T = grid_T;
+    d.grid_base = grid_base;
+    d.grid_inv_s = grid_inv_s;
+    d.grid_lim = grid_lim;
+    d.bucket_cnt = bucket_cnt;
+    d.bucket_off = bucket_off;
+    d.grid_ids = grid_ids;
+    d.cell_x = cell_x;
+    d.cell_y = cell_y;
+    d.row_mode = row_mode;
+    d.large_cnt = large_cnt;
+    d.large_ids = large_ids;
+    d.n_buckets = n_buckets;
     d.row_cnt = row_cnt;
     d.row_off = row_off;
     d.pair_a = pair_a;
@@ -242,6 +276,7 @@ struct shapes_batch {
     d.world_items = world_items;
     d.group_depth = group_depth;
     d.group_world_off = group_world_off;
+    d.group_worlds = group_worlds;
     d.counters = counters;
     return d;
   }
@@ -305,7 +340,7 @@ struct shapes_batch {
     ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
     isorted = dalloc<uint32_t>(item_cap, "cudaMalloc items");
     ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
-    const int64_t scan_n = std::max<int64_t>(N, pair_cap) + 1;
+    const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(N, pair_cap), n_buckets) + 1;
     tile_cap = (int32_t)((scan_n + shapes::kScanTile - 1) / shapes::kScanTile) + 1;
     tile_sums = dalloc<int32_t>(tile_cap, "cudaMalloc scan");
     snap_cap = contact_cap;
@@ -332,29 +367,89 @@ struct shapes_batch {
     ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
   }
 
-  void make_groups() {
-    h_group_world_off.clear();
-    h_group_world_off.push_back(0);
-    int64_t target = target_group_bodies;
-    if (target <= 0) target = std::max<int64_t>(64, (int64_t)N / (kSMs * 2));
-    int64_t acc = 0;
-    for (int w = 0; w < W; ++w) {
-      acc += h_world_body_off[w + 1] - h_world_body_off[w];
-      if (acc >= target) {
-        h_group_world_off.push_back(w + 1);
-        acc = 0;
+  /* Solver groups: worlds sorted by body count (largest first, so the longest
+   * dependency chains start first) and packed `per_group` at a time, so that a
+   * level of a group offers about one warp of updates (a world yields about
+   * iterations+1 updates per level).  target_group_bodies > 0 overrides the
+   * count with "worlds until this many bodies". */
+  void make_groups(int iterations) {
+    std::vector<int32_t> order(W);
+    for (int w = 0; w < W; ++w) order[w] = w;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return (h_world_body_off[a + 1] - h_world_body_off[a]) > (h_world_body_off[b + 1] - h_world_body_off[b]);
+    });
+    int per_group = std::max(1, std::min(shapes::kMaxGroupWorlds, (32 + iterations) / (iterations + 1)));
+    if (worlds_per_group_override > 0) per_group = std::min(shapes::kMaxGroupWorlds, worlds_per_group_override);
+    h_group_world_off.assign(1, 0);
+    int32_t max_bodies = 0, bodies = 0, in_group = 0;
+    for (int k = 0; k < W; ++k) {
+      const int w = order[k];
+      bodies += h_world_body_off[w + 1] - h_world_body_off[w];
+      ++in_group;
+      const bool close = target_group_bodies > 0 ? (bodies >= target_group_bodies || in_group == shapes::kMaxGroupWorlds)
+                                                 : in_group == per_group;
+      if (close || k == W - 1) {
+        h_group_world_off.push_back(k + 1);
+        max_bodies = std::max(max_bodies, bodies);
+        bodies = 0;
+        in_group = 0;
       }
     }
-    if (h_group_world_off.back() != W) h_group_world_off.push_back(W);
+    h_group_worlds = order;
     dfree(group_world_off);
+    dfree(group_worlds);
     dfree(group_depth);
     const size_t G = h_group_world_off.size() - 1;
+    smem_last_cap = std::min<int32_t>(max_bodies, 2560);
     group_world_off = dalloc<int32_t>(G + 1, "cudaMalloc groups");
+    group_worlds = dalloc<int32_t>(W, "cudaMalloc groups");
     group_depth = dalloc<int32_t>(G, "cudaMalloc groups");
-    ck(cudaMemcpy(group_world_off, h_group_world_off.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice), "upload groups");
+    ck(cudaMemcpy(group_world_off, h_group_world_off.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice),
+       "upload groups");
+    ck(cudaMemcpy(group_worlds, h_group_worlds.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload groups");
+    grouped_iterations = iterations;
   }
 
   int num_groups() const { return (int)h_group_world_off.size() - 1; }
+
+  /* Worlds with at least grid_min_bodies bodies use the grid broadphase. */
+  void setup_grid() {
+    dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
+    dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
+    std::vector<int32_t> T(W), base(W);
+    int64_t nb = 0;
+    any_grid = false;
+    for (int w = 0; w < W; ++w) {
+      const int32_t n = h_world_body_off[w + 1] - h_world_body_off[w];
+      int32_t t = 0;
+      if (n >= grid_min_bodies) {
+        t = 1;
+        while (t < 2 * n) t <<= 1;
+        any_grid = true;
+      }
+      T[w] = t;
+      base[w] = (int32_t)nb;
+      nb += t;
+    }
+    if (nb > INT32_MAX / 2) throw CudaError{cudaErrorMemoryAllocation};
+    n_buckets = (int32_t)nb;
+    grid_T = dalloc<int32_t>(W, "cudaMalloc grid");
+    grid_base = dalloc<int32_t>(W, "cudaMalloc grid");
+    grid_inv_s = dalloc<double>(W, "cudaMalloc grid");
+    grid_lim = dalloc<double>(W, "cudaMalloc grid");
+    bucket_cnt = dalloc<int32_t>((size_t)n_buckets + 1, "cudaMalloc grid");
+    bucket_off = dalloc<int32_t>((size_t)n_buckets + 1, "cudaMalloc grid");
+    grid_ids = dalloc<int32_t>(N, "cudaMalloc grid");
+    cell_x = dalloc<int32_t>(N, "cudaMalloc grid");
+    cell_y = dalloc<int32_t>(N, "cudaMalloc grid");
+    row_mode = dalloc<uint8_t>(N, "cudaMalloc grid");
+    large_cnt = dalloc<int32_t>(W, "cudaMalloc grid");
+    large_ids = dalloc<int32_t>(N, "cudaMalloc grid");
+    ck(cudaMemcpy(grid_T, T.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
+    ck(cudaMemcpy(grid_base, base.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
+    ck(cudaMemset(row_mode, 0, N), "memset");
+  }
+  int32_t smem_last_cap = 0; /* bodies whose last level fits the solver's shared memory */
 
   void scan(const int32_t* in, int n_cap, const unsigned long long* n_dev, int32_t* out) {
     stage(6, 3, [&]() { scan_raw(in, n_cap, n_dev, out); });
@@ -376,10 +471,29 @@ struct shapes_batch {
    * build, warm start, sweeps, integration. */
   void enqueue_step(const shapes_config& cfg, bool solve, int wb) {
     Dev d = view(wb);
-    ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntOverflow, stream), "memset");
-    stage(0, 1, [&]() { shapes::k_broadphase<true><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d); });
+    /* pairs/contacts are per step; hits, items and levels add up over the call */
+    ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2, stream), "memset");
+    if (any_grid) {
+      stage(0, 3, [&]() {
+        ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
+        shapes::k_grid_stats<<<W, 256, 0, stream>>>(d);
+        shapes::k_grid_bin<<<grid_for(N, 256), 256, 0, stream>>>(d);
+      });
+      scan(bucket_cnt, n_buckets, nullptr, bucket_off);
+      stage(0, 1, [&]() { shapes::k_grid_scatter<<<grid_for(N, 256), 256, 0, stream>>>(d); });
+    }
+    stage(0, any_grid ? 2 : 1, [&]() {
+      shapes::k_broadphase<true><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
+      if (any_grid) shapes::k_grid_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
+    });
     scan(row_cnt, N, nullptr, row_off);
-    stage(0, 1, [&]() { shapes::k_broadphase<false><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d); });
+    stage(0, any_grid ? 3 : 1, [&]() {
+      shapes::k_broadphase<false><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
+      if (any_grid) {
+        shapes::k_grid_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
+        shapes::k_grid_sort_rows<<<grid_for(N, 128), 128, 0, stream>>>(d);
+      }
+    });
     stage(6, 1, [&]() { shapes::k_world_pair_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
     stage(1, 1, [&]() { shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d); });
     scan(slot_cnt, pair_cap, counters + shapes::kCntPairs, slot_off);
@@ -389,11 +503,15 @@ struct shapes_batch {
                                                                            cfg.warm_start, solve ? 1 : 0);
     });
     if (!solve) return;
+    if (grouped_iterations != cfg.iterations) make_groups(cfg.iterations);
     const int G = num_groups();
-    stage(3, 1, [&]() { shapes::k_schedule<<<G, 128, 0, stream>>>(d, cfg.iterations, cfg.warm_start); });
+    const int wpc = solve_threads / 32;
+    /* each warp's slice of last levels: 40 KB of dynamic shared memory in all (static use is ~1 KB) */
+    const int per_warp = std::min<int>(smem_last_cap, (40 * 1024 / (int)sizeof(int32_t)) / wpc);
     stage(4, 1, [&]() {
-      shapes::k_solve<<<G, solve_threads, 0, stream>>>(d, cfg.iterations, cfg.external, cfg.accel_x, cfg.accel_y,
-                                                       cfg.dt);
+      shapes::k_schedule_solve<<<(G + wpc - 1) / wpc, solve_threads, (size_t)wpc * per_warp * sizeof(int32_t),
+                                 stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, cfg.accel_x, cfg.accel_y,
+                                           cfg.dt, G, per_warp);
     });
     stage(5, 1, [&]() { shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, cfg.dt, 1); });
   }
@@ -468,11 +586,16 @@ struct shapes_batch {
     free_step_buffers();
     dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly);
     dfree(emin); dfree(emax);
-    for (int k = 0; k < 10; ++k) dfree(body[k]);
+    for (int k = 0; k < 10; ++k) {
+      dfree(body[k]);
+      dfree(body_stage[k]);
+    }
     dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
+    dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
+    dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
     for (int k = 0; k < 2; ++k) dfree(cwo[k]);
-    dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off);
+    dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
     dfree(counters);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(snap_cwo);
@@ -590,6 +713,7 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       h->emin = dalloc<int32_t>(h->V, "cudaMalloc");
       h->emax = dalloc<int32_t>(h->V, "cudaMalloc");
       for (int k = 0; k < 10; ++k) h->body[k] = dalloc<double>(N, "cudaMalloc bodies");
+      for (int k = 0; k < 10; ++k) h->body_stage[k] = dalloc<double>(N, "cudaMalloc bodies");
       h->wx = dalloc<double>(h->V, "cudaMalloc");
       h->wy = dalloc<double>(h->V, "cudaMalloc");
       h->nx = dalloc<double>(h->V, "cudaMalloc");
@@ -618,9 +742,10 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
         ck(cudaMemcpy(h->body[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice), "upload bodies");
       /* empty cache: every world offset 0 */
       for (int k = 0; k < 2; ++k) ck(cudaMemset(h->cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
+      h->setup_grid();
       const int32_t pcap = (int32_t)std::min<int64_t>(std::max<int64_t>(1024, 8LL * N), INT32_MAX / 4);
       h->alloc_step_buffers(pcap, 2 * pcap, 8);
-      h->make_groups();
+      h->make_groups(2);
       Dev d = h->view(0);
       shapes::k_init_extents<<<grid_for(h->V, 128), 128, 0, h->stream>>>(d);
       h->pose(0, 0.0);
@@ -694,12 +819,19 @@ int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in) {
   if (!b || !body_arrays_ok(in)) return SHAPES_E_INVALID_ARG;
   double* bp[10];
   body_ptrs(in, bp);
-  for (int k = 0; k < 10; ++k)
-    for (int32_t i = 0; i < b->N; ++i)
-      if (!std::isfinite(bp[k][i])) return SHAPES_E_NAN;
   return guarded([&]() -> int {
     for (int k = 0; k < 10; ++k)
-      ck(cudaMemcpyAsync(b->body[k], bp[k], sizeof(double) * b->N, cudaMemcpyHostToDevice, b->stream), "upload");
+      ck(cudaMemcpyAsync(b->body_stage[k], bp[k], sizeof(double) * b->N, cudaMemcpyHostToDevice, b->stream), "upload");
+    ck(cudaMemsetAsync(b->counters + shapes::kCntBadInput, 0, sizeof(unsigned long long), b->stream), "memset");
+    shapes::k_check_finite<<<grid_for(10LL * b->N, 256), 256, 0, b->stream>>>(
+        b->body_stage[0], b->body_stage[1], b->body_stage[2], b->body_stage[3], b->body_stage[4],
+        b->body_stage[5], b->body_stage[6], b->body_stage[7], b->body_stage[8], b->body_stage[9], b->N,
+        b->counters + shapes::kCntBadInput);
+    unsigned long long bad = 0;
+    ck(cudaMemcpyAsync(&bad, b->counters + shapes::kCntBadInput, sizeof(bad), cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "validate");
+    if (bad) return SHAPES_E_NAN; /* live state untouched */
+    for (int k = 0; k < 10; ++k) std::swap(b->body[k], b->body_stage[k]);
     b->pose(0, 0.0);
     ck(cudaGetLastError(), "launch");
     ck(cudaStreamSynchronize(b->stream), "upload");
@@ -927,12 +1059,12 @@ int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches) {
 }
 
 int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads) {
-  if (!b || target_bodies_per_group < 0 || threads < 0 || threads > 1024 || (threads % 32) != 0)
+  if (!b || target_bodies_per_group < 0 || threads < 0 || threads > 256 || (threads % 32) != 0)
     return SHAPES_E_INVALID_ARG;
   return guarded([&]() -> int {
     b->target_group_bodies = target_bodies_per_group;
     b->solve_threads = threads > 0 ? threads : 128;
-    b->make_groups();
+    b->make_groups(b->grouped_iterations >= 0 ? b->grouped_iterations : 2);
     return SHAPES_OK;
   });
 }

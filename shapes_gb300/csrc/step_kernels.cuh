@@ -14,6 +14,7 @@
 #pragma once
 #include <cstdint>
 
+#include "fp64_ops.cuh"
 #include "shapes_sincos.h"
 
 namespace shapes {
@@ -22,6 +23,10 @@ constexpr int kMaxVerts = 64;
 constexpr uint32_t kWarmBit = 0x80000000u;
 constexpr uint8_t kFlagStatic = 1;
 constexpr uint8_t kFlagBoxNaN = 2;
+/* per-contact info byte */
+constexpr uint8_t kInfoHit = 1;
+constexpr uint8_t kInfoDynA = 2;
+constexpr uint8_t kInfoDynB = 4;
 
 /* Per-contact constraint data, built once per step (constraintGen,
  * Constraints/Contact.hs:60-72) plus the step-invariant factors of the solver:
@@ -30,11 +35,13 @@ constexpr uint8_t kFlagBoxNaN = 2;
 struct __align__(16) Con {
   double jn[6];
   double jf[6];
-  double bn;
+  double bn, bn0; /* baumgarte term, and bn + 0.0 */
   double rax, ray, rbx, rby, rnx, rny;
-  double mcn, mcf;
+  double mcn, mcf; /* effective-mass denominators */
   double mu;
   double e;
+  double rcn, rcf; /* RN(1/mcn), RN(1/mcf) for div_rn, or 0 when out of its range */
+  double fast;     /* 1 when both radii are below 2^500 and the normal below 2 (exact zero-bounce path) */
   double pad;
 };
 
@@ -66,6 +73,20 @@ struct Dev {
   double* box;      /* [4N] x0 x1 y0 y1 */
   uint64_t* boxk;   /* [4N] ordered keys of box */
   uint8_t* flags;   /* [N] */
+  /* grid broadphase (worlds with grid_T[w] > 0) */
+  const int32_t* grid_T;    /* [W] bucket table size (power of two), 0 = brute force */
+  const int32_t* grid_base; /* [W] first bucket of the world */
+  double* grid_inv_s;       /* [W] 1 / cell size, 0 = no usable grid this step */
+  double* grid_lim;         /* [W] (1 - 2^-20) * cell size: bodies below it in x and y use the grid */
+  int32_t* bucket_cnt;      /* [n_buckets + 1] counts, then scanned offsets */
+  int32_t* bucket_off;      /* [n_buckets + 1] */
+  int32_t* grid_ids;        /* [N] body ids sorted by bucket */
+  int32_t* cell_x;          /* [N] */
+  int32_t* cell_y;          /* [N] */
+  uint8_t* row_mode;        /* [N] 1 = row found through the grid */
+  int32_t* large_cnt;       /* [W] bodies of the world off the grid */
+  int32_t* large_ids;       /* [N] per-world region at world_body_off[w] */
+  int32_t n_buckets;
   int32_t* row_cnt; /* [N] mirrored per-row pair counts */
   int32_t* row_off; /* [N+1] scanned */
   int32_t* pair_a;  /* [pair_cap] global body index, the larger */
@@ -78,7 +99,7 @@ struct Dev {
   int32_t* c_ga;       /* [contact_cap] */
   int32_t* c_gb;       /* [contact_cap] */
   uint8_t* c_flip;     /* [contact_cap] */
-  uint8_t* c_hit;      /* [contact_cap] */
+  uint8_t* c_hit;      /* [contact_cap] kInfo* bits */
   double* c_val;       /* [contact_cap*5] */
   Con* con;            /* [contact_cap] */
   double* lam;         /* [2*contact_cap] this step's cache Lagrangians */
@@ -94,7 +115,8 @@ struct Dev {
   int32_t* ihist;             /* [item_cap] */
   int32_t* world_items;       /* [W] */
   int32_t* group_depth;       /* [G] */
-  const int32_t* group_world_off; /* [G+1] */
+  const int32_t* group_world_off; /* [G+1] offsets into group_worlds */
+  const int32_t* group_worlds;    /* [W] world ids, grouped */
   unsigned long long* counters;   /* [8] see kCnt* */
 };
 
@@ -105,21 +127,30 @@ enum {
   kCntItems = 3,
   kCntLevels = 4,
   kCntOverflow = 5,
+  kCntBadInput = 6,
 };
+
+/* Flags any non-finite value among n bodies' ten state arrays. */
+__global__ void k_check_finite(const double* a0, const double* a1, const double* a2, const double* a3,
+                               const double* a4, const double* a5, const double* a6, const double* a7,
+                               const double* a8, const double* a9, int n, unsigned long long* flag) {
+  const double* arr[10] = {a0, a1, a2, a3, a4, a5, a6, a7, a8, a9};
+  bool bad = false;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 10LL * n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double v = arr[t / n][t % n];
+    bad |= !isfinite(v);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
 
 /* ------------------------------------------------------------------------ */
 /* helpers                                                                    */
 /* ------------------------------------------------------------------------ */
 
-/* Order-preserving key of a binary64: for non-NaN a, b,
- * a < b  <=>  okey(a) < okey(b), and a == b <=> okey(a) == okey(b). */
-__device__ __forceinline__ uint64_t okey(double d) {
-  uint64_t u = (uint64_t)__double_as_longlong(d);
-  if (u == 0x8000000000000000ull) u = 0;
-  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-
 __device__ __forceinline__ bool is_nan(double d) { return d != d; }
+
+
 
 __device__ __forceinline__ uint64_t pack_key(int i, int j, int fa, int fb) {
   return ((uint64_t)i << 44) | ((uint64_t)j << 24) | ((uint64_t)fa << 12) | (uint64_t)fb;
@@ -266,6 +297,7 @@ __global__ void k_broadphase(Dev d) {
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw_total = (gridDim.x * blockDim.x) >> 5;
   for (int g = wid; g < d.n_bodies; g += nw_total) {
+    if (d.row_mode[g]) continue; /* this row comes from the grid */
     const int wld = d.body_world[g];
     const int off = d.world_body_off[wld];
     const int n = d.world_body_off[wld + 1] - off;
@@ -294,6 +326,202 @@ __global__ void k_broadphase(Dev d) {
       count += __popc(m);
     }
     if (COUNT && lane == 0) d.row_cnt[q] = count;
+  }
+}
+
+
+/* Grid broadphase for larger worlds.  It finds exactly the pairs the
+ * brute-force rows find, faster: the cell size s is twice the mean AABB extent
+ * of the world; a body is "small" when its width and height are below
+ * s (1 - 2^-20), its box is finite and its cell index fits 30 bits.  A small
+ * body is binned by the cell of its box's min corner, floor(x0 / s) and
+ * floor(y0 / s) (computed as x0 * (1/s): monotone in x0).  Two small bodies
+ * whose closed boxes overlap have |x0_i - x0_j| < s (1 - 2^-20) and likewise in
+ * y, so their cells differ by at most one in each axis: every such pair is
+ * found by scanning the 3x3 cells around a body.  Cells are hashed into a
+ * table of 2^k >= 2n buckets by their Morton code; a bucket may hold other
+ * cells, so candidates are kept only when their exact cell matches.  Bodies
+ * that are not small are listed per world and checked against everything:
+ * their own rows take the brute-force path, and every grid row also checks
+ * them.  Grid rows are written unordered and then sorted (descending j), so
+ * the final list is the reference's descending (i, j) order. */
+
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+  x &= 0xffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t cell_bucket(int cx, int cy, int T) {
+  return (spread16((uint32_t)cx) | (spread16((uint32_t)cy) << 1)) & (uint32_t)(T - 1);
+}
+
+/* One CTA per world: mean of max(width, height) over finite boxes -> 1/s. */
+__global__ void k_grid_stats(Dev d) {
+  __shared__ double s_sum[32];
+  __shared__ int s_cnt[32];
+  const int wld = blockIdx.x;
+  if (d.grid_T[wld] == 0) return;
+  const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+  double sum = 0.0;
+  int cnt = 0;
+  for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
+    const double w = d.box[4 * g + 1] - d.box[4 * g + 0];
+    const double h = d.box[4 * g + 3] - d.box[4 * g + 2];
+    const double e = w > h ? w : h;
+    if (small_mag(e)) {
+      sum += e;
+      ++cnt;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_sum[threadIdx.x >> 5] = sum;
+    s_cnt[threadIdx.x >> 5] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    int c = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      t += s_sum[k];
+      c += s_cnt[k];
+    }
+    const double s = c > 0 ? 2.0 * t / c : 0.0;
+    const double inv = (s > 0.0 && small_mag(s) && small_mag(1.0 / s)) ? 1.0 / s : 0.0;
+    d.grid_inv_s[wld] = inv;
+    d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
+    d.large_cnt[wld] = 0;
+  }
+}
+
+/* One thread per body: grid bodies get a cell and a bucket count, the rest go
+ * on their world's list of large bodies. */
+__global__ void k_grid_bin(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    const int T = d.grid_T[wld];
+    uint8_t mode = 0;
+    if (T > 0) {
+      const double inv_s = d.grid_inv_s[wld];
+      bool small = false;
+      int cx = 0, cy = 0;
+      if (inv_s > 0.0 && !(d.flags[g] & kFlagBoxNaN)) {
+        const double x0 = d.box[4 * g + 0], x1 = d.box[4 * g + 1];
+        const double y0 = d.box[4 * g + 2], y1 = d.box[4 * g + 3];
+        const double lim = d.grid_lim[wld];
+        const double qx = x0 * inv_s, qy = y0 * inv_s;
+        if (small_mag(x0) && small_mag(x1) && small_mag(y0) && small_mag(y1) && (x1 - x0) < lim &&
+            (y1 - y0) < lim && fabs(qx) < 0x1p30 && fabs(qy) < 0x1p30) {
+          small = true;
+          cx = (int)floor(qx);
+          cy = (int)floor(qy);
+        }
+      }
+      if (small) {
+        mode = 1;
+        d.cell_x[g] = cx;
+        d.cell_y[g] = cy;
+        atomicAdd(&d.bucket_cnt[d.grid_base[wld] + cell_bucket(cx, cy, T)], 1);
+      } else {
+        const int k = atomicAdd(&d.large_cnt[wld], 1);
+        d.large_ids[d.world_body_off[wld] + k] = g;
+      }
+    }
+    d.row_mode[g] = mode;
+  }
+}
+
+/* Places grid bodies into their buckets (bucket_off turns from starts into ends). */
+__global__ void k_grid_scatter(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (!d.row_mode[g]) continue;
+    const int wld = d.body_world[g];
+    const int b = d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld]);
+    const int pos = atomicAdd(&d.bucket_off[b], 1);
+    d.grid_ids[pos] = g;
+  }
+}
+
+/* One thread per grid row i: pairs (i, j), j < i, with the 3x3 cells' bodies
+ * and with the world's large bodies.  COUNT writes the row count; otherwise
+ * the row is written unordered at its offset.  Buckets are read between the
+ * starts (the ends of the previous bucket) and the ends left by the scatter. */
+template <bool COUNT>
+__global__ void k_grid_rows(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (!d.row_mode[g]) continue;
+    const int wld = d.body_world[g];
+    const int off = d.world_body_off[wld];
+    const int n = d.world_body_off[wld + 1] - off;
+    const int q = off + (n - 1 - (g - off));
+    const int T = d.grid_T[wld], base = d.grid_base[wld];
+    const int cx = d.cell_x[g], cy = d.cell_y[g];
+    const uint8_t fi = d.flags[g];
+    uint64_t ki[4];
+    ki[0] = d.boxk[4 * g + 0];
+    ki[1] = d.boxk[4 * g + 1];
+    ki[2] = d.boxk[4 * g + 2];
+    ki[3] = d.boxk[4 * g + 3];
+    int count = 0;
+    const int out = COUNT ? 0 : d.row_off[q];
+    for (int dy = -1; dy <= 1; ++dy) {
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int ncx = cx + dx, ncy = cy + dy;
+        const int b = base + cell_bucket(ncx, ncy, T);
+        const int k0 = b > 0 ? d.bucket_off[b - 1] : 0, k1 = d.bucket_off[b];
+        for (int k = k0; k < k1; ++k) {
+          const int j = d.grid_ids[k];
+          if (j >= g || d.cell_x[j] != ncx || d.cell_y[j] != ncy) continue;
+          if (pair_overlaps(d, g, j, fi, ki)) {
+            if (!COUNT && out + count < d.pair_cap) {
+              d.pair_a[out + count] = g;
+              d.pair_b[out + count] = j;
+            }
+            ++count;
+          }
+        }
+      }
+    }
+    const int nl = d.large_cnt[wld];
+    for (int k = 0; k < nl; ++k) {
+      const int j = d.large_ids[off + k];
+      if (j < g && pair_overlaps(d, g, j, fi, ki)) {
+        if (!COUNT && out + count < d.pair_cap) {
+          d.pair_a[out + count] = g;
+          d.pair_b[out + count] = j;
+        }
+        ++count;
+      }
+    }
+    if (COUNT) d.row_cnt[q] = count;
+  }
+}
+
+/* Sorts each grid row's j descending (rows hold a handful of pairs). */
+__global__ void k_grid_sort_rows(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (!d.row_mode[g]) continue;
+    const int wld = d.body_world[g];
+    const int off = d.world_body_off[wld];
+    const int n = d.world_body_off[wld + 1] - off;
+    const int q = off + (n - 1 - (g - off));
+    const int r0 = d.row_off[q], r1 = min(d.row_off[q + 1], d.pair_cap);
+    for (int a = r0 + 1; a < r1; ++a) {
+      const int v = d.pair_b[a];
+      int b = a - 1;
+      while (b >= r0 && d.pair_b[b] < v) {
+        d.pair_b[b + 1] = d.pair_b[b];
+        --b;
+      }
+      d.pair_b[b + 1] = v;
+    }
   }
 }
 
@@ -563,6 +791,7 @@ __global__ void k_build(Dev d, double dt, double beta, double slop, int warm_sta
       cc.jf[k + 3] = flip ? jf[k] : jf[k + 3];
     }
     cc.bn = depth > slop ? (beta / dt) * (slop - depth) : 0.0;
+    cc.bn0 = cc.bn + 0.0;
     cc.rax = px - xi;
     cc.ray = py - yi;
     cc.rbx = px - xj;
@@ -579,9 +808,13 @@ __global__ void k_build(Dev d, double dt, double beta, double slop, int warm_sta
     }
     cc.mcn = mcn;
     cc.mcf = mcf;
+    cc.rcn = recip_ok(mcn) ? 1.0 / mcn : 0.0;
+    cc.rcf = recip_ok(mcf) ? 1.0 / mcf : 0.0;
     cc.mu = (d.mu[ga] + d.mu[gb]) / 2.0;
     const double ea = d.bounce[ga], eb = d.bounce[gb];
     cc.e = ea <= eb ? ea : eb;
+    cc.fast = (small_mag(cc.rax) && small_mag(cc.ray) && small_mag(cc.rbx) && small_mag(cc.rby) &&
+               below_two(cc.rnx) && below_two(cc.rny)) ? 1.0 : 0.0;
     cc.pad = 0.0;
     d.con[c] = cc;
     /* warm-start lookup */
@@ -601,7 +834,10 @@ __global__ void k_build(Dev d, double dt, double beta, double slop, int warm_sta
         if (k > key) lo = mid + 1; else hi = mid - 1;
       }
     }
-    d.c_hit[c] = hit;
+    uint8_t info = hit ? kInfoHit : 0;
+    if (!(d.flags[ga] & kFlagStatic)) info |= kInfoDynA;
+    if (!(d.flags[gb] & kFlagStatic)) info |= kInfoDynB;
+    d.c_hit[c] = info;
     d.lam[2 * c] = l0;
     d.lam[2 * c + 1] = l1;
   }
@@ -644,94 +880,6 @@ __device__ int block_exclusive_scan(int32_t* a, int n, int32_t* smem /* >= 32 */
   return carry;
 }
 
-/* The reference applies warm starts then `iterations` sweeps strictly in
- * contact order (Solvers/Contact.hs:74-157).  Each update reads and writes only
- * its two bodies' velocities and its own Lagrangians, so running update u after
- * every earlier update that shares a non-static body with it reproduces the
- * sequential result bit for bit.  Static bodies are read-only in the step.
- * level(u) = 1 + max(level of the last earlier update on each of its dynamic
- * bodies); updates of one level touch disjoint bodies.  Levels pipeline the
- * sweeps: sweep s+1 starts on a body as soon as sweep s is done with it.
- * One CTA per solver group (a contiguous run of worlds): warp 0 scans its worlds
- * (lane = world), then the block counting-sorts the group's updates by level. */
-__global__ void k_schedule(Dev d, int iterations, int warm_start) {
-  __shared__ int32_t s_scan[32];
-  __shared__ int32_t s_depth;
-  if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
-  const int grp = blockIdx.x;
-  const int w0 = d.group_world_off[grp], w1 = d.group_world_off[grp + 1];
-  const int stride = iterations + 1;
-  const int c_base = d.world_contact_off[w0];
-  const size_t ibase = (size_t)stride * c_base;
-  if (threadIdx.x == 0) s_depth = 0;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    int depth = 0;
-    for (int wld = w0 + (int)threadIdx.x; wld < w1; wld += 32) {
-      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
-      for (int b = b0; b < b1; ++b) d.last[b] = 0;
-      const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
-      size_t out = (size_t)stride * c0;
-      int n_items = 0;
-      for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
-        for (int c = c0; c < c1; ++c) {
-          if (pass == 0 && !d.c_hit[c]) continue;
-          const int ga = d.c_ga[c], gb = d.c_gb[c];
-          const bool da = !(d.flags[ga] & kFlagStatic), db = !(d.flags[gb] & kFlagStatic);
-          const int la = da ? d.last[ga] : 0, lb = db ? d.last[gb] : 0;
-          const int lvl = (la > lb ? la : lb) + 1;
-          if (da) d.last[ga] = lvl;
-          if (db) d.last[gb] = lvl;
-          d.items[out + n_items] = (uint32_t)c | (pass == 0 ? kWarmBit : 0u);
-          d.ilevel[out + n_items] = lvl;
-          ++n_items;
-          depth = lvl > depth ? lvl : depth;
-        }
-      }
-      d.world_items[wld] = n_items;
-      if (warm_start) atomicAdd(&d.counters[kCntHits], (unsigned long long)(n_items - iterations * (c1 - c0)));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const int y = __shfl_xor_sync(0xffffffffu, depth, o);
-      depth = y > depth ? y : depth;
-    }
-    if (threadIdx.x == 0) s_depth = depth;
-  }
-  __syncthreads();
-  const int depth = s_depth;
-  if (threadIdx.x == 0) {
-    d.group_depth[grp] = depth;
-    atomicAdd(&d.counters[kCntLevels], (unsigned long long)depth);
-  }
-  if (depth == 0) return;
-  int32_t* hist = d.ihist + ibase;
-  for (int k = threadIdx.x; k < depth; k += blockDim.x) hist[k] = 0;
-  __syncthreads();
-  int total = 0;
-  for (int wld = w0; wld < w1; ++wld) {
-    const size_t o = (size_t)stride * d.world_contact_off[wld];
-    const int n_items = d.world_items[wld];
-    for (int k = threadIdx.x; k < n_items; k += blockDim.x) atomicAdd(&hist[d.ilevel[o + k] - 1], 1);
-    total += n_items;
-  }
-  __syncthreads();
-  block_exclusive_scan(hist, depth, s_scan);
-  __syncthreads();
-  for (int wld = w0; wld < w1; ++wld) {
-    const size_t o = (size_t)stride * d.world_contact_off[wld];
-    const int n_items = d.world_items[wld];
-    for (int k = threadIdx.x; k < n_items; k += blockDim.x) {
-      const int pos = atomicAdd(&hist[d.ilevel[o + k] - 1], 1);
-      d.isorted[ibase + pos] = d.items[o + k];
-    }
-  }
-  if (threadIdx.x == 0) atomicAdd(&d.counters[kCntItems], (unsigned long long)total);
-}
-
-/* ------------------------------------------------------------------------ */
-/* A9-A10 solver                                                              */
-/* ------------------------------------------------------------------------ */
-
 /* applyLagrangian2 (Constraint.hs:197-204): v += (J * lambda) * invMass. */
 __device__ __forceinline__ void apply_impulse(const double j[6], double l, double v[6],
                                               const double m[6]) {
@@ -746,88 +894,245 @@ __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
   return s;
 }
 
-/* One dependency level's update.  Warm: applySln of the cached Lagrangians
+/* One update.  Warm: applySln of the cached Lagrangians
  * (Solvers/Contact.hs:105-113).  Otherwise improveContactSln
  * (Solvers/Contact.hs:124-143): both new Lagrangians from the same velocities
  * (contactLagrangian, Constraints/Contact.hs:86-95; bounceB,
  * Restitution.hs:34-51; lagrangian2, Constraint.hs:164-169), then positive /
- * clampAbs (SolutionProcessors.hs:33-53) and applySln (non-penetration first). */
+ * clampAbs (SolutionProcessors.hs:33-53) and applySln (non-penetration first).
+ * bounceB is min 0 (e * (v_closing . n)); when e = 0 and every velocity and
+ * radius is below 2^500 the product is a signed zero and the result is +0, so
+ * b + bounceB equals the precomputed b + 0.0 bit for bit. */
 __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
   const int c = (int)(item & ~kWarmBit);
   const int ga = d.c_ga[c], gb = d.c_gb[c];
-  const Con& cc = d.con[c];
+  const double2* cp = reinterpret_cast<const double2*>(d.con + c);
   double j_n[6], j_f[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) { j_n[k] = cc.jn[k]; j_f[k] = cc.jf[k]; }
+  {
+    const double2 a0 = cp[0], a1 = cp[1], a2 = cp[2], a3 = cp[3], a4 = cp[4], a5 = cp[5];
+    j_n[0] = a0.x; j_n[1] = a0.y; j_n[2] = a1.x; j_n[3] = a1.y; j_n[4] = a2.x; j_n[5] = a2.y;
+    j_f[0] = a3.x; j_f[1] = a3.y; j_f[2] = a4.x; j_f[3] = a4.y; j_f[4] = a5.x; j_f[5] = a5.y;
+  }
   double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
   const double ima = d.iml[ga], ira = d.imr[ga], imb = d.iml[gb], irb = d.imr[gb];
   const double m[6] = {ima, ima, ira, imb, imb, irb};
   double ln_apply, lf_apply;
+  double2* lam2 = reinterpret_cast<double2*>(d.lam) + c;
+  const double2 cached = *lam2;
   if (item & kWarmBit) {
-    ln_apply = d.lam[2 * c];
-    lf_apply = d.lam[2 * c + 1];
+    ln_apply = cached.x;
+    lf_apply = cached.y;
   } else {
-    const double cn = d.lam[2 * c], cf = d.lam[2 * c + 1];
-    /* bounceB: closing velocity ((-va + (-wa) z× ra) + vb) + wb z× rb */
-    const double nwa = -v[2];
-    const double cvx = ((-v[0] + (-(nwa * cc.ray))) + v[3]) + (-(v[5] * cc.rby));
-    const double cvy = ((-v[1] + nwa * cc.rax) + v[4]) + v[5] * cc.rbx;
-    const double tb = cc.e * (cvx * cc.rnx + cvy * cc.rny);
-    const double bounce = 0.0 <= tb ? 0.0 : tb;
-    const double ln_new = (-(dot6(j_n, v) + (cc.bn + bounce))) / cc.mcn;
-    const double lf_new = (-(dot6(j_f, v) + 0.0)) / cc.mcf;
+    const double2 b6 = cp[6];   /* bn, bn0 */
+    const double2 b9 = cp[9];   /* rnx, rny */
+    const double2 b10 = cp[10]; /* mcn, mcf */
+    const double2 b11 = cp[11]; /* mu, e */
+    const double cn = cached.x, cf = cached.y;
+    const uint64_t ebits = (uint64_t)__double_as_longlong(b11.y) & 0x7fffffffffffffffull;
+    const bool fastflag = __double_as_longlong(cp[13].x) != 0;
+    double bias;
+    if (ebits == 0 && fastflag && small_mag(v[0]) && small_mag(v[1]) && small_mag(v[2]) &&
+        small_mag(v[3]) && small_mag(v[4]) && small_mag(v[5])) {
+      bias = b6.y;
+    } else {
+      const double2 b7 = cp[7]; /* rax, ray */
+      const double2 b8 = cp[8]; /* rbx, rby */
+      /* closing velocity ((-va + (-wa) z× ra) + vb) + wb z× rb */
+      const double nwa = -v[2];
+      const double cvx = ((-v[0] + (-(nwa * b7.y))) + v[3]) + (-(v[5] * b8.y));
+      const double cvy = ((-v[1] + nwa * b7.x) + v[4]) + v[5] * b8.x;
+      const double tb = b11.y * (cvx * b9.x + cvy * b9.y);
+      const double bounce = f_le(0.0, tb) ? 0.0 : tb;
+      bias = b6.x + bounce;
+    }
+    const double2 b12 = cp[12]; /* RN(1/mcn), RN(1/mcf) */
+    const double ln_new = div_rn(-(dot6(j_n, v) + bias), b10.x, b12.x);
+    const double lf_new = div_rn(-plus_zero(dot6(j_f, v)), b10.y, b12.y);
     const double neg_cn = -cn;
-    ln_apply = ln_new <= neg_cn ? neg_cn : ln_new;
+    ln_apply = f_le(ln_new, neg_cn) ? neg_cn : ln_new;
     const double ln_cache = cn + ln_apply;
-    const double thr = ln_cache * cc.mu;
+    const double thr = ln_cache * b11.x;
     const double acc = cf + lf_new;
-    const double acc2 = acc > thr ? thr : (acc < -thr ? -thr : acc);
+    const double acc2 = f_lt(thr, acc) ? thr : (f_lt(acc, -thr) ? -thr : acc);
     lf_apply = acc2 - cf;
-    d.lam[2 * c] = ln_cache;
-    d.lam[2 * c + 1] = acc2;
+    *lam2 = make_double2(ln_cache, acc2);
   }
   apply_impulse(j_n, ln_apply, v, m);
   apply_impulse(j_f, lf_apply, v, m);
-  if (!(d.flags[ga] & kFlagStatic)) {
+  const uint8_t info = d.c_hit[c];
+  if (info & kInfoDynA) {
     d.vx[ga] = v[0];
     d.vy[ga] = v[1];
     d.w[ga] = v[2];
   }
-  if (!(d.flags[gb] & kFlagStatic)) {
+  if (info & kInfoDynB) {
     d.vx[gb] = v[3];
     d.vy[gb] = v[4];
     d.w[gb] = v[5];
   }
 }
 
-/* One CTA per solver group: applyExternal (World.hs:156-158, constantAccel
- * External.hs:23-28) on the group's bodies, then every dependency level in
- * order with a block barrier between levels. */
-__global__ void k_solve(Dev d, int iterations, int external, double ax, double ay, double dt) {
+/* The reference applies warm starts then `iterations` sweeps strictly in
+ * contact order (Solvers/Contact.hs:74-157).  Each update reads and writes only
+ * its two bodies' velocities and its own Lagrangians, so running update u after
+ * every earlier update that shares a non-static body with it reproduces the
+ * sequential result bit for bit; static bodies are never written in the step.
+ * level(u) = 1 + max(level of the last earlier update on each of its dynamic
+ * bodies), and updates of one level touch disjoint bodies.  The levels pipeline
+ * the sweeps: sweep s+1 starts on a body as soon as sweep s is done with it, so
+ * a world offers about iterations+1 independent updates per level.
+ *
+ * Each warp owns one solver group: up to 32 worlds of similar size (the host
+ * sorts worlds by size and packs them so that a level fills about one warp).
+ * A warp never waits for another warp:
+ *   1. applyExternal (World.hs:156-158, constantAccel External.hs:23-28) on the
+ *      group's bodies;
+ *   2. lane l scans world l's updates in sequential order, keeping each body's
+ *      last level in the warp's slice of shared memory when it fits;
+ *   3. the warp counting-sorts each world's updates by level in place;
+ *   4. the warp runs the levels in order, lanes taking the level's updates of
+ *      all its worlds, with __syncwarp between levels.
+ * Steps 2-3 are latency-bound integer work that overlaps the FP64-bound step 4
+ * of the other warps on the SM. */
+constexpr int kMaxGroupWorlds = 32;
+
+__global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int external, double ax, double ay,
+                                 double dt, int n_groups, int smem_last_per_warp) {
+  extern __shared__ int32_t s_dyn[];
+  __shared__ int32_t s_pre[8][kMaxGroupWorlds + 1];
   if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
-  const int grp = blockIdx.x;
-  const int w0 = d.group_world_off[grp], w1 = d.group_world_off[grp + 1];
-  if (external) {
-    const int b0 = d.world_body_off[w0], b1 = d.world_body_off[w1];
-    for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
-      if (!(0.0 == d.iml[g])) {
-        d.vx[g] = d.vx[g] + ax * dt;
-        d.vy[g] = d.vy[g] + ay * dt;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int grp = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (grp >= n_groups) return;
+  const int o0 = d.group_world_off[grp], o1 = d.group_world_off[grp + 1];
+  const int nw = o1 - o0;
+  const int stride = iterations + 1;
+  int32_t* s_last = s_dyn + wib * smem_last_per_warp;
+  /* 1. gravity, 2a. reset last levels (lane-parallel over each world) */
+  int group_bodies = 0;
+  for (int k = 0; k < nw; ++k) {
+    const int wld = d.group_worlds[o0 + k];
+    group_bodies += d.world_body_off[wld + 1] - d.world_body_off[wld];
+  }
+  const bool smem_last = group_bodies <= smem_last_per_warp;
+  {
+    int base = 0;
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + lane; g < b1; g += 32) {
+        if (external && !(0.0 == d.iml[g])) {
+          d.vx[g] = d.vx[g] + ax * dt;
+          d.vy[g] = d.vy[g] + ay * dt;
+        }
+        if (smem_last) s_last[base + g - b0] = 0;
+        else d.last[g] = 0;
+      }
+      base += b1 - b0;
+    }
+  }
+  __syncwarp();
+  /* 2b. lane l scans world l */
+  int my_depth = 0, my_items = 0, my_hits = 0;
+  size_t my_region = 0;
+  if (lane < nw) {
+    const int wld = d.group_worlds[o0 + lane];
+    int base = 0;
+    for (int k = 0; k < lane; ++k) {
+      const int w2 = d.group_worlds[o0 + k];
+      base += d.world_body_off[w2 + 1] - d.world_body_off[w2];
+    }
+    const int b0 = d.world_body_off[wld];
+    int32_t* last = smem_last ? s_last + base - b0 : d.last;
+    const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+    my_region = (size_t)stride * c0;
+    for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
+      for (int c = c0; c < c1; ++c) {
+        const uint8_t info = d.c_hit[c];
+        if (pass == 0 && !(info & kInfoHit)) continue;
+        const int ga = d.c_ga[c], gb = d.c_gb[c];
+        const bool da = info & kInfoDynA, db = info & kInfoDynB;
+        const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
+        const int lvl = (la > lb ? la : lb) + 1;
+        if (da) last[ga] = lvl;
+        if (db) last[gb] = lvl;
+        d.items[my_region + my_items] = (uint32_t)c | (pass == 0 ? kWarmBit : 0u);
+        d.ilevel[my_region + my_items] = lvl;
+        ++my_items;
+        my_depth = lvl > my_depth ? lvl : my_depth;
+        my_hits += pass == 0;
       }
     }
   }
-  __syncthreads();
-  const int depth = d.group_depth[grp];
-  if (depth == 0) return;
-  const size_t ibase = (size_t)(iterations + 1) * d.world_contact_off[w0];
-  const int32_t* ends = d.ihist + ibase;
-  const uint32_t* items = d.isorted + ibase;
-  int lo = 0;
-  for (int lvl = 0; lvl < depth; ++lvl) {
-    const int hi = ends[lvl];
-    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) solve_item(d, items[k]);
-    lo = hi;
-    __syncthreads();
+  /* 3. per-world counting sort by level (hist in the world's own region: a
+   *    world's depth never exceeds its update count) */
+  int max_depth = my_depth, tot_items = my_items, tot_hits = my_hits;
+  for (int o = 16; o > 0; o >>= 1) {
+    max_depth = max(max_depth, __shfl_xor_sync(0xffffffffu, max_depth, o));
+    tot_items += __shfl_xor_sync(0xffffffffu, tot_items, o);
+    tot_hits += __shfl_xor_sync(0xffffffffu, tot_hits, o);
+  }
+  if (lane == 0) {
+    atomicAdd(&d.counters[kCntLevels], (unsigned long long)max_depth);
+    atomicAdd(&d.counters[kCntHits], (unsigned long long)tot_hits);
+    atomicAdd(&d.counters[kCntItems], (unsigned long long)tot_items);
+  }
+  for (int k = 0; k < nw; ++k) {
+    const int depth = __shfl_sync(0xffffffffu, my_depth, k);
+    const int n_items = __shfl_sync(0xffffffffu, my_items, k);
+    const size_t region = (size_t)__shfl_sync(0xffffffffu, (unsigned long long)my_region, k);
+    if (depth == 0) continue;
+    int32_t* hist = d.ihist + region;
+    for (int t = lane; t < depth; t += 32) hist[t] = 0;
+    __syncwarp();
+    for (int t = lane; t < n_items; t += 32) atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
+    __syncwarp();
+    int carry = 0;
+    for (int t0 = 0; t0 < depth; t0 += 32) {
+      const int t = t0 + lane;
+      const int x = t < depth ? hist[t] : 0;
+      int incl = x;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (t < depth) hist[t] = carry + incl - x;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+    for (int t = lane; t < n_items; t += 32) {
+      const int pos = atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
+      d.isorted[region + pos] = d.items[region + t];
+    }
+    __syncwarp();
+  }
+  /* 4. levels: hist[L] is now the end of level L+1 within the world's region */
+  int32_t* pre = s_pre[wib];
+  for (int L = 0; L < max_depth; ++L) {
+    int cnt = 0, start = 0;
+    if (lane < nw && L < my_depth) {
+      const int32_t* hist = d.ihist + my_region;
+      start = L > 0 ? hist[L - 1] : 0;
+      cnt = hist[L] - start;
+    }
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane < nw) pre[lane] = incl - cnt;
+    if (lane == 0) pre[nw] = total;
+    __syncwarp();
+    for (int t = lane; t < total; t += 32) {
+      int k = 0;
+      while (pre[k + 1] <= t) ++k; /* world of the t-th update */
+      const size_t region = (size_t)__ldg(&d.world_contact_off[d.group_worlds[o0 + k]]) * stride;
+      const int32_t* hist = d.ihist + region;
+      const int st = L > 0 ? hist[L - 1] : 0;
+      solve_item(d, d.isorted[region + st + (t - pre[k])]);
+    }
+    __syncwarp();
   }
 }
 

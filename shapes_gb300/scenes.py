@@ -126,22 +126,41 @@ def single_world_boxes(seed: int = 0, cols: int = 20, rows: int = 20, steps: int
                    iterations=4, steps=steps)
 
 
-def polygon_field(seed: int = 1, n: int = 65536, extent: float = 512.0, rmin=0.3, rmax=1.0) -> dict:
-    """Single world of n convex polygons (3-8 vertices, radius U[rmin,rmax],
-    vertex radii +-10%, random rotation) with centres uniform in extent^2.
-    Contact generation only."""
-    rng = np.random.default_rng(seed)
-    b = SceneBuilder()
+def polygons_arrays(rng, n: int, rmin: float, rmax: float):
+    """n perturbed regular polygons: returns (verts, nverts, area, inertia)."""
     nvs = rng.integers(3, 9, size=n)
     rs = rng.uniform(rmin, rmax, size=n)
-    ths = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    vo = np.zeros(n + 1, dtype=np.int64)
+    vo[1:] = np.cumsum(nvs)
+    owner = np.repeat(np.arange(n), nvs)
+    k = np.arange(vo[-1]) - vo[owner]
+    ang = 2.0 * np.pi * k / nvs[owner]
+    r = rs[owner] * rng.uniform(0.9, 1.1, size=vo[-1])
+    x, y = r * np.cos(ang), r * np.sin(ang)
+    nxt = np.arange(vo[-1]) + 1
+    nxt[vo[1:] - 1] = vo[:-1]
+    x1, y1 = x[nxt], y[nxt]
+    cr = x * y1 - x1 * y
+    area = 0.5 * np.bincount(owner, cr, minlength=n)
+    inertia = np.bincount(owner, cr * (x * x + x * x1 + x1 * x1 + y * y + y * y1 + y1 * y1), minlength=n) / 12.0
+    return np.stack([x, y], 1), nvs, area, inertia
+
+
+def polygon_field(seed: int = 1, n: int = 65536, extent: float = 512.0, rmin=0.3, rmax=1.0) -> dict:
+    """Single world of n convex polygons (3-8 vertices, radius U[rmin,rmax],
+    vertex radii +-10%, random rotation) with centres uniform in extent^2,
+    all dynamic with density 1.  Contact generation only."""
+    rng = np.random.default_rng(seed)
+    verts, nvs, area, inertia = polygons_arrays(rng, n, rmin, rmax)
+    f = {k: np.zeros(n) for k in BODY_FIELDS}
+    f["rot"] = rng.uniform(0.0, 2.0 * np.pi, size=n)
     cs = rng.uniform(0.0, extent, size=(n, 2))
-    for k in range(n):
-        xy = perturbed_polygon(rng, int(nvs[k]), float(rs[k]))
-        b.add(xy, (cs[k, 0], cs[k, 1]), ths[k])
-    b.end_world()
-    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
-                   iterations=0, steps=1)
+    f["pos_x"], f["pos_y"] = cs[:, 0].copy(), cs[:, 1].copy()
+    f["inv_mass_lin"] = 1.0 / area
+    f["inv_mass_rot"] = 1.0 / inertia
+    f["mu"][:] = DEFAULT_MU
+    return assemble([n], f, verts, nvs, dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP,
+                    accel=(0.0, -9.8), iterations=0, steps=1)
 
 
 def column_world(b: SceneBuilder, rng, n_bodies: int, gap=0.05, x_jitter=0.05, rot_jitter=0.02,
@@ -159,17 +178,63 @@ def column_world(b: SceneBuilder, rng, n_bodies: int, gap=0.05, x_jitter=0.05, r
     b.end_world()
 
 
-def batched_columns(seed: int = 2, n_worlds: int = 4096, nmin: int = 8, nmax: int = 512, steps: int = 300) -> dict:
+def assemble(world_sizes, fields: dict, verts: np.ndarray, nverts: np.ndarray, **config) -> dict:
+    """Scene dict from flat per-body arrays (bodies in world order)."""
+    off = np.zeros(len(world_sizes) + 1, dtype=np.int32)
+    off[1:] = np.cumsum(world_sizes)
+    vo = np.zeros(len(nverts) + 1, dtype=np.int32)
+    vo[1:] = np.cumsum(nverts)
+    return dict(world_body_offsets=off,
+                bodies={f: np.ascontiguousarray(fields[f], dtype=np.float64) for f in BODY_FIELDS},
+                vert_offsets=vo, local_xy=np.ascontiguousarray(verts, dtype=np.float64), config=config)
+
+
+def batched_columns(seed: int = 2, n_worlds: int = 4096, nmin: int = 8, nmax: int = 512, steps: int = 300,
+                    gap: float = 0.05, x_jitter: float = 0.05, rot_jitter: float = 0.02, slab_w: float = 40.0) -> dict:
     """n_worlds independent worlds, body count log-uniform in [nmin, nmax]
-    (slab included), boxes of side U[0.5,2] dropped in a column; dt = 1/60,
-    8 sweeps, 300 steps."""
+    (slab included): a static slab_w x 1 slab, then square boxes of side
+    U[0.5, 2] (density 1) stacked in a column with a small gap and seeded x /
+    rotation jitter; dt = 1/60, 8 sweeps, 300 steps."""
     rng = np.random.default_rng(seed)
-    b = SceneBuilder()
-    counts = np.rint(np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=n_worlds))).astype(int)
-    for nb in counts:
-        column_world(b, rng, int(nb))
-    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
-                   iterations=8, steps=steps)
+    counts = np.rint(np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=n_worlds))).astype(np.int64)
+    nb = counts - 1
+    total = int(nb.sum())
+    side = rng.uniform(0.5, 2.0, size=total)
+    xj = rng.uniform(-x_jitter, x_jitter, size=total)
+    rj = rng.uniform(-rot_jitter, rot_jitter, size=total)
+    world_of = np.repeat(np.arange(n_worlds), nb)
+    first = np.zeros(n_worlds, dtype=np.int64)
+    first[1:] = np.cumsum(nb)[:-1]
+    csum = np.cumsum(side + gap)
+    before = csum - (side + gap)  # sum over earlier boxes (all worlds)
+    base = np.where(first < total, before[np.minimum(first, total - 1)], 0.0)
+    y = gap + (before - base[world_of]) + side / 2.0
+    m = side * side
+    inertia = m * side * side / 6.0
+    n = n_worlds + total
+    is_slab = np.zeros(n, dtype=bool)
+    slab_pos = first + np.arange(n_worlds)
+    is_slab[slab_pos] = True
+    box_pos = np.flatnonzero(~is_slab)
+    f = {k: np.zeros(n) for k in BODY_FIELDS}
+    f["pos_x"][box_pos] = xj
+    f["pos_y"][box_pos] = y
+    f["rot"][box_pos] = rj
+    f["inv_mass_lin"][box_pos] = 1.0 / m
+    f["inv_mass_rot"][box_pos] = 1.0 / inertia
+    f["pos_y"][slab_pos] = -0.5
+    f["mu"][:] = DEFAULT_MU
+    f["bounce"][:] = DEFAULT_BOUNCE
+    half = np.zeros(n)
+    half_h = np.zeros(n)
+    half[box_pos] = side / 2.0
+    half_h[box_pos] = side / 2.0
+    half[slab_pos] = slab_w / 2.0
+    half_h[slab_pos] = 0.5
+    verts = np.stack([np.stack([half, half_h], 1), np.stack([-half, half_h], 1),
+                      np.stack([-half, -half_h], 1), np.stack([half, -half_h], 1)], 1).reshape(-1, 2)
+    return assemble(counts, f, verts, np.full(n, 4), dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE,
+                    slop=DEFAULT_SLOP, accel=(0.0, -9.8), iterations=8, steps=steps)
 
 
 def mixed_pile_world(b: SceneBuilder, rng, n_bodies: int, cols: int = 16, size=(0.4, 1.5), mu=(0.2, 0.8),

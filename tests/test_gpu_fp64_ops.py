@@ -1,0 +1,47 @@
+"""The exact binary64 helpers used by the kernels against the hardware IEEE
+operations they replace (integer-pipe comparisons, x + 0.0, and division by a
+precomputed reciprocal with Markstein's correction)."""
+import ctypes
+import math
+import struct
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def probe(built):
+    import torch
+
+    torch.cuda.set_device(0)
+    from shapes_gb300 import build as B
+
+    lib = ctypes.CDLL(str(B.PROBE_LIB))
+    lib.shapes_probe_div_check.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong,
+                                           ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_double)]
+    lib.shapes_probe_cmp_check.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_ulonglong)]
+    return lib
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13, 14])
+def test_div_rn_matches_hardware_division(probe, seed):
+    bad = ctypes.c_ulonglong()
+    first = (ctypes.c_double * 2)()
+    assert probe.shapes_probe_div_check(1 << 28, seed, ctypes.byref(bad), first) == 0
+    assert bad.value == 0, f"{bad.value} mismatches, first a={first[0]!r} b={first[1]!r}"
+
+
+def test_integer_comparisons_match_ieee(probe):
+    specials = [0.0, -0.0, 1.0, -1.0, math.inf, -math.inf, math.nan, -math.nan, 5e-324, -5e-324,
+                2.2250738585072014e-308, 1.7976931348623157e308, -1.7976931348623157e308, 0.5, 2.0, 3.0,
+                -3.0, 1e-300, -1e300, 1.0000000000000002, 0.9999999999999999]
+    rng = np.random.default_rng(0)
+    rnd = rng.standard_normal(200) * 10.0 ** rng.integers(-300, 300, 200)
+    vals = np.array(specials + list(rnd) + [struct.unpack("<d", struct.pack("<Q", 0x7ff8000000000001))[0]])
+    bad = ctypes.c_ulonglong()
+    assert probe.shapes_probe_cmp_check(vals.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(vals),
+                                        ctypes.byref(bad)) == 0
+    assert bad.value == 0

@@ -130,7 +130,7 @@ def test_mixed_polygon_worlds():
     b.close()
 
 
-@pytest.mark.parametrize("target,threads", [(1, 32), (64, 64), (100000, 256)])
+@pytest.mark.parametrize("target,threads", [(1, 32), (64, 64), (100000, 256), (0, 128)])
 def test_solver_packing_does_not_change_results(target, threads):
     sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
     b = batch_from_scene(sc)
@@ -272,3 +272,31 @@ def test_engine_api_mirror():
     for f in STATE_FIELDS:
         assert_bits_equal(got[f], want[f], f)
     st.batch.close()
+
+
+def test_container_world_grid_with_large_bodies():
+    """Grid broadphase with oversized static walls (checked off the grid) and a
+    world large enough for the grid path."""
+    sc = scenes.container_world(n=3000, width=60.0, steps=1)
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    b.collide()
+    ow[0].collide()
+    compare_collision(b, ow, "container collide")
+    b.step(config_of(sc), 240)
+    step_oracles(ow, sc, 240)
+    compare_bodies(b, ow, sc, "container 240 steps")
+    compare_collision(b, ow, "container step 240")
+    assert b.stats()["contacts"] > 500, b.stats()
+    b.close()
+
+
+@pytest.mark.parametrize("iters", [2, 8])
+def test_group_packing_matches_across_iteration_counts(iters):
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=96), list(range(0, 96, 2)))
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    b.step(config_of(sc, iterations=iters), 60)
+    step_oracles(ow, sc, 60, iterations=iters)
+    compare_bodies(b, ow, sc, f"iters {iters}")
+    b.close()
