@@ -192,6 +192,44 @@ int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches);
 
 void shapes_batch_destroy(shapes_batch* b);
 
+/* ---- Contact generation without allocation ----------------------------------
+ * No counterpart in the reference.  An extra entry point for callers that
+ * cannot allocate device memory themselves: plugins whose host application
+ * owns every device buffer and hands out pre-planned memory, and loops with a
+ * latency budget in which cudaMalloc/cudaFree (they synchronize the whole
+ * device) are not allowed.  It runs the same broadphase and contact
+ * generation as shapes_batch_collide on one world given entirely as device
+ * pointers (inputs and outputs), and its scratch memory is a fixed array
+ * inside the library, so it calls no cudaMalloc, cudaFree or allocating
+ * library routine.
+ *   Limits: n_bodies <= SHAPES_NOALLOC_MAX_BODIES, n_verts <=
+ *   SHAPES_NOALLOC_MAX_VERTS, broadphase pairs <= SHAPES_NOALLOC_MAX_PAIRS;
+ *   beyond them it returns SHAPES_E_CAPACITY.  The array (about 10 MB) is
+ *   held by every GPU that loads the library until the process exits.
+ *   The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   All calls share the one array: calls that overlap on the GPU (different
+ *   streams, threads or processes sharing the library) race.  The call
+ *   synchronizes `cuda_stream` (NULL = legacy default stream) before it
+ *   returns, so consecutive calls on one stream are safe.
+ *   Inputs (device): pos_x, pos_y, rot, inv_mass_lin, inv_mass_rot [n];
+ *   vert_offsets [n+1] (vert_offsets[0] = 0, 3..64 vertices per body,
+ *   checked on the device); local_verts_xy [2*n_verts], counter-clockwise
+ *   convex hulls.  Outputs (device): pairs_ij [2*pair_capacity],
+ *   contact_keys5 / contact_vals5 [5*contact_capacity] in the layouts of
+ *   shapes_batch_get_pairs / shapes_batch_get_contacts; *n_pairs and
+ *   *n_contacts (host) are set even when the capacities are too small
+ *   (SHAPES_E_BUFFER). */
+#define SHAPES_NOALLOC_MAX_BODIES 4096
+#define SHAPES_NOALLOC_MAX_VERTS 32768
+#define SHAPES_NOALLOC_MAX_PAIRS 32768
+int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, const double* pos_y, const double* rot,
+                           const double* inv_mass_lin, const double* inv_mass_rot, const int32_t* vert_offsets,
+                           const double* local_verts_xy, int32_t n_verts, int32_t* pairs_ij,
+                           int64_t pair_capacity, int32_t* contact_keys5, double* contact_vals5,
+                           int64_t contact_capacity, void* cuda_stream, int64_t* n_pairs,
+                           int64_t* n_contacts);
+
 /* Single-world convenience wrappers over a batch of one world. */
 int shapes_world_create(int32_t n_bodies, const shapes_bodies* bodies, const int32_t* vert_offsets,
                         const double* local_verts_xy, const uint8_t* shape_kind,

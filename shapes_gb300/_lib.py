@@ -112,6 +112,10 @@ SIGNATURES = [
     ("shapes_batch_destroy", None, [ctypes.c_void_p]),
     ("shapes_world_create", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(Bodies), _ip, _dp, _up,
                                            ctypes.POINTER(ctypes.c_void_p)]),
+    ("shapes_collide_noalloc", ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, _lp, _lp]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]

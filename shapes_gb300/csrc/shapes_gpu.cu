@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1070,3 +1071,286 @@ int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, in
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------------------------ */
+/* Broadphase + contact generation without allocating                        */
+/* ------------------------------------------------------------------------ */
+/*
+ * shapes_collide_noalloc serves callers that cannot allocate device memory
+ * themselves: plugins whose host application owns every device buffer and
+ * hands out pre-planned memory, and loops with a latency budget in which
+ * cudaMalloc/cudaFree (which synchronize the whole device) are not allowed.
+ * Its scratch lives in the fixed device array below, sized for at most
+ * SHAPES_NOALLOC_MAX_BODIES bodies, SHAPES_NOALLOC_MAX_VERTS vertices and
+ * SHAPES_NOALLOC_MAX_PAIRS broadphase pairs.  Every GPU that loads this
+ * library holds that array until the process exits.
+ */
+namespace {
+
+constexpr int kNaMaxBodies = SHAPES_NOALLOC_MAX_BODIES;
+constexpr int kNaMaxVerts = SHAPES_NOALLOC_MAX_VERTS;
+constexpr int kNaMaxPairs = SHAPES_NOALLOC_MAX_PAIRS;
+constexpr int kNaMaxContacts = 2 * kNaMaxPairs;
+constexpr int kNaTiles = (kNaMaxPairs + 1 + shapes::kScanTile - 1) / shapes::kScanTile + 1;
+
+/* Byte offsets of the scratch arrays, each 256-byte aligned. */
+struct NaPlan {
+  size_t world_body_off, body_world, lx, ly, emin, emax, wx, wy, nx, ny, box, boxk, flags, row_mode, row_cnt,
+      row_off, pair_a, pair_b, slot_cnt, slot_off, slot_feat, slot_val, world_pair_off, cwo, c_key, c_ga, c_gb,
+      c_flip, c_hit, c_val, tile_sums, counters, total;
+};
+
+constexpr size_t na_take(size_t& o, size_t bytes) {
+  const size_t at = o;
+  o += (bytes + 255) & ~size_t(255);
+  return at;
+}
+
+constexpr NaPlan na_plan() {
+  NaPlan p{};
+  size_t o = 0;
+  p.world_body_off = na_take(o, 2 * sizeof(int32_t));
+  p.body_world = na_take(o, kNaMaxBodies * sizeof(int32_t));
+  p.lx = na_take(o, kNaMaxVerts * sizeof(double));
+  p.ly = na_take(o, kNaMaxVerts * sizeof(double));
+  p.emin = na_take(o, kNaMaxVerts * sizeof(int32_t));
+  p.emax = na_take(o, kNaMaxVerts * sizeof(int32_t));
+  p.wx = na_take(o, kNaMaxVerts * sizeof(double));
+  p.wy = na_take(o, kNaMaxVerts * sizeof(double));
+  p.nx = na_take(o, kNaMaxVerts * sizeof(double));
+  p.ny = na_take(o, kNaMaxVerts * sizeof(double));
+  p.box = na_take(o, 4 * kNaMaxBodies * sizeof(double));
+  p.boxk = na_take(o, 4 * kNaMaxBodies * sizeof(uint64_t));
+  p.flags = na_take(o, kNaMaxBodies);
+  p.row_mode = na_take(o, kNaMaxBodies);
+  p.row_cnt = na_take(o, kNaMaxBodies * sizeof(int32_t));
+  p.row_off = na_take(o, (kNaMaxBodies + 1) * sizeof(int32_t));
+  p.pair_a = na_take(o, kNaMaxPairs * sizeof(int32_t));
+  p.pair_b = na_take(o, kNaMaxPairs * sizeof(int32_t));
+  p.slot_cnt = na_take(o, kNaMaxPairs * sizeof(int32_t));
+  p.slot_off = na_take(o, (kNaMaxPairs + 1) * sizeof(int32_t));
+  p.slot_feat = na_take(o, 2 * (size_t)kNaMaxPairs * sizeof(int32_t));
+  p.slot_val = na_take(o, 10 * (size_t)kNaMaxPairs * sizeof(double));
+  p.world_pair_off = na_take(o, 2 * sizeof(int32_t));
+  p.cwo = na_take(o, 2 * sizeof(int32_t));
+  p.c_key = na_take(o, kNaMaxContacts * sizeof(uint64_t));
+  p.c_ga = na_take(o, kNaMaxContacts * sizeof(int32_t));
+  p.c_gb = na_take(o, kNaMaxContacts * sizeof(int32_t));
+  p.c_flip = na_take(o, kNaMaxContacts);
+  p.c_hit = na_take(o, kNaMaxContacts);
+  p.c_val = na_take(o, 5 * (size_t)kNaMaxContacts * sizeof(double));
+  p.tile_sums = na_take(o, kNaTiles * sizeof(int32_t));
+  p.counters = na_take(o, 8 * sizeof(unsigned long long));
+  p.total = o;
+  return p;
+}
+
+constexpr NaPlan kNaPlan = na_plan();
+
+}  // namespace
+
+/* The scratch.  Device code may name it directly; in host code the name is a
+ * host-side stand-in, not a device address, so the host uses the address that
+ * cudaGetSymbolAddress returns (resolved once per device below). */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaPlan.total];
+
+namespace {
+
+/* Per-call set-up in scratch: the one-world offsets, de-interleaved local
+ * vertices and zeroed row modes; checks the caller's vertex offsets so that
+ * no later kernel can index outside the vertex arrays.  The counters were
+ * zeroed by the host before this kernel. */
+__global__ void k_noalloc_setup(int n, int nv, const int32_t* vert_off, const double* local_xy,
+                                unsigned char* base) {
+  int32_t* wbo = reinterpret_cast<int32_t*>(base + kNaPlan.world_body_off);
+  int32_t* bw = reinterpret_cast<int32_t*>(base + kNaPlan.body_world);
+  uint8_t* mode = base + kNaPlan.row_mode;
+  double* lx = reinterpret_cast<double*>(base + kNaPlan.lx);
+  double* ly = reinterpret_cast<double*>(base + kNaPlan.ly);
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(base + kNaPlan.counters);
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  if (t0 == 0) {
+    wbo[0] = 0;
+    wbo[1] = n;
+    if (vert_off[0] != 0 || vert_off[n] != nv) atomicOr(&cnt[shapes::kCntBadInput], 1ull);
+  }
+  for (int i = t0; i < n; i += stride) {
+    bw[i] = 0;
+    mode[i] = 0;
+    const int c = vert_off[i + 1] - vert_off[i];
+    if (c < 3 || c > shapes::kMaxVerts) atomicOr(&cnt[shapes::kCntBadInput], 1ull);
+  }
+  for (int v = t0; v < nv; v += stride) {
+    lx[v] = local_xy[2 * (size_t)v];
+    ly[v] = local_xy[2 * (size_t)v + 1];
+  }
+}
+
+/* Copies pairs and contacts from scratch into the caller's buffers. */
+__global__ void k_noalloc_out(int n_pairs, int n_contacts, const unsigned char* base, int32_t* pairs_ij,
+                              int32_t* keys5, double* vals5) {
+  const int32_t* pa = reinterpret_cast<const int32_t*>(base + kNaPlan.pair_a);
+  const int32_t* pb = reinterpret_cast<const int32_t*>(base + kNaPlan.pair_b);
+  const uint64_t* key = reinterpret_cast<const uint64_t*>(base + kNaPlan.c_key);
+  const uint8_t* flip = base + kNaPlan.c_flip;
+  const double* val = reinterpret_cast<const double*>(base + kNaPlan.c_val);
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int p = t0; p < n_pairs; p += stride) {
+    pairs_ij[2 * p] = pa[p];
+    pairs_ij[2 * p + 1] = pb[p];
+  }
+  for (int c = t0; c < n_contacts; c += stride) {
+    const uint64_t k = key[c];
+    keys5[5 * c] = (int32_t)(k >> 44);
+    keys5[5 * c + 1] = (int32_t)((k >> 24) & 0xfffff);
+    keys5[5 * c + 2] = (int32_t)((k >> 12) & 0xfff);
+    keys5[5 * c + 3] = (int32_t)(k & 0xfff);
+    keys5[5 * c + 4] = flip[c];
+    for (int q = 0; q < 5; ++q) vals5[5 * c + q] = val[5 * (size_t)c + q];
+  }
+}
+
+constexpr int kMaxDevices = 64;
+
+/* Device address of g_noalloc_scratch on the current device, looked up once
+ * per device (the first call on a device does this set-up). */
+int noalloc_scratch_ptr(unsigned char** out) {
+  static std::atomic<unsigned char*> ptrs[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SHAPES_E_CUDA;
+  unsigned char* p = ptrs[dev].load();
+  if (!p) {
+    void* addr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      g_last_error = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return SHAPES_E_CUDA;
+    }
+    p = static_cast<unsigned char*>(addr);
+    ptrs[dev].store(p);
+  }
+  *out = p;
+  return SHAPES_OK;
+}
+
+}  // namespace
+
+extern "C" int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, const double* pos_y, const double* rot,
+                                      const double* inv_mass_lin, const double* inv_mass_rot,
+                                      const int32_t* vert_offsets, const double* local_verts_xy, int32_t n_verts,
+                                      int32_t* pairs_ij, int64_t pair_capacity, int32_t* contact_keys5,
+                                      double* contact_vals5, int64_t contact_capacity, void* cuda_stream,
+                                      int64_t* n_pairs, int64_t* n_contacts) {
+  if (!pos_x || !pos_y || !rot || !inv_mass_lin || !inv_mass_rot || !vert_offsets || !local_verts_xy || !n_pairs ||
+      !n_contacts || n_bodies < 1 || n_verts < 3 * n_bodies)
+    return SHAPES_E_INVALID_ARG;
+  if (n_bodies > kNaMaxBodies || n_verts > kNaMaxVerts) {
+    g_last_error = "shapes_collide_noalloc: more than SHAPES_NOALLOC_MAX_BODIES bodies or SHAPES_NOALLOC_MAX_VERTS vertices";
+    return SHAPES_E_CAPACITY;
+  }
+  unsigned char* base = nullptr;
+  const int rc = noalloc_scratch_ptr(&base);
+  if (rc != SHAPES_OK) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  Dev d{};
+  d.n_worlds = 1;
+  d.n_bodies = n_bodies;
+  d.n_verts = n_verts;
+  d.pair_cap = kNaMaxPairs;
+  d.contact_cap = kNaMaxContacts;
+  d.world_body_off = reinterpret_cast<int32_t*>(base + kNaPlan.world_body_off);
+  d.body_world = reinterpret_cast<int32_t*>(base + kNaPlan.body_world);
+  d.vert_off = vert_offsets;
+  d.lx = reinterpret_cast<double*>(base + kNaPlan.lx);
+  d.ly = reinterpret_cast<double*>(base + kNaPlan.ly);
+  d.emin = reinterpret_cast<int32_t*>(base + kNaPlan.emin);
+  d.emax = reinterpret_cast<int32_t*>(base + kNaPlan.emax);
+  d.px = const_cast<double*>(pos_x);
+  d.py = const_cast<double*>(pos_y);
+  d.th = const_cast<double*>(rot);
+  d.iml = inv_mass_lin;
+  d.imr = inv_mass_rot;
+  d.wx = reinterpret_cast<double*>(base + kNaPlan.wx);
+  d.wy = reinterpret_cast<double*>(base + kNaPlan.wy);
+  d.nx = reinterpret_cast<double*>(base + kNaPlan.nx);
+  d.ny = reinterpret_cast<double*>(base + kNaPlan.ny);
+  d.box = reinterpret_cast<double*>(base + kNaPlan.box);
+  d.boxk = reinterpret_cast<uint64_t*>(base + kNaPlan.boxk);
+  d.flags = base + kNaPlan.flags;
+  d.row_mode = base + kNaPlan.row_mode;
+  d.row_cnt = reinterpret_cast<int32_t*>(base + kNaPlan.row_cnt);
+  d.row_off = reinterpret_cast<int32_t*>(base + kNaPlan.row_off);
+  d.pair_a = reinterpret_cast<int32_t*>(base + kNaPlan.pair_a);
+  d.pair_b = reinterpret_cast<int32_t*>(base + kNaPlan.pair_b);
+  d.slot_cnt = reinterpret_cast<int32_t*>(base + kNaPlan.slot_cnt);
+  d.slot_off = reinterpret_cast<int32_t*>(base + kNaPlan.slot_off);
+  d.slot_feat = reinterpret_cast<int32_t*>(base + kNaPlan.slot_feat);
+  d.slot_val = reinterpret_cast<double*>(base + kNaPlan.slot_val);
+  d.world_pair_off = reinterpret_cast<int32_t*>(base + kNaPlan.world_pair_off);
+  d.world_contact_off = reinterpret_cast<int32_t*>(base + kNaPlan.cwo);
+  d.c_key = reinterpret_cast<uint64_t*>(base + kNaPlan.c_key);
+  d.c_ga = reinterpret_cast<int32_t*>(base + kNaPlan.c_ga);
+  d.c_gb = reinterpret_cast<int32_t*>(base + kNaPlan.c_gb);
+  d.c_flip = base + kNaPlan.c_flip;
+  d.c_hit = base + kNaPlan.c_hit;
+  d.c_val = reinterpret_cast<double*>(base + kNaPlan.c_val);
+  d.counters = reinterpret_cast<unsigned long long*>(base + kNaPlan.counters);
+  int32_t* tile_sums = reinterpret_cast<int32_t*>(base + kNaPlan.tile_sums);
+  auto scan = [&](const int32_t* in, int n_cap, const unsigned long long* n_dev, int32_t* out) {
+    const int tiles = (n_cap + 1 + shapes::kScanTile - 1) / shapes::kScanTile;
+    shapes::k_scan_tiles<<<tiles, shapes::kScanThreads, 0, st>>>(in, n_cap, n_dev, tile_sums);
+    shapes::k_scan_tile_sums<<<1, 1024, 0, st>>>(tile_sums, tiles);
+    shapes::k_scan_apply<<<tiles, shapes::kScanThreads, 0, st>>>(in, n_cap, n_dev, tile_sums, out);
+  };
+  /* counters start at zero; the set-up kernel validates the vertex offsets */
+  cudaError_t e = cudaMemsetAsync(d.counters, 0, 8 * sizeof(unsigned long long), st);
+  unsigned long long cnt[8] = {0};
+  if (e == cudaSuccess) {
+    k_noalloc_setup<<<grid_for(std::max(n_bodies, n_verts), 256), 256, 0, st>>>(n_bodies, n_verts, vert_offsets,
+                                                                                 local_verts_xy, base);
+    e = cudaMemcpyAsync(cnt, d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_last_error = std::string("shapes_collide_noalloc: ") + cudaGetErrorString(e);
+    return SHAPES_E_CUDA;
+  }
+  if (cnt[shapes::kCntBadInput]) return SHAPES_E_INVALID_ARG;
+  shapes::k_init_extents<<<grid_for(n_verts, 128), 128, 0, st>>>(d);
+  shapes::k_integrate_pose<<<grid_for(n_bodies, 128), 128, 0, st>>>(d, 0.0, 0);
+  shapes::k_broadphase<true><<<grid_for((long long)n_bodies * 32, 256), 256, 0, st>>>(d);
+  scan(d.row_cnt, n_bodies, nullptr, d.row_off);
+  shapes::k_broadphase<false><<<grid_for((long long)n_bodies * 32, 256), 256, 0, st>>>(d);
+  shapes::k_world_pair_offsets<<<1, 32, 0, st>>>(d);
+  shapes::k_narrowphase<<<grid_for(kNaMaxPairs, 128), 128, 0, st>>>(d);
+  scan(d.slot_cnt, kNaMaxPairs, d.counters + shapes::kCntPairs, d.slot_off);
+  shapes::k_world_contact_offsets<<<1, 32, 0, st>>>(d);
+  shapes::k_build<<<grid_for(2LL * kNaMaxPairs, 128), 128, 0, st>>>(d, 1.0, 0.0, 0.0, 0, 0);
+  e = cudaMemcpyAsync(cnt, d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_last_error = std::string("shapes_collide_noalloc: ") + cudaGetErrorString(e);
+    return SHAPES_E_CUDA;
+  }
+  *n_pairs = (int64_t)cnt[shapes::kCntPairs];
+  *n_contacts = (int64_t)cnt[shapes::kCntContacts];
+  if (cnt[shapes::kCntOverflow]) {
+    g_last_error = "shapes_collide_noalloc: more than SHAPES_NOALLOC_MAX_PAIRS broadphase pairs";
+    return SHAPES_E_CAPACITY;
+  }
+  if (*n_pairs > pair_capacity || *n_contacts > contact_capacity) return SHAPES_E_BUFFER;
+  if ((*n_pairs > 0 && !pairs_ij) || (*n_contacts > 0 && (!contact_keys5 || !contact_vals5))) return SHAPES_E_INVALID_ARG;
+  if (*n_pairs > 0 || *n_contacts > 0) {
+    k_noalloc_out<<<grid_for(std::max(*n_pairs, *n_contacts), 256), 256, 0, st>>>(
+        (int)*n_pairs, (int)*n_contacts, base, pairs_ij, contact_keys5, contact_vals5);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      g_last_error = std::string("shapes_collide_noalloc: ") + cudaGetErrorString(e);
+      return SHAPES_E_CUDA;
+    }
+  }
+  return SHAPES_OK;
+}
