@@ -79,8 +79,20 @@ typedef struct shapes_config {
   int32_t iterations; /* improveWorld sweeps per step; 2 = reference */
   int32_t warm_start; /* SHAPES_WARM_START_* */
   int32_t external;   /* SHAPES_EXTERNAL_* */
-  int32_t reserved;   /* must be 0 */
+  int32_t flags;      /* SHAPES_FLAG_* */
 } shapes_config;
+
+/* Compute the per-world solver residual after each step's last sweep
+ * (readable with shapes_batch_get_world_metrics).  No counterpart in the
+ * reference, which reports no solver metrics. */
+#define SHAPES_FLAG_RESIDUAL 1
+/* Worlds of SHAPES_LARGE_WORLD_BODIES bodies or more are solved by a
+ * graph-coloured sweep (contacts coloured so that no two of a colour share a
+ * dynamic body, colours swept one after another) instead of the default
+ * order-preserving path; the coloured order differs from the reference's, so
+ * its results differ too.  No counterpart in the reference. */
+#define SHAPES_FLAG_COLOURED 2
+#define SHAPES_LARGE_WORLD_BODIES 4096
 
 /* Counters of the most recent step or collide call, summed over worlds.
  * pairs and contacts are those of the call's last step; cache_hits,
@@ -169,12 +181,34 @@ int shapes_batch_set_cache(shapes_batch* b, const int32_t* world_counts, const i
 
 int shapes_batch_get_stats(shapes_batch* b, shapes_stats* out);
 
+/* Per-world metrics (arrays of n_worlds, either may be NULL).
+ *   residual: RMS over the world's contacts of the normal and friction
+ *     impulses one more sweep would apply after the last step's final sweep
+ *     (needs SHAPES_FLAG_RESIDUAL on that step; NaN otherwise);
+ *   max_depth: the largest contact depth on the current poses (the next
+ *     step's contacts), found by running shapes_batch_collide.
+ * No counterpart in the reference. */
+int shapes_batch_get_world_metrics(shapes_batch* b, double* residual, double* max_depth);
+
 /* Solver packing.  Worlds are sorted by size and packed into groups, one warp
  * per group; target_bodies_per_group > 0 closes a group once it holds that many
  * bodies (0 = automatic: about one warp of updates per dependency level);
- * threads = warps per CTA x 32, at most 256 (0 = 128).  Results do not depend
+ * threads = warps per CTA x 32, at most 256 (0 = 32).  Results do not depend
  * on the packing. */
 int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads);
+/* Same, with a fixed number of worlds per warp group (1..32), as chosen by
+ * shapes_batch_autotune. */
+int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, int32_t threads);
+
+/* Autotuner for the solver packing: from the current state, times
+ * `steps_per_trial` steps for each candidate (worlds per warp group x warps
+ * per CTA), restores the state exactly after every trial, and keeps the
+ * fastest.  The world state and cache are left exactly as they were; results
+ * never depend on the packing.  Tune on a state that has contacts (e.g. after
+ * the scene settles).  chosen_* may be NULL.  Allocates temporary device
+ * memory for the saved state. */
+int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t steps_per_trial,
+                          int32_t* chosen_worlds_per_group, int32_t* chosen_threads);
 
 /* Run this handle's device work on a caller-owned CUDA stream (a
  * cudaStream_t passed as void*), e.g. a framework's current stream; NULL
@@ -189,6 +223,11 @@ int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream);
 #define SHAPES_STAGE_COUNT 7
 int shapes_batch_set_profiling(shapes_batch* b, int32_t enabled);
 int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches);
+/* While profiling: per solver group of the last step, 8 int64 each
+ * (clock at start, after the dependency scan, after the level sort, at end;
+ * dependency levels; updates; bodies; worlds).  *n_groups receives the group
+ * count; `out` may be NULL to query it. */
+int shapes_batch_get_group_clocks(shapes_batch* b, int64_t* out, int32_t* n_groups);
 
 void shapes_batch_destroy(shapes_batch* b);
 

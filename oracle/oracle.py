@@ -44,6 +44,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_world_step.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32]
         L.oracle_world_collide.argtypes = [ctypes.c_void_p]
+        L.oracle_world_residual.restype = ctypes.c_double
+        L.oracle_world_residual.argtypes = [ctypes.c_void_p]
         L.oracle_world_num_bodies.restype = ctypes.c_int32
         L.oracle_world_num_bodies.argtypes = [ctypes.c_void_p]
         L.oracle_world_get_bodies.argtypes = [ctypes.c_void_p, _dp]
@@ -103,6 +105,10 @@ class OracleWorld:
 
     def collide(self):
         lib().oracle_world_collide(self._h)
+
+    def residual(self) -> float:
+        """RMS of what one more sweep would apply after the last step."""
+        return float(lib().oracle_world_residual(self._h))
 
     def bodies(self) -> dict:
         out = np.empty((self.n, 10), dtype=np.float64)

@@ -89,6 +89,7 @@ struct ContactConstraint {
 };
 
 struct World {
+  double residual = 0.0; /* RMS of one non-applying sweep after the last step */
   std::vector<Body> bodies;
   std::vector<Hull> hulls;
   std::vector<CacheEntry> cache;
@@ -486,7 +487,9 @@ static inline double lagrangian2(const Body& a, const Body& b, const double j[6]
  * solutionProcessor (Constraints/Contact.hs:101-110) = positive for the normal
  * (SolutionProcessors.hs:33-35) and clampAbs by nonpen·pairMu for friction
  * (SolutionProcessors.hs:42-53, Friction.hs:46-56), then applySln. */
-static inline void improve_contact(const ContactConstraint& cc, CacheEntry& cache, Body& a, Body& b) {
+static inline void improve_amounts(const ContactConstraint& cc, const CacheEntry& cache, const Body& a,
+                                   const Body& b, double* ln_apply_out, double* lf_apply_out, double* ln_cache_out,
+                                   double* lf_cache_out) {
   /* bounceB */
   const double e = a.bounce <= b.bounce ? a.bounce : b.bounce;
   const double nwax = -((-a.w) * cc.ray), nway = (-a.w) * cc.rax;
@@ -506,10 +509,18 @@ static inline void improve_contact(const ContactConstraint& cc, CacheEntry& cach
   const double thr = ln_cache * mu;
   const double acc = cache.lf + lf_new;
   const double acc2 = acc > thr ? thr : (acc < -thr ? -thr : acc);
-  const double lf_apply = acc2 - cache.lf;
+  *ln_apply_out = ln_apply;
+  *lf_apply_out = acc2 - cache.lf;
+  *ln_cache_out = ln_cache;
+  *lf_cache_out = acc2;
+}
+
+static inline void improve_contact(const ContactConstraint& cc, CacheEntry& cache, Body& a, Body& b) {
+  double ln_apply, lf_apply, ln_cache, lf_cache;
+  improve_amounts(cc, cache, a, b, &ln_apply, &lf_apply, &ln_cache, &lf_cache);
   apply_sln(ln_apply, lf_apply, cc, a, b);
   cache.ln = ln_cache;
-  cache.lf = acc2;
+  cache.lf = lf_cache;
 }
 
 /* ---- A12 the step -------------------------------------------------------- */
@@ -565,6 +576,19 @@ static void step_world(World& w, const StepConfig& cfg) {
       const Contact& ct = w.contacts[k];
       improve_contact(cons[k], lag[k], w.bodies[ct.key.i], w.bodies[ct.key.j]);
     }
+  }
+  /* Solver residual (no reference counterpart): the amounts one more sweep
+   * would apply, every contact seeing the final velocities; RMS over the normal
+   * and friction amounts of all contacts. */
+  {
+    double sum = 0.0;
+    for (size_t k = 0; k < C; ++k) {
+      const Contact& ct = w.contacts[k];
+      double dn, df, cn, cf;
+      improve_amounts(cons[k], lag[k], w.bodies[ct.key.i], w.bodies[ct.key.j], &dn, &df, &cn, &cf);
+      sum += dn * dn + df * df;
+    }
+    w.residual = C ? std::sqrt(sum / (2.0 * (double)C)) : 0.0;
   }
   w.cache.swap(lag);
   /* 6. advance (World.hs:167-169) → advanceObj (Constraint.hs:225-229) */
@@ -623,6 +647,8 @@ void oracle_world_collide(void* h) {
   broadphase(w);
   narrowphase(w);
 }
+
+double oracle_world_residual(void* h) { return static_cast<World*>(h)->residual; }
 
 int32_t oracle_world_num_bodies(void* h) { return (int32_t) static_cast<World*>(h)->bodies.size(); }
 

@@ -29,6 +29,9 @@ SHAPES_EXTERNAL_NONE = 0
 SHAPES_EXTERNAL_CONSTANT_ACCEL = 1
 SHAPES_WARM_START_OFF = 0
 SHAPES_WARM_START_CACHE = 1
+SHAPES_FLAG_RESIDUAL = 1
+SHAPES_FLAG_COLOURED = 2
+SHAPES_LARGE_WORLD_BODIES = 4096
 
 STAGE_NAMES = ("broadphase", "narrowphase", "build", "schedule", "solve", "integrate", "scan")
 STAGE_COUNT = len(STAGE_NAMES)
@@ -60,7 +63,7 @@ class Config(ctypes.Structure):
         ("iterations", ctypes.c_int32),
         ("warm_start", ctypes.c_int32),
         ("external", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
     ]
 
 
@@ -105,10 +108,14 @@ SIGNATURES = [
     ("shapes_batch_get_cache", ctypes.c_int, [ctypes.c_void_p, _ip, _dp, ctypes.c_int64, _ip]),
     ("shapes_batch_set_cache", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _dp]),
     ("shapes_batch_get_stats", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    ("shapes_batch_get_world_metrics", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     ("shapes_batch_set_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    ("shapes_batch_set_launch_groups", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_stream", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("shapes_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Config), ctypes.c_int32, _ip, _ip]),
     ("shapes_batch_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_get_profile", ctypes.c_int, [ctypes.c_void_p, _dp, _lp]),
+    ("shapes_batch_get_group_clocks", ctypes.c_int, [ctypes.c_void_p, _lp, _ip]),
     ("shapes_batch_destroy", None, [ctypes.c_void_p]),
     ("shapes_world_create", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(Bodies), _ip, _dp, _up,
                                            ctypes.POINTER(ctypes.c_void_p)]),
@@ -246,10 +253,24 @@ class Batch:
         check(lib().shapes_batch_set_cache(self._h, _ptr(wc, _ip), _ptr(k, _ip), _ptr(lam, _dp)),
               "shapes_batch_set_cache")
 
+    def world_metrics(self) -> tuple[np.ndarray, np.ndarray]:
+        """(residual after the last step's final sweep, max depth on the current poses) per world."""
+        r = np.empty(self.n_worlds)
+        dmax = np.empty(self.n_worlds)
+        check(lib().shapes_batch_get_world_metrics(self._h, _ptr(r, _dp), _ptr(dmax, _dp)),
+              "shapes_batch_get_world_metrics")
+        return r, dmax
+
     def stats(self) -> dict:
         s = Stats()
         check(lib().shapes_batch_get_stats(self._h, ctypes.byref(s)), "shapes_batch_get_stats")
         return {f[0]: getattr(s, f[0]) for f in Stats._fields_}
+
+    def autotune(self, cfg: Config, steps_per_trial: int = 5) -> tuple[int, int]:
+        wpg, thr = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().shapes_batch_autotune(self._h, ctypes.byref(cfg), steps_per_trial, ctypes.byref(wpg),
+                                          ctypes.byref(thr)), "shapes_batch_autotune")
+        return wpg.value, thr.value
 
     def set_stream(self, cuda_stream: int | None) -> None:
         check(lib().shapes_batch_set_stream(self._h, ctypes.c_void_p(cuda_stream or None)), "shapes_batch_set_stream")
@@ -263,12 +284,29 @@ class Batch:
         check(lib().shapes_batch_get_profile(self._h, _ptr(ms, _dp), _ptr(n, _lp)), "shapes_batch_get_profile")
         return {name: (float(ms[k]), int(n[k])) for k, name in enumerate(STAGE_NAMES)}
 
+    def set_launch_groups(self, worlds_per_group: int, threads: int) -> None:
+        """Fixed worlds per warp group (what the autotuner chooses)."""
+        check(lib().shapes_batch_set_launch_groups(self._h, worlds_per_group, threads),
+              "shapes_batch_set_launch_groups")
+
+    def group_clocks(self) -> np.ndarray:
+        """Per solver group of the last profiled step: [start, after scan, after sort, end,
+        levels, updates, bodies, worlds] (clock64 units)."""
+        g = ctypes.c_int32()
+        check(lib().shapes_batch_get_group_clocks(self._h, None, ctypes.byref(g)), "shapes_batch_get_group_clocks")
+        out = np.zeros(8 * max(g.value, 1), dtype=np.int64)
+        check(lib().shapes_batch_get_group_clocks(self._h, _ptr(out, _lp), ctypes.byref(g)),
+              "shapes_batch_get_group_clocks")
+        return out[: 8 * g.value].reshape(-1, 8)
+
     def set_launch(self, target_bodies_per_group: int, threads: int) -> None:
         check(lib().shapes_batch_set_launch(self._h, target_bodies_per_group, threads), "shapes_batch_set_launch")
 
 
 def make_config(dt: float, baumgarte: float = 0.01, slop: float = 0.02, accel=(0.0, -9.8),
-                iterations: int = 2, warm_start: bool = True, external: bool = True) -> Config:
+                iterations: int = 2, warm_start: bool = True, external: bool = True,
+                residual: bool = False, coloured: bool = False) -> Config:
     return Config(dt, baumgarte, slop, float(accel[0]), float(accel[1]), int(iterations),
                   SHAPES_WARM_START_CACHE if warm_start else SHAPES_WARM_START_OFF,
-                  SHAPES_EXTERNAL_CONSTANT_ACCEL if external else SHAPES_EXTERNAL_NONE, 0)
+                  SHAPES_EXTERNAL_CONSTANT_ACCEL if external else SHAPES_EXTERNAL_NONE,
+                  (SHAPES_FLAG_RESIDUAL if residual else 0) | (SHAPES_FLAG_COLOURED if coloured else 0))

@@ -22,6 +22,7 @@
 
 #include "../../include/shapes_gpu.h"
 #include "step_kernels.cuh"
+#include "large_world.cuh"
 
 using shapes::Con;
 using shapes::Dev;
@@ -137,6 +138,11 @@ struct shapes_batch {
   int32_t* ilevel = nullptr;
   uint32_t* isorted = nullptr;
   int32_t* ihist = nullptr;
+  int4* gdesc = nullptr;
+  int4* idesc = nullptr;
+  int32_t* ghist = nullptr;
+  long long* phase_clock = nullptr; /* [8 * G], allocated while profiling */
+  int32_t phase_clock_groups = 0;
   int32_t* world_items = nullptr;
   int32_t* group_depth = nullptr;
   int32_t* group_world_off = nullptr;
@@ -144,13 +150,35 @@ struct shapes_batch {
   std::vector<int32_t> h_group_world_off;
   std::vector<int32_t> h_group_worlds;
   int32_t grouped_iterations = -1;
+  /* worlds solved by the large-world paths (not packed into warp groups) */
+  int32_t large_world_bodies = SHAPES_LARGE_WORLD_BODIES;
+  std::vector<int32_t> large_worlds;
+  int32_t lw_nb_max = 0;
+  int32_t* lw_bcnt = nullptr;
+  int32_t* lw_bstart = nullptr;
+  int32_t* lw_bh = nullptr;
+  int32_t* lw_bn = nullptr;
+  int32_t* lw_done = nullptr;
+  int32_t* lw_refs = nullptr;
+  int32_t* lw_rank = nullptr;
+  int32_t* lw_hrank = nullptr;
+  int32_t* lw_hitflag = nullptr;
+  int32_t* lw_hitoff = nullptr;
+  int32_t* lw_hit_idx = nullptr;
+  int32_t* lw_color = nullptr;
+  int32_t* lw_color_cnt = nullptr;
+  int32_t* lw_color_list = nullptr;
+  unsigned long long* lw_ctl = nullptr; /* 8 per large world */
   int32_t worlds_per_group_override = 0;
   int32_t target_group_bodies = 0;
-  int32_t solve_threads = 128;
+  int32_t solve_threads = 32;
   /* scans */
   int32_t* tile_sums = nullptr;
   int32_t tile_cap = 0;
   unsigned long long* counters = nullptr;
+  double* world_residual = nullptr;
+  double* world_depth = nullptr;
+  bool residual_valid = false;
   /* snapshot for retries */
   double* snap_body[6] = {nullptr};
   uint64_t* snap_key = nullptr;
@@ -274,11 +302,17 @@ struct shapes_batch {
     d.ilevel = ilevel;
     d.isorted = isorted;
     d.ihist = ihist;
+    d.gdesc = gdesc;
+    d.idesc = idesc;
+    d.phase_clock = profiling ? phase_clock : nullptr;
+    d.ghist = ghist;
     d.world_items = world_items;
     d.group_depth = group_depth;
     d.group_world_off = group_world_off;
     d.group_worlds = group_worlds;
     d.counters = counters;
+    d.world_residual = world_residual;
+    d.world_depth = world_depth;
     return d;
   }
 
@@ -286,9 +320,13 @@ struct shapes_batch {
     dfree(pair_a); dfree(pair_b); dfree(slot_cnt); dfree(slot_off); dfree(slot_feat); dfree(slot_val);
     for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
     dfree(c_ga); dfree(c_gb); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
-    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist);
+    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist); dfree(gdesc); dfree(ghist); dfree(idesc);
+    idesc = nullptr;
     dfree(tile_sums);
     dfree(snap_key); dfree(snap_lam);
+    dfree(lw_refs); dfree(lw_rank); dfree(lw_hrank); dfree(lw_hitflag); dfree(lw_hitoff); dfree(lw_hit_idx);
+    dfree(lw_color); dfree(lw_color_list);
+    lw_refs = lw_rank = lw_hrank = lw_hitflag = lw_hitoff = lw_hit_idx = lw_color = lw_color_list = nullptr;
     pair_a = pair_b = slot_cnt = slot_off = slot_feat = nullptr;
     slot_val = nullptr;
     c_key[0] = c_key[1] = nullptr;
@@ -299,6 +337,8 @@ struct shapes_batch {
     con = nullptr;
     items = isorted = nullptr;
     ilevel = ihist = nullptr;
+    gdesc = nullptr;
+    ghist = nullptr;
     tile_sums = nullptr;
     snap_key = nullptr;
     snap_lam = nullptr;
@@ -307,6 +347,7 @@ struct shapes_batch {
   /* (Re)allocates every buffer sized by pairs/contacts/updates.  Cache
    * contents in c_key/lam[cache_buf] are preserved across a regrowth. */
   void alloc_step_buffers(int32_t new_pair_cap, int32_t new_contact_cap, int iterations) {
+    if (stream) ck(cudaStreamSynchronize(stream), "sync");
     const int32_t old_cap = contact_cap;
     uint64_t* keep_key = nullptr;
     double* keep_lam = nullptr;
@@ -337,13 +378,26 @@ struct shapes_batch {
     c_hit = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
     c_val = dalloc<double>(5 * (size_t)contact_cap, "cudaMalloc contacts");
     con = dalloc<Con>(contact_cap, "cudaMalloc constraints");
-    items = dalloc<uint32_t>(item_cap, "cudaMalloc items");
+    items = dalloc<uint32_t>(1, "cudaMalloc items");
     ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
-    isorted = dalloc<uint32_t>(item_cap, "cudaMalloc items");
-    ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
-    const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(N, pair_cap), n_buckets) + 1;
+    isorted = dalloc<uint32_t>(1, "cudaMalloc items");
+    ihist = dalloc<int32_t>(1, "cudaMalloc items");
+    gdesc = dalloc<int4>(item_cap + W + 1, "cudaMalloc items");
+    ghist = dalloc<int32_t>(item_cap + W + 1, "cudaMalloc items");
+    idesc = dalloc<int4>(item_cap, "cudaMalloc items");
+    const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(N, contact_cap), n_buckets) + 1;
     tile_cap = (int32_t)((scan_n + shapes::kScanTile - 1) / shapes::kScanTile) + 1;
     tile_sums = dalloc<int32_t>(tile_cap, "cudaMalloc scan");
+    if (!large_worlds.empty()) {
+      lw_refs = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc large world");
+      lw_rank = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc large world");
+      lw_hrank = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc large world");
+      lw_hitflag = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_hitoff = dalloc<int32_t>((size_t)contact_cap + 1, "cudaMalloc large world");
+      lw_hit_idx = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_color = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_color_list = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+    }
     snap_cap = contact_cap;
     snap_key = dalloc<uint64_t>(snap_cap, "cudaMalloc snapshot");
     snap_lam = dalloc<double>(2 * (size_t)snap_cap, "cudaMalloc snapshot");
@@ -360,12 +414,16 @@ struct shapes_batch {
 
   void ensure_items(int iterations) {
     if ((int64_t)(iterations + 1) * contact_cap <= item_cap) return;
-    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist);
+    ck(cudaStreamSynchronize(stream), "sync");
+    dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist); dfree(gdesc); dfree(ghist); dfree(idesc);
     item_cap = (int64_t)(iterations + 1) * contact_cap;
     items = dalloc<uint32_t>(item_cap, "cudaMalloc items");
     ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
-    isorted = dalloc<uint32_t>(item_cap, "cudaMalloc items");
-    ihist = dalloc<int32_t>(item_cap, "cudaMalloc items");
+    isorted = dalloc<uint32_t>(1, "cudaMalloc items");
+    ihist = dalloc<int32_t>(1, "cudaMalloc items");
+    gdesc = dalloc<int4>(item_cap + W + 1, "cudaMalloc items");
+    ghist = dalloc<int32_t>(item_cap + W + 1, "cudaMalloc items");
+    idesc = dalloc<int4>(item_cap, "cudaMalloc items");
   }
 
   /* Solver groups: worlds sorted by body count (largest first, so the longest
@@ -374,22 +432,25 @@ struct shapes_batch {
    * iterations+1 updates per level).  target_group_bodies > 0 overrides the
    * count with "worlds until this many bodies". */
   void make_groups(int iterations) {
-    std::vector<int32_t> order(W);
-    for (int w = 0; w < W; ++w) order[w] = w;
+    if (stream) ck(cudaStreamSynchronize(stream), "sync"); /* no kernel may still read the old groups */
+    std::vector<int32_t> order;
+    for (int w = 0; w < W; ++w)
+      if (h_world_body_off[w + 1] - h_world_body_off[w] < large_world_bodies) order.push_back(w);
+    const int n_small = (int)order.size();
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
       return (h_world_body_off[a + 1] - h_world_body_off[a]) > (h_world_body_off[b + 1] - h_world_body_off[b]);
     });
-    int per_group = std::max(1, std::min(shapes::kMaxGroupWorlds, (32 + iterations) / (iterations + 1)));
+    int per_group = std::max(1, std::min(shapes::kMaxGroupWorlds, 32 / (iterations + 1)));
     if (worlds_per_group_override > 0) per_group = std::min(shapes::kMaxGroupWorlds, worlds_per_group_override);
     h_group_world_off.assign(1, 0);
     int32_t max_bodies = 0, bodies = 0, in_group = 0;
-    for (int k = 0; k < W; ++k) {
+    for (int k = 0; k < n_small; ++k) {
       const int w = order[k];
       bodies += h_world_body_off[w + 1] - h_world_body_off[w];
       ++in_group;
       const bool close = target_group_bodies > 0 ? (bodies >= target_group_bodies || in_group == shapes::kMaxGroupWorlds)
                                                  : in_group == per_group;
-      if (close || k == W - 1) {
+      if (close || k == n_small - 1) {
         h_group_world_off.push_back(k + 1);
         max_bodies = std::max(max_bodies, bodies);
         bodies = 0;
@@ -401,17 +462,103 @@ struct shapes_batch {
     dfree(group_worlds);
     dfree(group_depth);
     const size_t G = h_group_world_off.size() - 1;
-    smem_last_cap = std::min<int32_t>(max_bodies, 2560);
+    /* shared slice per warp (int32 units): last levels (1 per body) during the
+     * scan, then velocities (3 doubles = 6 per body) during the solve */
+    smem_last_cap = std::min<int32_t>(6 * max_bodies, 10240);
     group_world_off = dalloc<int32_t>(G + 1, "cudaMalloc groups");
-    group_worlds = dalloc<int32_t>(W, "cudaMalloc groups");
-    group_depth = dalloc<int32_t>(G, "cudaMalloc groups");
+    group_worlds = dalloc<int32_t>(std::max(n_small, 1), "cudaMalloc groups");
+    group_depth = dalloc<int32_t>(std::max<size_t>(G, 1), "cudaMalloc groups");
     ck(cudaMemcpy(group_world_off, h_group_world_off.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice),
        "upload groups");
-    ck(cudaMemcpy(group_worlds, h_group_worlds.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload groups");
+    if (n_small > 0)
+      ck(cudaMemcpy(group_worlds, h_group_worlds.data(), sizeof(int32_t) * n_small, cudaMemcpyHostToDevice),
+         "upload groups");
     grouped_iterations = iterations;
+    dfree(phase_clock);
+    phase_clock = dalloc<long long>(8 * std::max<size_t>(G, 1), "cudaMalloc groups");
+    phase_clock_groups = (int32_t)G;
   }
 
   int num_groups() const { return (int)h_group_world_off.size() - 1; }
+
+  /* Worlds with at least large_world_bodies bodies are solved by the
+   * large-world paths; their per-body scratch is sized for the largest. */
+  void setup_large_worlds() {
+    large_worlds.clear();
+    lw_nb_max = 0;
+    for (int w = 0; w < W; ++w) {
+      const int32_t n = h_world_body_off[w + 1] - h_world_body_off[w];
+      if (n >= large_world_bodies) {
+        large_worlds.push_back(w);
+        lw_nb_max = std::max(lw_nb_max, n);
+      }
+    }
+    if (large_worlds.empty()) return;
+    lw_bcnt = dalloc<int32_t>((size_t)lw_nb_max + 1, "cudaMalloc large world");
+    lw_bstart = dalloc<int32_t>((size_t)lw_nb_max + 1, "cudaMalloc large world");
+    lw_bh = dalloc<int32_t>(lw_nb_max, "cudaMalloc large world");
+    lw_bn = dalloc<int32_t>(lw_nb_max, "cudaMalloc large world");
+    lw_done = dalloc<int32_t>(lw_nb_max, "cudaMalloc large world");
+    lw_color_cnt = dalloc<int32_t>(shapes::kMaxColors + 1, "cudaMalloc large world");
+    lw_ctl = dalloc<unsigned long long>(8 * large_worlds.size(), "cudaMalloc large world");
+  }
+
+  shapes::LW lw_view(size_t k) const {
+    shapes::LW w{};
+    w.wld = large_worlds[k];
+    w.b0 = h_world_body_off[w.wld];
+    w.nb = h_world_body_off[w.wld + 1] - w.b0;
+    w.bcnt = lw_bcnt;
+    w.bstart = lw_bstart;
+    w.refs = lw_refs;
+    w.rank = lw_rank;
+    w.hrank = lw_hrank;
+    w.bh = lw_bh;
+    w.bn = lw_bn;
+    w.done = lw_done;
+    w.hitflag = lw_hitflag;
+    w.hitoff = lw_hitoff;
+    w.hit_idx = lw_hit_idx;
+    w.color = lw_color;
+    w.color_cnt = lw_color_cnt;
+    w.color_list = lw_color_list;
+    w.ctl = lw_ctl + 8 * k;
+    return w;
+  }
+
+  /* Solve one large world: ranks of every contact on its bodies, then the
+   * ordered dataflow kernel, or the coloured sweep. */
+  void solve_large_world(const Dev& d, size_t k, const shapes_config& cfg) {
+    shapes::LW w = lw_view(k);
+    const int cap = contact_cap;
+    stage(3, 5, [&]() {
+      shapes::k_lw_setup<<<grid_for(w.nb + 1, 256), 256, 0, stream>>>(d, w);
+      shapes::k_lw_count<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+      scan_raw(w.bcnt, w.nb, nullptr, w.bstart);
+      shapes::k_lw_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+      shapes::k_lw_rank<<<grid_for(w.nb, 128), 128, 0, stream>>>(d, w);
+      scan_raw(w.hitflag, cap, w.ctl + 4, w.hitoff);
+      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+    });
+    stage(4, 1, [&]() {
+      if (cfg.external)
+        shapes::k_lw_gravity<<<grid_for(w.nb, 256), 256, 0, stream>>>(d, w, cfg.accel_x, cfg.accel_y, cfg.dt);
+      if (!(cfg.flags & SHAPES_FLAG_COLOURED)) {
+        shapes::k_lw_ordered<<<kSMs * 8, 128, 0, stream>>>(d, w, cfg.iterations, cfg.warm_start);
+        return;
+      }
+      shapes::k_lw_color_init<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+      for (int r = 0; r < 24; ++r) shapes::k_lw_color_round<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+      shapes::k_lw_color_count<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+      scan_raw(w.color_cnt, shapes::kMaxColors, nullptr, w.color_cnt);
+      shapes::k_lw_color_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+      for (int pass = cfg.warm_start ? 0 : 1; pass <= cfg.iterations; ++pass) {
+        for (int col = 0; col < shapes::kSeqColor; ++col)
+          shapes::k_lw_color_pass<<<grid_for(cap / 8 + 1, 128), 128, 0, stream>>>(d, w, col, pass == 0);
+        shapes::k_lw_color_seq<<<1, 32, 0, stream>>>(d, w, pass == 0);
+      }
+    });
+  }
 
   /* Worlds with at least grid_min_bodies bodies use the grid broadphase. */
   void setup_grid() {
@@ -472,8 +619,10 @@ struct shapes_batch {
    * build, warm start, sweeps, integration. */
   void enqueue_step(const shapes_config& cfg, bool solve, int wb) {
     Dev d = view(wb);
-    /* pairs/contacts are per step; hits, items and levels add up over the call */
+    /* pairs/contacts and the group allocator are per step; hits, items and
+     * levels add up over the call */
     ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2, stream), "memset");
+    ck(cudaMemsetAsync(counters + shapes::kCntGroupAlloc, 0, sizeof(unsigned long long), stream), "memset");
     if (any_grid) {
       stage(0, 3, [&]() {
         ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
@@ -504,16 +653,19 @@ struct shapes_batch {
                                                                            cfg.warm_start, solve ? 1 : 0);
     });
     if (!solve) return;
-    if (grouped_iterations != cfg.iterations) make_groups(cfg.iterations);
-    const int G = num_groups();
+    const int G = num_groups(); /* groups for cfg.iterations were built by run() before this view */
     const int wpc = solve_threads / 32;
     /* each warp's slice of last levels: 40 KB of dynamic shared memory in all (static use is ~1 KB) */
-    const int per_warp = std::min<int>(smem_last_cap, (40 * 1024 / (int)sizeof(int32_t)) / wpc);
-    stage(4, 1, [&]() {
-      shapes::k_schedule_solve<<<(G + wpc - 1) / wpc, solve_threads, (size_t)wpc * per_warp * sizeof(int32_t),
-                                 stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, cfg.accel_x, cfg.accel_y,
-                                           cfg.dt, G, per_warp);
-    });
+    const int per_warp = std::min<int>(smem_last_cap, (40 * 1024 / (int)sizeof(int32_t)) / wpc) & ~1;
+    if (G > 0)
+      stage(4, 1, [&]() {
+        shapes::k_schedule_solve<<<(G + wpc - 1) / wpc, solve_threads, (size_t)wpc * per_warp * sizeof(int32_t),
+                                   stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, cfg.accel_x,
+                                             cfg.accel_y, cfg.dt, G, per_warp);
+      });
+    for (size_t k = 0; k < large_worlds.size(); ++k) solve_large_world(d, k, cfg);
+    if (cfg.flags & SHAPES_FLAG_RESIDUAL)
+      stage(4, 1, [&]() { shapes::k_residual<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d); });
     stage(5, 1, [&]() { shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, cfg.dt, 1); });
   }
 
@@ -537,6 +689,9 @@ struct shapes_batch {
   /* Runs `nsteps` steps (or one collide when !solve) with overflow retries. */
   int run(const shapes_config& cfg, int32_t nsteps, bool solve) {
     ensure_items(solve ? cfg.iterations : 0);
+    /* (re)build the solver groups before any device view of this call is
+     * taken: make_groups reallocates the group arrays */
+    if (solve && grouped_iterations != cfg.iterations) make_groups(cfg.iterations);
     int retries = 0;
     for (;;) {
       ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 8, stream), "memset");
@@ -559,6 +714,15 @@ struct shapes_batch {
       ck(cudaGetLastError(), "launch");
       if (profiling) collect_profile();
       for (int k = 0; k < 8; ++k) agg[k] = h[k];
+      if (!agg[shapes::kCntOverflow] && solve && !large_worlds.empty()) {
+        std::vector<unsigned long long> ctl(8 * large_worlds.size());
+        ck(cudaMemcpy(ctl.data(), lw_ctl, sizeof(unsigned long long) * ctl.size(), cudaMemcpyDeviceToHost), "ctl");
+        for (size_t k = 0; k < large_worlds.size(); ++k)
+          if (ctl[8 * k + 1]) {
+            g_last_error = "large-world solver: a bounded wait gave up";
+            return SHAPES_E_TIMEOUT;
+          }
+      }
       if (!agg[shapes::kCntOverflow]) {
         stats.pairs = (int64_t)agg[shapes::kCntPairs];
         stats.contacts = (int64_t)agg[shapes::kCntContacts];
@@ -597,7 +761,11 @@ struct shapes_batch {
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
     for (int k = 0; k < 2; ++k) dfree(cwo[k]);
     dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
+    dfree(phase_clock);
     dfree(counters);
+    dfree(lw_bcnt); dfree(lw_bstart); dfree(lw_bh); dfree(lw_bn); dfree(lw_done); dfree(lw_color_cnt); dfree(lw_ctl);
+    dfree(world_residual);
+    dfree(world_depth);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(snap_cwo);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
@@ -729,6 +897,8 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       h->last = dalloc<int32_t>(N, "cudaMalloc");
       h->world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
       h->counters = dalloc<unsigned long long>(8, "cudaMalloc");
+      h->world_residual = dalloc<double>(n_worlds, "cudaMalloc");
+      h->world_depth = dalloc<double>(n_worlds, "cudaMalloc");
       for (int k = 0; k < 6; ++k) h->snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
       h->snap_cwo = dalloc<int32_t>(n_worlds + 1, "cudaMalloc snapshot");
       ck(cudaMemcpy(h->world_body_off, world_body_offsets, sizeof(int32_t) * (n_worlds + 1), cudaMemcpyHostToDevice), "upload");
@@ -744,6 +914,7 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       /* empty cache: every world offset 0 */
       for (int k = 0; k < 2; ++k) ck(cudaMemset(h->cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
       h->setup_grid();
+      h->setup_large_worlds();
       const int32_t pcap = (int32_t)std::min<int64_t>(std::max<int64_t>(1024, 8LL * N), INT32_MAX / 4);
       h->alloc_step_buffers(pcap, 2 * pcap, 8);
       h->make_groups(2);
@@ -779,7 +950,7 @@ static int check_cfg(const shapes_config* c) {
     return SHAPES_E_UNSUPPORTED;
   if (c->external != SHAPES_EXTERNAL_NONE && c->external != SHAPES_EXTERNAL_CONSTANT_ACCEL)
     return SHAPES_E_UNSUPPORTED;
-  if (c->reserved != 0) return SHAPES_E_INVALID_ARG;
+  if (c->flags & ~(SHAPES_FLAG_RESIDUAL | SHAPES_FLAG_COLOURED)) return SHAPES_E_INVALID_ARG;
   return SHAPES_OK;
 }
 
@@ -790,7 +961,9 @@ int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps)
   if (nsteps == 0) return SHAPES_OK;
   return guarded([&]() -> int {
     ck(cudaSetDevice(b->device), "cudaSetDevice");
-    return b->run(*cfg, nsteps, true);
+    const int rc = b->run(*cfg, nsteps, true);
+    b->residual_valid = rc == SHAPES_OK && (cfg->flags & SHAPES_FLAG_RESIDUAL);
+    return rc;
   });
 }
 
@@ -1023,10 +1196,126 @@ int shapes_batch_set_cache(shapes_batch* b, const int32_t* world_counts, const i
   });
 }
 
+int shapes_batch_get_world_metrics(shapes_batch* b, double* residual, double* max_depth) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    if (residual) {
+      if (b->residual_valid)
+        ck(cudaMemcpy(residual, b->world_residual, sizeof(double) * b->W, cudaMemcpyDeviceToHost), "download");
+      else
+        std::fill(residual, residual + b->W, std::nan(""));
+    }
+    if (max_depth) {
+      shapes_config cfg{};
+      cfg.dt = 1.0;
+      const int rc = b->run(cfg, 1, false);
+      if (rc != SHAPES_OK) return rc;
+      Dev d = b->view(b->results_buf);
+      shapes::k_world_depth<<<(b->W * 32 + 127) / 128, 128, 0, b->stream>>>(d);
+      ck(cudaGetLastError(), "launch");
+      ck(cudaMemcpyAsync(max_depth, b->world_depth, sizeof(double) * b->W, cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    return SHAPES_OK;
+  });
+}
+
 int shapes_batch_get_stats(shapes_batch* b, shapes_stats* out) {
   if (!b || !out) return SHAPES_E_INVALID_ARG;
   *out = b->stats;
   return SHAPES_OK;
+}
+
+int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t steps_per_trial,
+                          int32_t* chosen_worlds_per_group, int32_t* chosen_threads) {
+  if (!b || steps_per_trial < 1) return SHAPES_E_INVALID_ARG;
+  const int rc0 = check_cfg(cfg);
+  if (rc0 != SHAPES_OK) return rc0;
+  return guarded([&]() -> int {
+    const int N = b->N, W = b->W;
+    /* save the state the trials start from */
+    int32_t n_cache = 0;
+    ck(cudaMemcpyAsync(&n_cache, b->cwo[b->cache_buf] + W, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    std::vector<void*> saved;
+    auto keep = [&](const void* src, size_t bytes) {
+      void* p = nullptr;
+      ck(cudaMalloc(&p, std::max<size_t>(bytes, 1)), "cudaMalloc autotune");
+      saved.push_back(p);
+      ck(cudaMemcpyAsync(p, src, bytes, cudaMemcpyDeviceToDevice, b->stream), "copy");
+      return p;
+    };
+    const int cache_buf0 = b->cache_buf;
+    void* sb[6];
+    for (int k = 0; k < 6; ++k) sb[k] = keep(b->body[k], sizeof(double) * N);
+    void* skey = keep(b->c_key[cache_buf0], sizeof(uint64_t) * n_cache);
+    void* slam = keep(b->lam[cache_buf0], sizeof(double) * 2 * n_cache);
+    void* scwo = keep(b->cwo[cache_buf0], sizeof(int32_t) * (W + 1));
+    const int32_t wpg0 = b->worlds_per_group_override, thr0 = b->solve_threads, tgt0 = b->target_group_bodies;
+    const bool prof0 = b->profiling;
+    b->profiling = false;
+    auto restore_state = [&]() {
+      b->cache_buf = cache_buf0;
+      for (int k = 0; k < 6; ++k)
+        ck(cudaMemcpyAsync(b->body[k], sb[k], sizeof(double) * N, cudaMemcpyDeviceToDevice, b->stream), "copy");
+      if (n_cache > b->contact_cap) throw CudaError{cudaErrorMemoryAllocation};
+      ck(cudaMemcpyAsync(b->c_key[cache_buf0], skey, sizeof(uint64_t) * n_cache, cudaMemcpyDeviceToDevice, b->stream), "copy");
+      ck(cudaMemcpyAsync(b->lam[cache_buf0], slam, sizeof(double) * 2 * n_cache, cudaMemcpyDeviceToDevice, b->stream), "copy");
+      ck(cudaMemcpyAsync(b->cwo[cache_buf0], scwo, sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, b->stream), "copy");
+      b->pose(0, 0.0);
+    };
+    const int base = std::max(1, std::min(shapes::kMaxGroupWorlds, 32 / (cfg->iterations + 1)));
+    std::vector<std::pair<int, int>> cands;
+    for (int wpg : {1, base / 2, base, base + 1, 2 * base})
+      for (int thr : {32, 64, 128})
+        if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds &&
+            std::find(cands.begin(), cands.end(), std::make_pair(wpg, thr)) == cands.end())
+          cands.emplace_back(wpg, thr);
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    std::pair<int, int> best_c = {wpg0, thr0};
+    int rc = SHAPES_OK;
+    for (const auto& c : cands) {
+      restore_state();
+      b->worlds_per_group_override = c.first;
+      b->target_group_bodies = 0;
+      b->solve_threads = c.second;
+      b->make_groups(cfg->iterations);
+      ck(cudaEventRecord(e0, b->stream), "event");
+      rc = b->run(*cfg, steps_per_trial, true);
+      if (rc != SHAPES_OK) break;
+      ck(cudaEventRecord(e1, b->stream), "event");
+      ck(cudaEventSynchronize(e1), "event");
+      float ms = 0.f;
+      ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+      if (ms < best) {
+        best = ms;
+        best_c = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    restore_state();
+    if (rc == SHAPES_OK) {
+      b->worlds_per_group_override = best_c.first;
+      b->target_group_bodies = 0;
+      b->solve_threads = best_c.second;
+    } else {
+      b->worlds_per_group_override = wpg0;
+      b->target_group_bodies = tgt0;
+      b->solve_threads = thr0;
+    }
+    b->make_groups(cfg->iterations);
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    for (void* p : saved) cudaFree(p);
+    b->profiling = prof0;
+    b->have_results = false;
+    if (chosen_worlds_per_group) *chosen_worlds_per_group = b->worlds_per_group_override;
+    if (chosen_threads) *chosen_threads = b->solve_threads;
+    return rc;
+  });
 }
 
 int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream) {
@@ -1059,12 +1348,37 @@ int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches) {
   return SHAPES_OK;
 }
 
+int shapes_batch_get_group_clocks(shapes_batch* b, int64_t* out, int32_t* n_groups) {
+  if (!b || !n_groups) return SHAPES_E_INVALID_ARG;
+  *n_groups = b->phase_clock_groups;
+  if (!out) return SHAPES_OK;
+  return guarded([&]() -> int {
+    ck(cudaMemcpy(out, b->phase_clock, sizeof(long long) * 8 * b->phase_clock_groups, cudaMemcpyDeviceToHost),
+       "download");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, int32_t threads) {
+  if (!b || worlds_per_group < 1 || worlds_per_group > shapes::kMaxGroupWorlds || threads < 0 || threads > 256 ||
+      (threads % 32) != 0)
+    return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    b->target_group_bodies = 0;
+    b->worlds_per_group_override = worlds_per_group;
+    b->solve_threads = threads > 0 ? threads : 32;
+    b->make_groups(b->grouped_iterations >= 0 ? b->grouped_iterations : 2);
+    return SHAPES_OK;
+  });
+}
+
 int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads) {
   if (!b || target_bodies_per_group < 0 || threads < 0 || threads > 256 || (threads % 32) != 0)
     return SHAPES_E_INVALID_ARG;
   return guarded([&]() -> int {
     b->target_group_bodies = target_bodies_per_group;
-    b->solve_threads = threads > 0 ? threads : 128;
+    b->worlds_per_group_override = 0;
+    b->solve_threads = threads > 0 ? threads : 32;
     b->make_groups(b->grouped_iterations >= 0 ? b->grouped_iterations : 2);
     return SHAPES_OK;
   });

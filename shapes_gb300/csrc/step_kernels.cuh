@@ -112,12 +112,18 @@ struct Dev {
   uint32_t* items;            /* [item_cap] */
   int32_t* ilevel;            /* [item_cap] */
   uint32_t* isorted;          /* [item_cap] */
-  int32_t* ihist;             /* [item_cap] */
+  int32_t* ihist;             /* [item_cap] (unused by the warp-group solver) */
+  int4* gdesc;                /* [item_cap + W + 1] per-group updates sorted by level: {id, a, b, info | world << 8} */
+  int4* idesc;                /* [item_cap] the same descriptors in sequential order, per world region */
+  long long* phase_clock;     /* [G * 8] per-group phase clocks when profiling, else null */
+  int32_t* ghist;             /* [item_cap + W + 1] per-group level ends */
   int32_t* world_items;       /* [W] */
   int32_t* group_depth;       /* [G] */
   const int32_t* group_world_off; /* [G+1] offsets into group_worlds */
   const int32_t* group_worlds;    /* [W] world ids, grouped */
   unsigned long long* counters;   /* [8] see kCnt* */
+  double* world_residual;         /* [W] */
+  double* world_depth;            /* [W] */
 };
 
 enum {
@@ -128,6 +134,7 @@ enum {
   kCntLevels = 4,
   kCntOverflow = 5,
   kCntBadInput = 6,
+  kCntGroupAlloc = 7, /* bump allocator of the per-group regions (reset every step) */
 };
 
 /* Flags any non-finite value among n bodies' ten state arrays. */
@@ -894,6 +901,38 @@ __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
   return s;
 }
 
+/* Where a solver group keeps its bodies' velocities during the solve: in the
+ * warp's shared-memory slice (slot = global body index + delta of its world)
+ * when the group fits, else in global memory. */
+struct VelStore {
+  double* s;   /* shared: 3 doubles per slot */
+  const Dev* d;
+  __device__ __forceinline__ void load(int g, int delta, double& x, double& y, double& w) const {
+    if (s) {
+      const double* p = s + 3 * (g + delta);
+      x = p[0]; y = p[1]; w = p[2];
+    } else {
+      x = d->vx[g]; y = d->vy[g]; w = d->w[g];
+    }
+  }
+  __device__ __forceinline__ void store(int g, int delta, double x, double y, double w) const {
+    if (s) {
+      double* p = s + 3 * (g + delta);
+      p[0] = x; p[1] = y; p[2] = w;
+    } else {
+      d->vx[g] = x; d->vy[g] = y; d->w[g] = w;
+    }
+  }
+};
+
+/* Pulls a constraint record's cache lines into L1 ahead of its level. */
+__device__ __forceinline__ void prefetch_con(const Con* c) {
+  const char* p = reinterpret_cast<const char*>(c);
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 128));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + sizeof(Con) - 8));
+}
+
 /* One update.  Warm: applySln of the cached Lagrangians
  * (Solvers/Contact.hs:105-113).  Otherwise improveContactSln
  * (Solvers/Contact.hs:124-143): both new Lagrangians from the same velocities
@@ -903,9 +942,9 @@ __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
  * bounceB is min 0 (e * (v_closing . n)); when e = 0 and every velocity and
  * radius is below 2^500 the product is a signed zero and the result is +0, so
  * b + bounceB equals the precomputed b + 0.0 bit for bit. */
-__device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
+__device__ __forceinline__ void solve_item(const Dev& d, uint32_t item, int ga, int gb, uint8_t info,
+                                           const VelStore& vs, int delta) {
   const int c = (int)(item & ~kWarmBit);
-  const int ga = d.c_ga[c], gb = d.c_gb[c];
   const double2* cp = reinterpret_cast<const double2*>(d.con + c);
   double j_n[6], j_f[6];
   {
@@ -913,8 +952,10 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
     j_n[0] = a0.x; j_n[1] = a0.y; j_n[2] = a1.x; j_n[3] = a1.y; j_n[4] = a2.x; j_n[5] = a2.y;
     j_f[0] = a3.x; j_f[1] = a3.y; j_f[2] = a4.x; j_f[3] = a4.y; j_f[4] = a5.x; j_f[5] = a5.y;
   }
-  double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
-  const double ima = d.iml[ga], ira = d.imr[ga], imb = d.iml[gb], irb = d.imr[gb];
+  double v[6];
+  vs.load(ga, delta, v[0], v[1], v[2]);
+  vs.load(gb, delta, v[3], v[4], v[5]);
+  const double ima = __ldg(d.iml + ga), ira = __ldg(d.imr + ga), imb = __ldg(d.iml + gb), irb = __ldg(d.imr + gb);
   const double m[6] = {ima, ima, ira, imb, imb, irb};
   double ln_apply, lf_apply;
   double2* lam2 = reinterpret_cast<double2*>(d.lam) + c;
@@ -927,6 +968,7 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
     const double2 b9 = cp[9];   /* rnx, rny */
     const double2 b10 = cp[10]; /* mcn, mcf */
     const double2 b11 = cp[11]; /* mu, e */
+    const double2 b12 = cp[12]; /* RN(1/mcn), RN(1/mcf) */
     const double cn = cached.x, cf = cached.y;
     const uint64_t ebits = (uint64_t)__double_as_longlong(b11.y) & 0x7fffffffffffffffull;
     const bool fastflag = __double_as_longlong(cp[13].x) != 0;
@@ -945,7 +987,6 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
       const double bounce = f_le(0.0, tb) ? 0.0 : tb;
       bias = b6.x + bounce;
     }
-    const double2 b12 = cp[12]; /* RN(1/mcn), RN(1/mcf) */
     const double ln_new = div_rn(-(dot6(j_n, v) + bias), b10.x, b12.x);
     const double lf_new = div_rn(-plus_zero(dot6(j_f, v)), b10.y, b12.y);
     const double neg_cn = -cn;
@@ -959,17 +1000,8 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item) {
   }
   apply_impulse(j_n, ln_apply, v, m);
   apply_impulse(j_f, lf_apply, v, m);
-  const uint8_t info = d.c_hit[c];
-  if (info & kInfoDynA) {
-    d.vx[ga] = v[0];
-    d.vy[ga] = v[1];
-    d.w[ga] = v[2];
-  }
-  if (info & kInfoDynB) {
-    d.vx[gb] = v[3];
-    d.vy[gb] = v[4];
-    d.w[gb] = v[5];
-  }
+  if (info & kInfoDynA) vs.store(ga, delta, v[0], v[1], v[2]);
+  if (info & kInfoDynB) vs.store(gb, delta, v[3], v[4], v[5]);
 }
 
 /* The reference applies warm starts then `iterations` sweeps strictly in
@@ -998,8 +1030,8 @@ constexpr int kMaxGroupWorlds = 32;
 
 __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int external, double ax, double ay,
                                  double dt, int n_groups, int smem_last_per_warp) {
-  extern __shared__ int32_t s_dyn[];
-  __shared__ int32_t s_pre[8][kMaxGroupWorlds + 1];
+  extern __shared__ __align__(16) int32_t s_dyn[];
+  __shared__ int32_t s_delta[8][kMaxGroupWorlds];
   if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int grp = blockIdx.x * (blockDim.x >> 5) + wib;
@@ -1008,6 +1040,7 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
   const int nw = o1 - o0;
   const int stride = iterations + 1;
   int32_t* s_last = s_dyn + wib * smem_last_per_warp;
+  if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 0] = clock64();
   /* 1. gravity, 2a. reset last levels (lane-parallel over each world) */
   int group_bodies = 0;
   for (int k = 0; k < nw; ++k) {
@@ -1046,94 +1079,240 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
     int32_t* last = smem_last ? s_last + base - b0 : d.last;
     const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
     my_region = (size_t)stride * c0;
-    for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
-      for (int c = c0; c < c1; ++c) {
-        const uint8_t info = d.c_hit[c];
-        if (pass == 0 && !(info & kInfoHit)) continue;
-        const int ga = d.c_ga[c], gb = d.c_gb[c];
-        const bool da = info & kInfoDynA, db = info & kInfoDynB;
-        const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
-        const int lvl = (la > lb ? la : lb) + 1;
-        if (da) last[ga] = lvl;
-        if (db) last[gb] = lvl;
-        d.items[my_region + my_items] = (uint32_t)c | (pass == 0 ? kWarmBit : 0u);
-        d.ilevel[my_region + my_items] = lvl;
-        ++my_items;
-        my_depth = lvl > my_depth ? lvl : my_depth;
-        my_hits += pass == 0;
+    /* The only loop-carried dependency is through last[]; the next contact's
+     * info and bodies are loaded one iteration ahead so their latency hides
+     * behind the current update's shared-memory work. */
+    int pass = warm_start ? 0 : 1;
+    int c = c0;
+    uint8_t info_n = 0;
+    int ga_n = 0, gb_n = 0;
+    if (c0 < c1) {
+      info_n = d.c_hit[c0];
+      ga_n = d.c_ga[c0];
+      gb_n = d.c_gb[c0];
+    } else {
+      pass = iterations + 1;
+    }
+    while (pass <= iterations) {
+      const uint8_t info = info_n;
+      const int ga = ga_n, gb = gb_n, cur_c = c, cur_pass = pass;
+      if (++c == c1) {
+        c = c0;
+        ++pass;
       }
+      if (pass <= iterations) {
+        info_n = d.c_hit[c];
+        ga_n = d.c_ga[c];
+        gb_n = d.c_gb[c];
+      }
+      if (cur_pass == 0 && !(info & kInfoHit)) continue;
+      const bool da = info & kInfoDynA, db = info & kInfoDynB;
+      const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
+      const int lvl = (la > lb ? la : lb) + 1;
+      if (da) last[ga] = lvl;
+      if (db) last[gb] = lvl;
+      d.idesc[my_region + my_items] =
+          make_int4((int)((uint32_t)cur_c | (cur_pass == 0 ? kWarmBit : 0u)), ga, gb, (int)info | (lane << 8));
+      d.ilevel[my_region + my_items] = lvl;
+      ++my_items;
+      my_depth = lvl > my_depth ? lvl : my_depth;
+      my_hits += cur_pass == 0;
     }
   }
-  /* 3. per-world counting sort by level (hist in the world's own region: a
-   *    world's depth never exceeds its update count) */
+  if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 1] = clock64();
+  /* 3. the group's updates counting-sorted by level into a region of gdesc /
+   *    ghist taken from a bump allocator, as packed descriptors, so that a
+   *    level is one contiguous run */
   int max_depth = my_depth, tot_items = my_items, tot_hits = my_hits;
   for (int o = 16; o > 0; o >>= 1) {
     max_depth = max(max_depth, __shfl_xor_sync(0xffffffffu, max_depth, o));
     tot_items += __shfl_xor_sync(0xffffffffu, tot_items, o);
     tot_hits += __shfl_xor_sync(0xffffffffu, tot_hits, o);
   }
+  int gbase = 0;
   if (lane == 0) {
     atomicAdd(&d.counters[kCntLevels], (unsigned long long)max_depth);
     atomicAdd(&d.counters[kCntHits], (unsigned long long)tot_hits);
     atomicAdd(&d.counters[kCntItems], (unsigned long long)tot_items);
+    gbase = (int)atomicAdd(&d.counters[kCntGroupAlloc], (unsigned long long)(tot_items + 1));
   }
+  gbase = __shfl_sync(0xffffffffu, gbase, 0);
+  int32_t* gh = d.ghist + gbase;
+  int4* gdesc = d.gdesc + gbase;
+  /* the histogram lives in the warp's shared slice when the depth fits (the
+   * last levels are dead by now), else in gh */
+  int32_t* hist = max_depth <= smem_last_per_warp ? s_last : gh;
+  for (int t = lane; t < max_depth; t += 32) hist[t] = 0;
+  __syncwarp();
   for (int k = 0; k < nw; ++k) {
-    const int depth = __shfl_sync(0xffffffffu, my_depth, k);
     const int n_items = __shfl_sync(0xffffffffu, my_items, k);
     const size_t region = (size_t)__shfl_sync(0xffffffffu, (unsigned long long)my_region, k);
-    if (depth == 0) continue;
-    int32_t* hist = d.ihist + region;
-    for (int t = lane; t < depth; t += 32) hist[t] = 0;
-    __syncwarp();
+#pragma unroll 8
     for (int t = lane; t < n_items; t += 32) atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
-    __syncwarp();
+  }
+  __syncwarp();
+  {
     int carry = 0;
-    for (int t0 = 0; t0 < depth; t0 += 32) {
+    for (int t0 = 0; t0 < max_depth; t0 += 32) {
       const int t = t0 + lane;
-      const int x = t < depth ? hist[t] : 0;
+      const int x = t < max_depth ? hist[t] : 0;
       int incl = x;
       for (int o = 1; o < 32; o <<= 1) {
         const int y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
       }
-      if (t < depth) hist[t] = carry + incl - x;
+      if (t < max_depth) hist[t] = carry + incl - x;
       carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    __syncwarp();
+  }
+  __syncwarp();
+  for (int k = 0; k < nw; ++k) {
+    const int n_items = __shfl_sync(0xffffffffu, my_items, k);
+    const size_t region = (size_t)__shfl_sync(0xffffffffu, (unsigned long long)my_region, k);
+#pragma unroll 8
     for (int t = lane; t < n_items; t += 32) {
-      const int pos = atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
-      d.isorted[region + pos] = d.items[region + t];
+      const int4 u = d.idesc[region + t];
+      gdesc[atomicAdd(&hist[d.ilevel[region + t] - 1], 1)] = u;
     }
-    __syncwarp();
   }
-  /* 4. levels: hist[L] is now the end of level L+1 within the world's region */
-  int32_t* pre = s_pre[wib];
+  __syncwarp();
+  if (hist != gh)
+    for (int t = lane; t < max_depth; t += 32) gh[t] = hist[t];
+  __syncwarp();
+  if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 2] = clock64();
+  /* 4. levels.  gh[L] is now the end of level L (0-based) in gdesc.  The
+   *    group's velocities move to the warp's shared slice when they fit (3
+   *    doubles per body), so the only dependent access per level is a
+   *    shared-memory load.  A two-deep software pipeline keeps everything else
+   *    off that path: while level L runs, the descriptors of level L+1 are in
+   *    registers with their constraint lines being pulled into L1, and the
+   *    descriptors and end offset of level L+2 are loading. */
+  const bool smem_vel = 6 * group_bodies <= smem_last_per_warp;
+  int32_t* dl = s_delta[wib];
+  if (lane < nw) {
+    const int wld = d.group_worlds[o0 + lane];
+    int base = 0;
+    for (int k = 0; k < lane; ++k) {
+      const int w2 = d.group_worlds[o0 + k];
+      base += d.world_body_off[w2 + 1] - d.world_body_off[w2];
+    }
+    dl[lane] = base - d.world_body_off[wld];
+  }
+  __syncwarp();
+  VelStore vs;
+  vs.d = &d;
+  vs.s = smem_vel ? reinterpret_cast<double*>(s_last) : nullptr;
+  if (smem_vel) {
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + lane; g < b1; g += 32) {
+        double* p = vs.s + 3 * (g + dl[k]);
+        p[0] = d.vx[g];
+        p[1] = d.vy[g];
+        p[2] = d.w[g];
+      }
+    }
+  }
+  __syncwarp();
+  const int4 none = make_int4(0, 0, 0, 0);
+  /* e_prev = start of level L, e_cur = end of level L, e_next = end of L+1 */
+  int e_prev = 0;
+  int e_cur = max_depth > 0 ? gh[0] : 0;
+  int e_next = max_depth > 1 ? gh[1] : e_cur;
+  int4 cur = lane < e_cur ? gdesc[lane] : none;
+  int4 nxt = e_cur + lane < e_next ? gdesc[e_cur + lane] : none;
+  if (lane < e_cur) prefetch_con(d.con + (cur.x & ~kWarmBit));
   for (int L = 0; L < max_depth; ++L) {
-    int cnt = 0, start = 0;
-    if (lane < nw && L < my_depth) {
-      const int32_t* hist = d.ihist + my_region;
-      start = L > 0 ? hist[L - 1] : 0;
-      cnt = hist[L] - start;
-    }
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (lane < nw) pre[lane] = incl - cnt;
-    if (lane == 0) pre[nw] = total;
-    __syncwarp();
-    for (int t = lane; t < total; t += 32) {
-      int k = 0;
-      while (pre[k + 1] <= t) ++k; /* world of the t-th update */
-      const size_t region = (size_t)__ldg(&d.world_contact_off[d.group_worlds[o0 + k]]) * stride;
-      const int32_t* hist = d.ihist + region;
-      const int st = L > 0 ? hist[L - 1] : 0;
-      solve_item(d, d.isorted[region + st + (t - pre[k])]);
+    /* issue level L+2's loads; they are consumed one iteration later */
+    const int e_next2 = L + 2 < max_depth ? gh[L + 2] : e_next;
+    const int4 nxt2 = e_next + lane < tot_items ? gdesc[e_next + lane] : none;
+    if (e_cur + lane < e_next) prefetch_con(d.con + (nxt.x & ~kWarmBit));
+    const int count = e_cur - e_prev;
+    if (lane < count)
+      solve_item(d, (uint32_t)cur.x, cur.y, cur.z, (uint8_t)(cur.w & 0xff), vs, dl[cur.w >> 8]);
+    for (int t = lane + 32; t < count; t += 32) { /* levels wider than a warp */
+      const int4 u = gdesc[e_prev + t];
+      solve_item(d, (uint32_t)u.x, u.y, u.z, (uint8_t)(u.w & 0xff), vs, dl[u.w >> 8]);
     }
     __syncwarp();
+    cur = nxt;
+    nxt = nxt2;
+    e_prev = e_cur;
+    e_cur = e_next;
+    e_next = e_next2;
   }
+  if (smem_vel) {
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + lane; g < b1; g += 32) {
+        const double* p = vs.s + 3 * (g + dl[k]);
+        d.vx[g] = p[0];
+        d.vy[g] = p[1];
+        d.w[g] = p[2];
+      }
+    }
+  }
+  if (d.phase_clock && lane == 0) {
+    d.phase_clock[8 * grp + 3] = clock64();
+    d.phase_clock[8 * grp + 4] = max_depth;
+    d.phase_clock[8 * grp + 5] = tot_items;
+    d.phase_clock[8 * grp + 6] = group_bodies;
+    d.phase_clock[8 * grp + 7] = nw;
+  }
+}
+
+/* Per-world solver residual after the last sweep: one more improveContactSln
+ * pass over the world's contacts that applies nothing (every contact sees the
+ * final velocities), reporting sqrt(mean over contacts of the normal and
+ * friction amounts it would apply, squared).  One warp per world, fixed
+ * summation order. */
+__global__ void k_residual(Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int wld = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (wld >= d.n_worlds) return;
+  const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+  double sum = 0.0;
+  for (int c = c0 + lane; c < c1; c += 32) {
+    const int ga = d.c_ga[c], gb = d.c_gb[c];
+    const double2* cp = reinterpret_cast<const double2*>(d.con + c);
+    double j_n[6], j_f[6];
+    const double2 a0 = cp[0], a1 = cp[1], a2 = cp[2], a3 = cp[3], a4 = cp[4], a5 = cp[5];
+    j_n[0] = a0.x; j_n[1] = a0.y; j_n[2] = a1.x; j_n[3] = a1.y; j_n[4] = a2.x; j_n[5] = a2.y;
+    j_f[0] = a3.x; j_f[1] = a3.y; j_f[2] = a4.x; j_f[3] = a4.y; j_f[4] = a5.x; j_f[5] = a5.y;
+    const double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
+    const double2 b6 = cp[6], b7 = cp[7], b8 = cp[8], b9 = cp[9], b10 = cp[10], b11 = cp[11], b12 = cp[12];
+    const double2 cached = reinterpret_cast<const double2*>(d.lam)[c];
+    const double nwa = -v[2];
+    const double cvx = ((-v[0] + (-(nwa * b7.y))) + v[3]) + (-(v[5] * b8.y));
+    const double cvy = ((-v[1] + nwa * b7.x) + v[4]) + v[5] * b8.x;
+    const double tb = b11.y * (cvx * b9.x + cvy * b9.y);
+    const double bias = b6.x + (f_le(0.0, tb) ? 0.0 : tb);
+    const double ln_new = div_rn(-(dot6(j_n, v) + bias), b10.x, b12.x);
+    const double lf_new = div_rn(-plus_zero(dot6(j_f, v)), b10.y, b12.y);
+    const double ln_apply = f_le(ln_new, -cached.x) ? -cached.x : ln_new;
+    const double thr = (cached.x + ln_apply) * b11.x;
+    const double acc = cached.y + lf_new;
+    const double acc2 = f_lt(thr, acc) ? thr : (f_lt(acc, -thr) ? -thr : acc);
+    const double lf_apply = acc2 - cached.y;
+    sum += ln_apply * ln_apply + lf_apply * lf_apply;
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) d.world_residual[wld] = c1 > c0 ? sqrt(sum / (2.0 * (c1 - c0))) : 0.0;
+}
+
+/* Per-world maximum penetration depth over the contacts of the last collide.
+ * One warp per world. */
+__global__ void k_world_depth(Dev d) {
+  const int lane = threadIdx.x & 31;
+  const int wld = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (wld >= d.n_worlds) return;
+  const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+  double m = 0.0;
+  for (int c = c0 + lane; c < c1; c += 32) m = fmax(m, d.c_val[5 * (size_t)c + 4]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) d.world_depth[wld] = m;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -300,3 +300,48 @@ def test_group_packing_matches_across_iteration_counts(iters):
     step_oracles(ow, sc, 60, iterations=iters)
     compare_bodies(b, ow, sc, f"iters {iters}")
     b.close()
+
+
+def test_autotune_keeps_state_and_results():
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=128), list(range(0, 128, 4)))
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 90)
+    step_oracles(ow, sc, 90)
+    before = b.get_bodies()
+    k0, l0, _ = b.get_cache()
+    wpg, thr = b.autotune(cfg, 3)
+    assert 1 <= wpg <= 32 and thr in (32, 64, 128)
+    after = b.get_bodies()
+    k1, l1, _ = b.get_cache()
+    for f in STATE_FIELDS:
+        assert_bits_equal(after[f], before[f], f"autotune restored {f}")
+    assert np.array_equal(k0, k1)
+    assert_bits_equal(l0, l1, "autotune restored cache")
+    b.step(cfg, 30)
+    step_oracles(ow, sc, 30)
+    compare_bodies(b, ow, sc, "after autotune")
+    b.close()
+
+
+def test_world_metrics_residual_and_depth():
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(16)))
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    b.step(config_of(sc), 100)
+    step_oracles(ow, sc, 100)
+    cfg = config_of(sc)
+    cfg.flags = _lib.SHAPES_FLAG_RESIDUAL
+    b.step(cfg, 1)
+    step_oracles(ow, sc, 1)
+    res, depth = b.world_metrics()
+    for w, o in enumerate(ow):
+        want = o.residual()
+        assert abs(res[w] - want) <= 1e-12 * max(1.0, abs(want)), (w, res[w], want)
+        o.collide()
+        _, vals = o.contacts()
+        want_d = max(0.0, vals[:, 4].max()) if len(vals) else 0.0
+        assert depth[w] == want_d
+    compare_bodies(b, ow, sc, "after metrics")
+    b.close()
