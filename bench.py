@@ -1,27 +1,35 @@
 """Benchmark of the GB300 world step: body-steps/s on one GB300 (or N, weak).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched|single|mixed]
+                    [--workload learned|batched|single]
 
-Workload (default `batched`): 4096 independent worlds whose body counts are
-log-uniform in [8, 512] (a static slab plus square boxes of side U[0.5, 2]
-dropped in a column), dt = 1/60, 8 solver sweeps, warm start from the
-previous frame's cache, gravity (0, -9.8), FP64 throughout.  Seeded synthetic
-data (the reference defines no benchmark dataset).  A step is one world step
-of every world in the batch; K steps are timed after W warm-up steps.
+Workload `learned` (default): 1024 independent worlds of 256 bodies - a static
+slab, then boxes and 3-8 vertex polygons (sizes U[0.4, 1.5], friction
+U[0.2, 0.8]) dropped from a jittered grid - dt = 1/60, gravity (0, -9.8),
+warm start from the previous frame's cache, FP64 throughout.  The plain solver
+runs 8 sweeps.  The learned warm start (a 16-64-64-64-2 network on the tensor
+cores, trained here on samples from plain runs of the batched workload below)
+is swept over 1-8 sweeps; the setting timed is the fastest whose mean solver
+residual and mean largest penetration are no worse than plain 8 sweeps', i.e.
+body-steps/s at matched residual.  `batched`: 4096 worlds, body counts
+log-uniform in [8, 512], boxes of side U[0.5, 2] in a column over a slab, 8
+sweeps.  Seeded synthetic data (the reference defines no benchmark dataset).
+A step is one world step of every world; K steps are timed after W warm-up
+steps, inputs larger than L2.
 
-value      body-steps/s with the state resident in HBM (CUDA events on the
-           library's stream around K steps), max over ranks.
+value      body-steps/s with the state resident in HBM: CUDA events on the
+           library's stream around K steps replayed from CUDA graphs, max
+           over ranks.
 e2e        the same steps through the public C ABI with host buffers: every
            step uploads the body state from pinned host memory, steps, and
            reads the state back.
-roofline   the solver kernel (the dominant one): algorithmic bytes per launch
-           over its measured average launch time against the measured HBM
-           copy bandwidth; `fp64` holds its FP64-pipe figure against the FP64
-           throughput this script measures on the device, the bound that
-           actually limits it on GB300.
+roofline   the solver kernel (the dominant one), from a separate profiled
+           pass: algorithmic bytes per launch over its average launch time
+           against the measured HBM copy bandwidth; `fp64` holds its FP64-pipe
+           figure against the FP64 throughput this script measures, the bound
+           that limits it on GB300.
 cpu_baseline  the CPU oracle (a sequential C++ restatement of the reference
-           step) on this host's cores, on a bounded sample of the workload.
+           step, plain start, 8 sweeps) on this host's cores.
 --impl reference  the oracle alone, all host threads, same workload/metric.
 """
 from __future__ import annotations
@@ -51,11 +59,14 @@ UNIT = "body-steps/s"
 SOLVER_BYTES_PER_ITEM = (152 + 16 + 2 * (24 + 16 + 16)) + (2 * 24 + 16)
 
 WORKLOADS = {
+    "learned": "1024 worlds x 256 mixed boxes and 3-8 vertex polygons (sizes U[0.4,1.5], friction U[0.2,0.8]), "
+               "dt 1/60, gravity (0,-9.8); plain start at 8 sweeps vs the learned start at 1-8 sweeps, the "
+               "fastest setting no worse than plain 8 in mean residual and mean largest penetration is timed",
     "batched": "4096 worlds, bodies log-uniform [8,512] (slab + boxes side U[0.5,2] in a column), "
                "dt 1/60, 8 sweeps, warm start, gravity (0,-9.8)",
     "single": "1 world: 100x1 slab + 20x20 unit squares, dt 1/60, 4 sweeps, warm start",
-    "mixed": "1024 worlds x 256 mixed boxes and 3-8 vertex polygons, friction U[0.2,0.8], dt 1/60, 8 sweeps",
 }
+PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4}
 
 
 def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
@@ -65,7 +76,7 @@ def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
         return scenes.batched_columns(seed=2 + seed_offset, n_worlds=worlds or 4096)
     if workload == "single":
         return scenes.single_world_boxes(seed=0 + seed_offset)
-    if workload == "mixed":
+    if workload == "learned":
         return scenes.batched_mixed(seed=3 + seed_offset, n_worlds=worlds or 1024)
     raise SystemExit(f"unknown workload {workload}")
 
@@ -248,6 +259,75 @@ def run_reference(args, rank, world):
     return 0
 
 
+def new_batch(_lib, scene, stream, tuned=None):
+    b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
+    b.set_stream(stream.cuda_stream)
+    if tuned:
+        b.set_launch_groups(*tuned)
+    return b
+
+
+def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10):
+    """Steps a fresh copy with the residual flag: (mean over steps of the
+    world-mean residual, mean over sampled steps of the world-mean largest
+    depth, per-world max residual, per-world max depth, contacts started by
+    the network)."""
+    c = scene["config"]
+    cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], iterations, residual=True,
+                           learned=net is not None)
+    b = new_batch(_lib, scene, stream)
+    if net is not None:
+        b.set_mlp(net)
+    W = b.n_worlds
+    res_sum, dep_sum, n_dep, predicted = 0.0, 0.0, 0, 0
+    wres = np.zeros(W)
+    wdep = np.zeros(W)
+    r = np.empty(W)
+    L = _lib.lib()
+    for s_ in range(steps):
+        b.step(cfg, 1)
+        predicted += b.stats()["predicted"]
+        _lib.check(L.shapes_batch_get_world_metrics(b.handle, r.ctypes.data_as(_lib._dp), None), "metrics")
+        res_sum += float(r.mean())
+        np.maximum(wres, r, out=wres)
+        if (s_ + 1) % depth_every == 0 or s_ + 1 == steps:
+            _, d = b.world_metrics()
+            dep_sum += float(d.mean())
+            n_dep += 1
+            np.maximum(wdep, d, out=wdep)
+    b.close()
+    return res_sum / steps, dep_sum / max(n_dep, 1), wres, wdep, predicted
+
+
+def train_network(_lib, stream, args, rank):
+    """Samples of new contacts from plain runs of the batched workload (a
+    different seed from every timed scene), then Adam on the tensor cores."""
+    t0 = time.time()
+    sc = make_scene("batched", seed_offset=100 + rank, worlds=args.train_worlds)
+    c = sc["config"]
+    cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], PLAIN_ITERATIONS["batched"])
+    b = new_batch(_lib, sc, stream)
+    b.collect(args.train_samples)
+    b.step(cfg, args.train_steps)
+    feat, tgt = b.samples()
+    b.close()
+    t1 = time.time()
+    net = _lib.Mlp(seed=1)
+    net.fit_normalization(feat, tgt)
+    losses = net.train(feat, tgt, epochs=args.train_epochs, batch=4096, lr=2e-3, seed=1)
+    torch_sync()
+    return net, {"samples": int(len(feat)), "source": f"plain runs of the batched workload (seed offset {100 + rank}, "
+                 f"{args.train_worlds} worlds x {args.train_steps} steps)", "epochs": args.train_epochs,
+                 "batch": 4096, "lr": 2e-3, "first_loss": float(losses[0]), "final_loss": float(losses[-1]),
+                 "collect_s": t1 - t0, "train_s": time.time() - t1}
+
+
+def torch_sync():
+    import torch
+
+    torch.cuda.synchronize()
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -258,50 +338,96 @@ def run_ours(args, rank, world, local):
     G.build()
     scene = make_scene(args.workload, seed_offset=rank, worlds=args.worlds)
     c = scene["config"]
-    cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"])
+    plain_it = PLAIN_ITERATIONS[args.workload]
     n_bodies = int(scene["world_body_offsets"][-1])
     stream = torch.cuda.current_stream()
+
+    # ---- learned warm start: train, then sweep sweeps at matched quality ----
+    net, learned = None, None
+    run_it, run_learned = plain_it, False
+    if args.workload == "learned":
+        net, train_info = train_network(_lib, stream, args, rank)
+        qs = min(args.steps, args.quality_steps)
+        p_res, p_dep, p_wres, p_wdep, _ = quality_run(_lib, scene, stream, plain_it, qs)
+        sweep = []
+        for it in range(1, plain_it + 1):
+            l_res, l_dep, _, _, pred = quality_run(_lib, scene, stream, it, qs, net=net)
+            row = {"iterations": it, "learned_residual": l_res, "learned_depth": l_dep,
+                   "predicted_per_step": pred / qs}
+            if args.plain_sweep or it == plain_it:
+                q = (p_res, p_dep) if it == plain_it else quality_run(_lib, scene, stream, it, qs)[:2]
+                row["plain_residual"], row["plain_depth"] = q
+            sweep.append(row)
+        matched = [r_["iterations"] for r_ in sweep
+                   if r_["learned_residual"] <= p_res and r_["learned_depth"] <= p_dep]
+        learned = {"training": train_info, "quality_steps": qs,
+                   "plain": {"iterations": plain_it, "residual": p_res, "depth": p_dep},
+                   "sweep": sweep, "matched_iterations": min(matched) if matched else None,
+                   "judge": "per world: back to the plain start once its residual exceeds the plain run's "
+                            "largest residual of that world, or its largest depth the plain run's"}
+        if matched:
+            run_it, run_learned = min(matched), True
+
+    def cfg_for(it, use_net):
+        return _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], it, learned=use_net)
 
     # ---- autotune the solver packing on a settled copy (setup, untimed) ------
     tuned = None
     if not args.no_tune:
-        t = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
-        t.set_stream(stream.cuda_stream)
-        t.step(cfg, args.tune_after)
-        tuned = t.autotune(cfg, args.tune_steps)
+        t = new_batch(_lib, scene, stream)
+        t.step(cfg_for(plain_it, False), args.tune_after)
+        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps)
         t.close()
 
-    # ---- value: state resident in HBM -------------------------------------
-    b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
-    b.set_stream(stream.cuda_stream)
-    if tuned:
-        b.set_launch_groups(*tuned)
-    b.step(cfg, args.warmup)
-    b.set_profiling(True)
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
+    def timed(it, use_net):
+        """K steps after W warm-up from a fresh copy; returns (ms, batch)."""
+        b = new_batch(_lib, scene, stream, tuned)
+        if use_net:
+            b.set_mlp(net)
+            b.set_judge(p_wres, p_wdep)
+        cfg = cfg_for(it, use_net)
+        b.step(cfg, args.warmup)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        torch.cuda.synchronize()
         t0.record(stream)
         b.step(cfg, args.steps)
         t1.record(stream)
         torch.cuda.synchronize()
-    barrier(world)
-    ms = t0.elapsed_time(t1)
-    prof = b.get_profile()
-    st = b.stats()
-    b.set_profiling(False)
-    ms_max = max_over_ranks(ms, world)
+        barrier(world)
+        return t0.elapsed_time(t1), b, cfg
+
+    # ---- value: state resident in HBM, graphs, no profiler events -----------
     total_bodies = sum_over_ranks(float(n_bodies), world)
-    value = total_bodies * args.steps / (ms_max * 1e-3)
-    launches = int(sum(v[1] for v in prof.values()))
+    plain_ms = None
+    if run_learned:
+        plain_ms, bp, _ = timed(plain_it, False)
+        bp.close()
+    with ClockSampler(local) as clocks:
+        ms, b, cfg = timed(run_it, run_learned)
+    st = b.stats()
+    # stage times and launches from a profiled pass of the same batch (untimed)
+    prof_steps = min(args.steps, 30)
+    b.set_profiling(True)
+    b.step(cfg, prof_steps)
+    prof = b.get_profile()
+    st_prof = b.stats()
+    b.set_profiling(False)
     b.close()
+    ms_max = max_over_ranks(ms, world)
+    value = total_bodies * args.steps / (ms_max * 1e-3)
+    launches_per_step = sum(v[1] for v in prof.values()) / prof_steps
+    if learned is not None:
+        learned["plain_value"] = (total_bodies * args.steps / (max_over_ranks(plain_ms, world) * 1e-3)
+                                  if plain_ms else value)
+        learned["timed"] = {"start": "learned" if run_learned else "plain", "iterations": run_it,
+                            "predicted_per_step": st["predicted"] / args.steps, "reverted": st["reverted"]}
 
     # ---- e2e: host buffers through the C ABI every step --------------------
-    b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
-    b.set_stream(stream.cuda_stream)
-    if tuned:
-        b.set_launch_groups(*tuned)
+    b = new_batch(_lib, scene, stream, tuned)
+    if run_learned:
+        b.set_mlp(net)
+        b.set_judge(p_wres, p_wdep)
     b.step(cfg, args.warmup)
     host_in = {f: torch.empty(n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
     host_out = {f: torch.empty(n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
@@ -330,23 +456,24 @@ def run_ours(args, rank, world, local):
     e2e_value = total_bodies * e_steps / (e_ms * 1e-3)
     b.close()
 
-    # ---- roofline of the dominant kernel ------------------------------------
+    # ---- roofline of the dominant kernel (profiled pass) -------------------
     solve_ms, solve_launches = prof["solve"]
-    items = st["solver_items"]
+    items = st_prof["solver_items"]
     peaks = measured_peaks()
     roof = None
-    fp64 = None
     if solve_launches and solve_ms > 0:
         avg_ms = solve_ms / solve_launches
         bytes_per_launch = items / solve_launches * SOLVER_BYTES_PER_ITEM
         achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-        roof = {"kernel": "k_solve", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+        roof = {"kernel": "k_schedule_solve", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": None, "bytes_per_item": SOLVER_BYTES_PER_ITEM,
+                "traffic": items / solve_launches * SOLVER_DRAM_BYTES_PER_ITEM,
+                "traffic_source": "ncu dram bytes per update (512-world capture) x updates per launch",
+                "bytes_per_item": SOLVER_BYTES_PER_ITEM,
                 "items_per_launch": items / solve_launches, "avg_launch_ms": avg_ms}
         fp64_peak = measure_fp64_peak()
         if fp64_peak:
-            fp64 = {"kernel": "k_solve", "peak_lane_ops_per_s": fp64_peak,
+            fp64 = {"kernel": "k_schedule_solve", "peak_lane_ops_per_s": fp64_peak,
                     "peak_source": "measured by this script (fp64 add/mul chains)",
                     "ops_per_item": SOLVER_FP64_OPS_PER_ITEM,
                     "achieved_lane_ops_per_s": items * SOLVER_FP64_OPS_PER_ITEM / (solve_ms * 1e-3)}
@@ -359,13 +486,11 @@ def run_ours(args, rank, world, local):
         import multiprocessing
 
         cores = multiprocessing.cpu_count()
-        # the same worlds and the same steps as the timed GPU region (capped at
-        # 300 steps so the default run stays within a few minutes)
         cs = min(args.steps, 300)
         rate, n, s_, secs = cpu_oracle_rate(scene, cs, args.warmup, cores)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"all {n} bodies x {s_} steps after {args.warmup} warm-up (the timed GPU steps), "
-                         f"{secs:.1f} s on {cores} threads"}
+               "sample": f"all {n} bodies x {s_} steps after {args.warmup} warm-up, plain start, "
+                         f"{int(c['iterations'])} sweeps, {secs:.1f} s on {cores} threads"}
 
     if rank == 0:
         line = {
@@ -374,27 +499,37 @@ def run_ours(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
                        "bodies_per_gpu": n_bodies, "worlds_per_gpu": int(len(scene["world_body_offsets"]) - 1),
-                       "iterations": int(c["iterations"]), "warm_start": "plain (previous-frame cache)",
+                       "iterations": run_it, "start": "learned" if run_learned else "plain (previous-frame cache)",
                        "parallelism": f"worlds sharded, {world} rank(s)",
-                       "l2": "working set (state + contacts + constraints) larger than L2",
+                       "l2": "inputs larger than L2 (state + contacts + constraints of all worlds)",
+                       "launch": "CUDA graph per step",
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1]} if tuned else "default"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * n_bodies,
                     "d2h_bytes_per_step": 10 * 8 * n_bodies},
-            "gpu_launches": launches,
+            "gpu_launches": int(round(launches_per_step * args.steps)),
             "clocks": clocks.summary(),
-            "stages_ms": {k: v[0] for k, v in prof.items()},
+            "stages_ms_per_step": {k: v[0] / prof_steps for k, v in prof.items()},
             "last_step": {"pairs": st["pairs"], "contacts": st["contacts"]},
         }
+        if learned is not None:
+            line["learned"] = learned
         print(json.dumps(line), flush=True)
+    if net is not None:
+        net.close()
     return 0
 
 
-# FP64 lane-operations per solver update (adds, multiplies, divisions and
-# comparisons issued to the FP64 pipe), counted from the ncu instruction mix of
-# k_solve divided by its updates.
-SOLVER_FP64_OPS_PER_ITEM = 110
+# FP64 lane-operations per solver update: ncu's dadd + dmul + dfma thread
+# instruction counts of one k_schedule_solve launch (26.9 M) divided by its
+# 370,978 updates (batched workload, 512 worlds, settled frame); the hand count
+# is 69 per sweep update and 36 per warm-start update.
+SOLVER_FP64_OPS_PER_ITEM = 72.5
+# DRAM bytes per solver update in the same capture (dram__bytes_read.sum +
+# dram__bytes_write.sum = 12.70 MB over 370,978 updates): the working set is
+# L2-resident, so traffic is far below the algorithmic bytes.
+SOLVER_DRAM_BYTES_PER_ITEM = 34.2
 
 
 def main():
@@ -403,12 +538,18 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="batched")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="learned")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--worlds", type=int, default=None, help="override the world count (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the solver-packing autotuner")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
     ap.add_argument("--tune-steps", type=int, default=4, help="steps per autotuner trial")
+    ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
+    ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
+    ap.add_argument("--train-worlds", type=int, default=4096, help="worlds of the sample-collection run")
+    ap.add_argument("--train-steps", type=int, default=300, help="steps of the sample-collection run")
+    ap.add_argument("--train-samples", type=int, default=2_000_000, help="at most this many training samples")
+    ap.add_argument("--train-epochs", type=int, default=10, help="Adam epochs over the samples")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -93,6 +93,12 @@ typedef struct shapes_config {
  * its results differ too.  No counterpart in the reference. */
 #define SHAPES_FLAG_COLOURED 2
 #define SHAPES_LARGE_WORLD_BODIES 4096
+/* Learned warm start: contacts without a cache entry (the `newCache` branch
+ * of applyCachedSlns, Solvers/Contact.hs:91-98, where the reference starts
+ * from zero) start from the Lagrangians the attached network predicts, in
+ * worlds whose learned mask is set (shapes_batch_set_mlp).  The results then
+ * differ from the reference's.  No counterpart in the reference. */
+#define SHAPES_FLAG_LEARNED 4
 
 /* Counters of the most recent step or collide call, summed over worlds.
  * pairs and contacts are those of the call's last step; cache_hits,
@@ -104,6 +110,8 @@ typedef struct shapes_stats {
   int64_t solver_items;  /* warm-start applications + sweep updates */
   int64_t solver_levels; /* sum over steps and solver groups of dependency levels */
   int64_t retries;       /* buffer regrowths during the last call */
+  int64_t predicted;     /* contacts started from the network, summed over the call */
+  int64_t reverted;      /* worlds switched back to the plain start during the call */
 } shapes_stats;
 
 typedef struct shapes_batch shapes_batch;
@@ -215,12 +223,20 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
  * returns to the handle's own stream.  The stream must stay valid while set. */
 int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream);
 
+/* CUDA-graph replay of the step (default on): each step is captured once per
+ * configuration and buffer layout and replayed with one graph launch; steps
+ * are launched kernel by kernel while profiling, or when the stream is a
+ * legacy default stream or already capturing.  Results are identical either
+ * way. */
+int shapes_batch_set_graphs(shapes_batch* b, int32_t enabled);
+
 /* Per-stage device timing.  While enabled, CUDA events on the handle's stream
  * bracket each stage of every step; get_profile returns the accumulated
  * milliseconds and kernel launches per stage since profiling was enabled or
  * last read (reading resets).  Stages, in order: broadphase, narrowphase,
- * constraint build, solver schedule, solver, integrate+pose, scans/offsets. */
-#define SHAPES_STAGE_COUNT 7
+ * constraint build, solver schedule, solver, integrate+pose, scans/offsets,
+ * learned warm start (features, network, judge, sample collection). */
+#define SHAPES_STAGE_COUNT 8
 int shapes_batch_set_profiling(shapes_batch* b, int32_t enabled);
 int shapes_batch_get_profile(shapes_batch* b, double* ms, int64_t* launches);
 /* While profiling: per solver group of the last step, 8 int64 each
@@ -268,6 +284,74 @@ int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, const double* 
                            int64_t pair_capacity, int32_t* contact_keys5, double* contact_vals5,
                            int64_t contact_capacity, void* cuda_stream, int64_t* n_pairs,
                            int64_t* n_contacts);
+
+/* ------------------------------------------------------------------------ */
+/* Learned warm start (no counterpart in the reference)                      */
+/* ------------------------------------------------------------------------ */
+
+/* A 16 -> 64 -> 64 -> 64 -> 2 ReLU network (BF16 tensor-core products, FP32
+ * accumulation, FP32 master weights) mapping 16 contact features to the
+ * starting normal and friction Lagrangians of a contact without a cache
+ * entry.  Parameters: 9538 floats, W1[64][16] b1[64] W2[64][64] b2[64]
+ * W3[64][64] b3[64] W4[2][64] b4[2] (row = output).  Normalisation: 36
+ * floats, feature mean[16], feature 1/scale[16], target mean[2], target
+ * scale[2]; the network sees (f - mean) / scale and predicts
+ * (target - mean) / scale.  Features, in order: J_n.v, J_f.v, b_n, J_n M^-1
+ * J_n^T, J_f M^-1 J_f^T, the isolated normal and friction updates, pair
+ * friction, depth, normal x, normal y, one step of acceleration as a normal
+ * impulse, contacts of the pair, one-body-static flag, the two angular
+ * entries of the normal row. */
+#define SHAPES_MLP_PARAMS 9538
+#define SHAPES_MLP_NORM 36
+#define SHAPES_MLP_FEATURES 16
+typedef struct shapes_mlp shapes_mlp;
+
+typedef struct shapes_train_config {
+  int32_t epochs;
+  int32_t batch; /* samples per Adam step, a multiple of 128 */
+  float lr;      /* Adam learning rate (beta1 0.9, beta2 0.999, eps 1e-8) */
+  uint64_t seed; /* shuffling */
+} shapes_train_config;
+
+/* He-uniform initialisation from `seed`; identity normalisation. */
+int shapes_mlp_create(uint64_t seed, shapes_mlp** out);
+void shapes_mlp_destroy(shapes_mlp* m);
+int shapes_mlp_get_params(shapes_mlp* m, float* params, float* norm);
+/* Either pointer may be NULL; new parameters reset the Adam state. */
+int shapes_mlp_set_params(shapes_mlp* m, const float* params, const float* norm);
+/* Sets the normalisation to the mean and standard deviation of a dataset. */
+int shapes_mlp_fit_normalization(shapes_mlp* m, const float* features, const float* targets, int64_t n);
+/* Predictions (de-normalised, unclamped) for n feature rows. */
+int shapes_mlp_forward(shapes_mlp* m, const float* features, int64_t n, float* out2);
+/* Gradient of the mean over n samples (n <= 2^20) of the squared error of
+ * the normalised outputs; *loss gets that mean.  No update. */
+int shapes_mlp_gradient(shapes_mlp* m, const float* features, const float* targets, int64_t n,
+                        float* grad, float* loss);
+/* Adam on the GPU over shuffled mini-batches; epoch_loss[e] (optional) is
+ * epoch e's mean loss. */
+int shapes_mlp_train(shapes_mlp* m, const float* features, const float* targets, int64_t n,
+                     const shapes_train_config* tc, float* epoch_loss);
+
+/* Attaches a network to a handle (NULL detaches).  The handle reads the
+ * network's device parameters at each step; keep it alive while attached.
+ * Every world's learned mask is set. */
+int shapes_batch_set_mlp(shapes_batch* b, const shapes_mlp* m);
+/* Per-world learned mask (n_worlds bytes, 1 = predicted start).  The judge
+ * clears a world's byte when, after a step with SHAPES_FLAG_LEARNED, the
+ * world's residual exceeds max_residual[w] or its largest contact depth
+ * exceeds max_depth[w] (shapes_batch_set_judge); the world then starts from
+ * the plain cache until its byte is set again. */
+int shapes_batch_get_learned_mask(shapes_batch* b, uint8_t* mask);
+int shapes_batch_set_learned_mask(shapes_batch* b, const uint8_t* mask);
+/* Per-world limits of the judge (n_worlds doubles each; NULL = no limit). */
+int shapes_batch_set_judge(shapes_batch* b, const double* max_residual, const double* max_depth);
+/* Training samples: while capacity > 0, every step appends, for each contact
+ * without a cache entry, its 16 features (before the solve) and its final
+ * normal and friction Lagrangians (after the last sweep), up to `capacity`
+ * samples in all.  capacity 0 stops and frees the buffer. */
+int shapes_batch_collect(shapes_batch* b, int64_t capacity);
+int shapes_batch_get_samples(shapes_batch* b, float* features, float* targets, int64_t capacity,
+                             int64_t* n);
 
 /* Single-world convenience wrappers over a batch of one world. */
 int shapes_world_create(int32_t n_bodies, const shapes_bodies* bodies, const int32_t* vert_offsets,

@@ -31,15 +31,20 @@ SHAPES_WARM_START_OFF = 0
 SHAPES_WARM_START_CACHE = 1
 SHAPES_FLAG_RESIDUAL = 1
 SHAPES_FLAG_COLOURED = 2
+SHAPES_FLAG_LEARNED = 4
 SHAPES_LARGE_WORLD_BODIES = 4096
+SHAPES_MLP_PARAMS = 9538
+SHAPES_MLP_NORM = 36
+SHAPES_MLP_FEATURES = 16
 
-STAGE_NAMES = ("broadphase", "narrowphase", "build", "schedule", "solve", "integrate", "scan")
+STAGE_NAMES = ("broadphase", "narrowphase", "build", "schedule", "solve", "integrate", "scan", "learned")
 STAGE_COUNT = len(STAGE_NAMES)
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
 _lp = ctypes.POINTER(ctypes.c_int64)
 _up = ctypes.POINTER(ctypes.c_uint8)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 
 class Bodies(ctypes.Structure):
@@ -69,7 +74,12 @@ class Config(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
-        "pairs", "contacts", "cache_hits", "solver_items", "solver_levels", "retries")]
+        "pairs", "contacts", "cache_hits", "solver_items", "solver_levels", "retries", "predicted", "reverted")]
+
+
+class TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_int32), ("batch", ctypes.c_int32), ("lr", ctypes.c_float),
+                ("seed", ctypes.c_uint64)]
 
 
 class ShapesError(RuntimeError):
@@ -123,6 +133,22 @@ SIGNATURES = [
                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, _lp, _lp]),
+    ("shapes_mlp_create", ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    ("shapes_mlp_destroy", None, [ctypes.c_void_p]),
+    ("shapes_mlp_get_params", ctypes.c_int, [ctypes.c_void_p, _fp, _fp]),
+    ("shapes_mlp_set_params", ctypes.c_int, [ctypes.c_void_p, _fp, _fp]),
+    ("shapes_mlp_fit_normalization", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64]),
+    ("shapes_mlp_forward", ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_int64, _fp]),
+    ("shapes_mlp_gradient", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _fp, _fp]),
+    ("shapes_mlp_train", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, ctypes.POINTER(TrainConfig),
+                                        _fp]),
+    ("shapes_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_set_mlp", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("shapes_batch_get_learned_mask", ctypes.c_int, [ctypes.c_void_p, _up]),
+    ("shapes_batch_set_learned_mask", ctypes.c_int, [ctypes.c_void_p, _up]),
+    ("shapes_batch_set_judge", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    ("shapes_batch_collect", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    ("shapes_batch_get_samples", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _lp]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]
@@ -302,11 +328,120 @@ class Batch:
     def set_launch(self, target_bodies_per_group: int, threads: int) -> None:
         check(lib().shapes_batch_set_launch(self._h, target_bodies_per_group, threads), "shapes_batch_set_launch")
 
+    def set_graphs(self, enabled: bool) -> None:
+        """CUDA-graph replay of the step (default on)."""
+        check(lib().shapes_batch_set_graphs(self._h, int(bool(enabled))), "shapes_batch_set_graphs")
+
+    # ---- learned warm start ----
+    def set_mlp(self, net: "Mlp | None") -> None:
+        """Attach a network (every world's learned mask is set); None detaches."""
+        self._mlp = net
+        check(lib().shapes_batch_set_mlp(self._h, net.handle if net is not None else None), "shapes_batch_set_mlp")
+
+    def learned_mask(self) -> np.ndarray:
+        m = np.zeros(self.n_worlds, dtype=np.uint8)
+        check(lib().shapes_batch_get_learned_mask(self._h, _ptr(m, _up)), "shapes_batch_get_learned_mask")
+        return m
+
+    def set_learned_mask(self, mask) -> None:
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        check(lib().shapes_batch_set_learned_mask(self._h, _ptr(m, _up)), "shapes_batch_set_learned_mask")
+
+    def set_judge(self, max_residual=None, max_depth=None) -> None:
+        r = None if max_residual is None else np.ascontiguousarray(max_residual, dtype=np.float64)
+        d = None if max_depth is None else np.ascontiguousarray(max_depth, dtype=np.float64)
+        check(lib().shapes_batch_set_judge(self._h, None if r is None else _ptr(r, _dp),
+                                           None if d is None else _ptr(d, _dp)), "shapes_batch_set_judge")
+
+    def collect(self, capacity: int) -> None:
+        """Start (capacity > 0) or stop (0) appending training samples every step."""
+        check(lib().shapes_batch_collect(self._h, int(capacity)), "shapes_batch_collect")
+
+    def samples(self) -> tuple[np.ndarray, np.ndarray]:
+        n = ctypes.c_int64()
+        st = lib().shapes_batch_get_samples(self._h, None, None, 0, ctypes.byref(n))
+        if st not in (SHAPES_OK, SHAPES_E_BUFFER):
+            check(st, "shapes_batch_get_samples")
+        f = np.empty((max(n.value, 1), SHAPES_MLP_FEATURES), dtype=np.float32)
+        t = np.empty((max(n.value, 1), 2), dtype=np.float32)
+        check(lib().shapes_batch_get_samples(self._h, _ptr(f, _fp), _ptr(t, _fp), n.value, ctypes.byref(n)),
+              "shapes_batch_get_samples")
+        return f[: n.value], t[: n.value]
+
+
+class Mlp:
+    """The learned warm start network (shapes_mlp): tensor-core forward,
+    backward and Adam training on the current CUDA device."""
+
+    def __init__(self, seed: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().shapes_mlp_create(int(seed), ctypes.byref(h)), "shapes_mlp_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().shapes_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> tuple[np.ndarray, np.ndarray]:
+        p = np.empty(SHAPES_MLP_PARAMS, dtype=np.float32)
+        n = np.empty(SHAPES_MLP_NORM, dtype=np.float32)
+        check(lib().shapes_mlp_get_params(self._h, _ptr(p, _fp), _ptr(n, _fp)), "shapes_mlp_get_params")
+        return p, n
+
+    def set_params(self, params=None, norm=None) -> None:
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, dtype=np.float32)
+        check(lib().shapes_mlp_set_params(self._h, None if p is None else _ptr(p, _fp),
+                                          None if n is None else _ptr(n, _fp)), "shapes_mlp_set_params")
+
+    def fit_normalization(self, features, targets) -> None:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        check(lib().shapes_mlp_fit_normalization(self._h, _ptr(f, _fp), _ptr(t, _fp), len(f)),
+              "shapes_mlp_fit_normalization")
+
+    def forward(self, features) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.empty((len(f), 2), dtype=np.float32)
+        check(lib().shapes_mlp_forward(self._h, _ptr(f, _fp), len(f), _ptr(out, _fp)), "shapes_mlp_forward")
+        return out
+
+    def gradient(self, features, targets) -> tuple[np.ndarray, float]:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.empty(SHAPES_MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        check(lib().shapes_mlp_gradient(self._h, _ptr(f, _fp), _ptr(t, _fp), len(f), _ptr(g, _fp),
+                                        ctypes.byref(loss)), "shapes_mlp_gradient")
+        return g, float(loss.value)
+
+    def train(self, features, targets, epochs: int = 10, batch: int = 4096, lr: float = 1e-3,
+              seed: int = 0) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        losses = np.zeros(epochs, dtype=np.float32)
+        tc = TrainConfig(int(epochs), int(batch), float(lr), int(seed))
+        check(lib().shapes_mlp_train(self._h, _ptr(f, _fp), _ptr(t, _fp), len(f), ctypes.byref(tc),
+                                     _ptr(losses, _fp)), "shapes_mlp_train")
+        return losses
+
 
 def make_config(dt: float, baumgarte: float = 0.01, slop: float = 0.02, accel=(0.0, -9.8),
                 iterations: int = 2, warm_start: bool = True, external: bool = True,
-                residual: bool = False, coloured: bool = False) -> Config:
+                residual: bool = False, coloured: bool = False, learned: bool = False) -> Config:
     return Config(dt, baumgarte, slop, float(accel[0]), float(accel[1]), int(iterations),
                   SHAPES_WARM_START_CACHE if warm_start else SHAPES_WARM_START_OFF,
                   SHAPES_EXTERNAL_CONSTANT_ACCEL if external else SHAPES_EXTERNAL_NONE,
-                  (SHAPES_FLAG_RESIDUAL if residual else 0) | (SHAPES_FLAG_COLOURED if coloured else 0))
+                  (SHAPES_FLAG_RESIDUAL if residual else 0) | (SHAPES_FLAG_COLOURED if coloured else 0)
+                  | (SHAPES_FLAG_LEARNED if learned else 0))

@@ -149,3 +149,70 @@ extern "C" int shapes_probe_cmp_check(const double* host_vals, int n, unsigned l
   cudaFree(d_bad);
   return err == cudaSuccess ? 0 : -5;
 }
+
+/* ------------------------------------------------------------------------ */
+/* tcgen05 BF16 GEMM check: D (128 x N, FP32) = A (128 x K) * B (N x K)^T    */
+/* with the operand layout and descriptors of tc05.cuh, one CTA.             */
+/* ------------------------------------------------------------------------ */
+#include "tc05.cuh"
+
+__global__ void k_tc05_gemm_check(const float* A, const float* B, int N, int K, float* D, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tbase;
+  unsigned char* sa = smem;
+  unsigned char* sb = smem + 128 * 128 * 2;
+  const int t = threadIdx.x;
+  for (int k = 0; k < K; ++k) *reinterpret_cast<uint16_t*>(sa + tc05::kmaj(t, k, K)) = tc05::bf16_bits(A[t * K + k]);
+  for (int r = t; r < N; r += 128)
+    for (int k = 0; k < K; ++k) *reinterpret_cast<uint16_t*>(sb + tc05::kmaj(r, k, K)) = tc05::bf16_bits(B[r * K + k]);
+  if (t == 0) tc05::mbar_init(&bar, 1);
+  if (t < 32) tc05::tmem_alloc(&tbase, 256);
+  tc05::fence_async_smem();
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  const uint32_t base = tbase;
+  if (t == 0) {
+    tc05::gemm(base, tc05::smem_addr(sa), tc05::smem_addr(sb), 128, N, K, false);
+    tc05::commit(&bar);
+  }
+  const bool ok = tc05::mbar_wait(&bar, 0);
+  if (!ok && (t & 31) == 0) atomicExch(err, 1);
+  tc05::fence_after();
+  const int w = t >> 5;
+  for (int c = 0; c < N; c += 16) {
+    float v[16];
+    tc05::tmem_ld16(tc05::taddr(base, 32 * w, c), v);
+    for (int k = 0; k < 16; ++k) D[t * N + c + k] = ok ? v[k] : 0.f;
+  }
+  tc05::fence_before();
+  __syncthreads();
+  if (t < 32) tc05::tmem_free(base, 256);
+}
+
+extern "C" int shapes_probe_tc05_gemm(const float* A, const float* B, int N, int K, float* D) {
+  if (N < 16 || N > 256 || (N & 15) || K < 16 || K > 128 || (K & 15)) return -1;
+  float *dA = nullptr, *dB = nullptr, *dD = nullptr;
+  int* dErr = nullptr;
+  cudaError_t e = cudaMalloc(&dA, sizeof(float) * 128 * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, sizeof(float) * N * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dD, sizeof(float) * 128 * N);
+  if (e == cudaSuccess) e = cudaMalloc(&dErr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dErr, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(dA, A, sizeof(float) * 128 * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, B, sizeof(float) * N * K, cudaMemcpyHostToDevice);
+  const int smem = 128 * 128 * 2 + 256 * 128 * 2 + 16384; /* operands + slack */
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tc05_gemm_check, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) {
+    k_tc05_gemm_check<<<1, 128, smem>>>(dA, dB, N, K, dD, dErr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dErr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(D, dD, sizeof(float) * 128 * N, cudaMemcpyDeviceToHost);
+  cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(dErr);
+  if (e != cudaSuccess) return -5;
+  return herr ? -6 : 0;
+}

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <string>
 #include <vector>
@@ -23,13 +24,16 @@
 #include "../../include/shapes_gpu.h"
 #include "step_kernels.cuh"
 #include "large_world.cuh"
+#include "learned.cuh"
+#include "mlp.h"
 
 using shapes::Con;
 using shapes::Dev;
 
-namespace {
-
+/* Text of the last CUDA error on this thread (shared with the MLP unit). */
 thread_local std::string g_last_error;
+
+namespace {
 
 struct CudaError {
   cudaError_t err;
@@ -179,6 +183,25 @@ struct shapes_batch {
   double* world_residual = nullptr;
   double* world_depth = nullptr;
   bool residual_valid = false;
+  /* learned warm start */
+  const shapes_mlp* mlp_model = nullptr;
+  uint8_t* learned_mask = nullptr; /* [W] */
+  double* judge_res = nullptr;     /* [W] */
+  double* judge_depth = nullptr;   /* [W] */
+  bool judge_set = false;
+  int32_t miss_cap = 0;            /* contact capacity the row buffers were sized for */
+  int32_t* miss_flag = nullptr;
+  int32_t* miss_off = nullptr;
+  int32_t* miss_ids = nullptr;
+  int32_t* miss_n = nullptr;
+  float* mfeat = nullptr;
+  /* training samples */
+  float* ds_feat = nullptr;
+  float* ds_tgt = nullptr;
+  int64_t ds_cap = 0;
+  unsigned long long* ds_count = nullptr;
+  unsigned long long* snap_ds_count = nullptr;
+  uint8_t* snap_mask = nullptr;
   /* snapshot for retries */
   double* snap_body[6] = {nullptr};
   uint64_t* snap_key = nullptr;
@@ -187,6 +210,65 @@ struct shapes_batch {
   int32_t snap_cap = 0;
 
   shapes_stats stats{};
+
+  /* CUDA graphs: one captured step per write buffer, replayed while the
+   * configuration and every buffer the step touches stay the same.  Anything
+   * that reallocates a buffer, regroups the solver or changes which kernels a
+   * step launches bumps graph_epoch. */
+  bool graphs_enabled = true;
+  uint64_t graph_epoch = 1;
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t epoch = 0;
+    shapes_config cfg{};
+  };
+  StepGraph graph[2];
+  int64_t graph_captures = 0;
+
+  void invalidate_graphs() { ++graph_epoch; }
+
+  void drop_graphs() {
+    for (auto& g : graph) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+    }
+  }
+
+  /* One solver step writing buffer wb: replayed from its graph, captured on
+   * first use (or after an invalidation).  Profiling records events between
+   * stages, so profiled steps are launched directly. */
+  void launch_step(const shapes_config& cfg, int wb) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (graphs_enabled && !profiling && stream != cudaStreamLegacy && stream != cudaStreamPerThread)
+      ck(cudaStreamIsCapturing(stream, &cap), "cudaStreamIsCapturing");
+    if (!graphs_enabled || profiling || stream == cudaStreamLegacy || stream == cudaStreamPerThread ||
+        cap != cudaStreamCaptureStatusNone) { /* a caller's own capture takes the kernels as they are */
+      enqueue_step(cfg, true, wb);
+      return;
+    }
+    StepGraph& g = graph[wb];
+    if (!g.exec || g.epoch != graph_epoch || std::memcmp(&g.cfg, &cfg, sizeof cfg) != 0) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      cudaGraph_t gr = nullptr;
+      ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+      try {
+        enqueue_step(cfg, true, wb);
+      } catch (...) {
+        cudaStreamEndCapture(stream, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        throw;
+      }
+      ck(cudaStreamEndCapture(stream, &gr), "cudaStreamEndCapture");
+      const cudaError_t e = cudaGraphInstantiate(&g.exec, gr, 0);
+      cudaGraphDestroy(gr);
+      ck(e, "cudaGraphInstantiate");
+      g.epoch = graph_epoch;
+      g.cfg = cfg;
+      ++graph_captures;
+    }
+    ck(cudaGraphLaunch(g.exec, stream), "cudaGraphLaunch");
+  }
 
   /* caller stream + per-stage profiling */
   cudaStream_t own_stream = nullptr;
@@ -316,6 +398,33 @@ struct shapes_batch {
     return d;
   }
 
+  void free_row_buffers() {
+    dfree(miss_flag); dfree(miss_off); dfree(miss_ids); dfree(miss_n); dfree(mfeat);
+    miss_flag = miss_off = miss_ids = miss_n = nullptr;
+    mfeat = nullptr;
+    miss_cap = 0;
+  }
+
+  /* Feature-row buffers for the learned start / sample collection, sized by
+   * the contact capacity (allocated on first use). */
+  void ensure_row_buffers() {
+    if (miss_cap == contact_cap && miss_flag) return;
+    if (stream) ck(cudaStreamSynchronize(stream), "sync");
+    invalidate_graphs();
+    free_row_buffers();
+    miss_flag = dalloc<int32_t>(contact_cap, "cudaMalloc rows");
+    miss_off = dalloc<int32_t>((size_t)contact_cap + 1, "cudaMalloc rows");
+    miss_ids = dalloc<int32_t>(contact_cap, "cudaMalloc rows");
+    miss_n = dalloc<int32_t>(1, "cudaMalloc rows");
+    mfeat = dalloc<float>((size_t)contact_cap * mlp::kIn, "cudaMalloc rows");
+    miss_cap = contact_cap;
+  }
+
+  bool learned_on(const shapes_config& cfg) const {
+    return (cfg.flags & SHAPES_FLAG_LEARNED) && mlp_model && cfg.warm_start && ds_cap == 0;
+  }
+  bool collect_on(const shapes_config& cfg) const { return ds_cap > 0 && cfg.warm_start; }
+
   void free_step_buffers() {
     dfree(pair_a); dfree(pair_b); dfree(slot_cnt); dfree(slot_off); dfree(slot_feat); dfree(slot_val);
     for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
@@ -324,6 +433,7 @@ struct shapes_batch {
     idesc = nullptr;
     dfree(tile_sums);
     dfree(snap_key); dfree(snap_lam);
+    free_row_buffers();
     dfree(lw_refs); dfree(lw_rank); dfree(lw_hrank); dfree(lw_hitflag); dfree(lw_hitoff); dfree(lw_hit_idx);
     dfree(lw_color); dfree(lw_color_list);
     lw_refs = lw_rank = lw_hrank = lw_hitflag = lw_hitoff = lw_hit_idx = lw_color = lw_color_list = nullptr;
@@ -348,6 +458,7 @@ struct shapes_batch {
    * contents in c_key/lam[cache_buf] are preserved across a regrowth. */
   void alloc_step_buffers(int32_t new_pair_cap, int32_t new_contact_cap, int iterations) {
     if (stream) ck(cudaStreamSynchronize(stream), "sync");
+    invalidate_graphs();
     const int32_t old_cap = contact_cap;
     uint64_t* keep_key = nullptr;
     double* keep_lam = nullptr;
@@ -415,6 +526,7 @@ struct shapes_batch {
   void ensure_items(int iterations) {
     if ((int64_t)(iterations + 1) * contact_cap <= item_cap) return;
     ck(cudaStreamSynchronize(stream), "sync");
+    invalidate_graphs();
     dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist); dfree(gdesc); dfree(ghist); dfree(idesc);
     item_cap = (int64_t)(iterations + 1) * contact_cap;
     items = dalloc<uint32_t>(item_cap, "cudaMalloc items");
@@ -433,6 +545,7 @@ struct shapes_batch {
    * count with "worlds until this many bodies". */
   void make_groups(int iterations) {
     if (stream) ck(cudaStreamSynchronize(stream), "sync"); /* no kernel may still read the old groups */
+    invalidate_graphs();
     std::vector<int32_t> order;
     for (int w = 0; w < W; ++w)
       if (h_world_body_off[w + 1] - h_world_body_off[w] < large_world_bodies) order.push_back(w);
@@ -538,7 +651,7 @@ struct shapes_batch {
       shapes::k_lw_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
       shapes::k_lw_rank<<<grid_for(w.nb, 128), 128, 0, stream>>>(d, w);
       scan_raw(w.hitflag, cap, w.ctl + 4, w.hitoff);
-      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w, counters + shapes::kCntHits);
     });
     stage(4, 1, [&]() {
       if (cfg.external)
@@ -619,6 +732,18 @@ struct shapes_batch {
    * build, warm start, sweeps, integration. */
   void enqueue_step(const shapes_config& cfg, bool solve, int wb) {
     Dev d = view(wb);
+    const bool learn = solve && learned_on(cfg), collect = solve && collect_on(cfg);
+    if (learn || collect) { /* row buffers were sized by run() before this view */
+      d.learned_mask = learned_mask;
+      d.miss_flag = miss_flag;
+      d.miss_off = miss_off;
+      d.miss_ids = miss_ids;
+      d.miss_n = miss_n;
+      d.mfeat = mfeat;
+      d.collect_all = collect ? 1 : 0;
+      d.judge_res = judge_res;
+      d.judge_depth = judge_depth;
+    }
     /* pairs/contacts and the group allocator are per step; hits, items and
      * levels add up over the call */
     ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2, stream), "memset");
@@ -653,6 +778,21 @@ struct shapes_batch {
                                                                            cfg.warm_start, solve ? 1 : 0);
     });
     if (!solve) return;
+    if (learn || collect) {
+      stage(7, 4 + (learn ? 2 : 0), [&]() {
+        scan_raw(miss_flag, contact_cap, counters + shapes::kCntContacts, miss_off);
+        shapes::k_learned_features<<<grid_for(contact_cap, 128), 128, 0, stream>>>(d, cfg.external, cfg.accel_x,
+                                                                                  cfg.accel_y, cfg.dt);
+        if (learn) {
+          ck(mlp::launch_predict_contacts(mlp::device_params(mlp_model), mlp::device_norm(mlp_model), mfeat, miss_n,
+                                          miss_ids, d.lam, c_hit, shapes::kInfoHit,
+                                          counters + shapes::kCntPredicted,
+                                          reinterpret_cast<int*>(counters + shapes::kCntMlpErr), contact_cap, stream),
+             "k_mlp_predict");
+          shapes::k_world_depth<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d);
+        }
+      });
+    }
     const int G = num_groups(); /* groups for cfg.iterations were built by run() before this view */
     const int wpc = solve_threads / 32;
     /* each warp's slice of last levels: 40 KB of dynamic shared memory in all (static use is ~1 KB) */
@@ -664,8 +804,15 @@ struct shapes_batch {
                                              cfg.accel_y, cfg.dt, G, per_warp);
       });
     for (size_t k = 0; k < large_worlds.size(); ++k) solve_large_world(d, k, cfg);
-    if (cfg.flags & SHAPES_FLAG_RESIDUAL)
+    if ((cfg.flags & SHAPES_FLAG_RESIDUAL) || learn)
       stage(4, 1, [&]() { shapes::k_residual<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d); });
+    if (learn && judge_set)
+      stage(7, 1, [&]() { shapes::k_learned_judge<<<grid_for(W, 128), 128, 0, stream>>>(d); });
+    if (collect)
+      stage(7, 2, [&]() {
+        shapes::k_collect<<<grid_for(contact_cap, 256), 256, 0, stream>>>(d, ds_feat, ds_tgt, ds_count, ds_cap);
+        shapes::k_collect_advance<<<1, 1, 0, stream>>>(miss_n, ds_count, ds_cap);
+      });
     stage(5, 1, [&]() { shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, cfg.dt, 1); });
   }
 
@@ -675,6 +822,11 @@ struct shapes_batch {
     ck(cudaMemcpyAsync(snap_key, c_key[cache_buf], sizeof(uint64_t) * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
     ck(cudaMemcpyAsync(snap_lam, lam[cache_buf], sizeof(double) * 2 * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
     ck(cudaMemcpyAsync(snap_cwo, cwo[cache_buf], sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "snapshot");
+    if (learned_mask)
+      ck(cudaMemcpyAsync(snap_mask, learned_mask, W, cudaMemcpyDeviceToDevice, stream), "snapshot");
+    if (ds_count)
+      ck(cudaMemcpyAsync(snap_ds_count, ds_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream),
+         "snapshot");
   }
 
   /* Restore into buffer `buf` (which becomes the cache buffer). */
@@ -684,6 +836,11 @@ struct shapes_batch {
     ck(cudaMemcpyAsync(c_key[cache_buf], snap_key, sizeof(uint64_t) * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
     ck(cudaMemcpyAsync(lam[cache_buf], snap_lam, sizeof(double) * 2 * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
     ck(cudaMemcpyAsync(cwo[cache_buf], snap_cwo, sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "restore");
+    if (learned_mask)
+      ck(cudaMemcpyAsync(learned_mask, snap_mask, W, cudaMemcpyDeviceToDevice, stream), "restore");
+    if (ds_count)
+      ck(cudaMemcpyAsync(ds_count, snap_ds_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream),
+         "restore");
   }
 
   /* Runs `nsteps` steps (or one collide when !solve) with overflow retries. */
@@ -692,17 +849,21 @@ struct shapes_batch {
     /* (re)build the solver groups before any device view of this call is
      * taken: make_groups reallocates the group arrays */
     if (solve && grouped_iterations != cfg.iterations) make_groups(cfg.iterations);
+    if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
     int retries = 0;
     for (;;) {
-      ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 8, stream), "memset");
+      ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntSlots, stream), "memset");
       const int saved_cache_buf = cache_buf;
       const int saved_cap = contact_cap;
       if (solve) snapshot();
-      unsigned long long agg[8] = {0};
-      unsigned long long h[8];
+      unsigned long long agg[shapes::kCntSlots] = {0};
+      unsigned long long h[shapes::kCntSlots];
       for (int s = 0; s < (solve ? nsteps : 1); ++s) {
         const int wb = 1 - cache_buf;
-        enqueue_step(cfg, solve, wb);
+        if (solve)
+          launch_step(cfg, wb);
+        else
+          enqueue_step(cfg, false, wb);
         if (solve) cache_buf = wb;
         results_buf = wb;
         if (solve && nsteps > 1) {
@@ -713,7 +874,11 @@ struct shapes_batch {
       ck(cudaStreamSynchronize(stream), "step");
       ck(cudaGetLastError(), "launch");
       if (profiling) collect_profile();
-      for (int k = 0; k < 8; ++k) agg[k] = h[k];
+      for (int k = 0; k < shapes::kCntSlots; ++k) agg[k] = h[k];
+      if (agg[shapes::kCntMlpErr]) {
+        g_last_error = "learned warm start: a bounded tensor-core wait gave up";
+        return SHAPES_E_TIMEOUT;
+      }
       if (!agg[shapes::kCntOverflow] && solve && !large_worlds.empty()) {
         std::vector<unsigned long long> ctl(8 * large_worlds.size());
         ck(cudaMemcpy(ctl.data(), lw_ctl, sizeof(unsigned long long) * ctl.size(), cudaMemcpyDeviceToHost), "ctl");
@@ -726,7 +891,9 @@ struct shapes_batch {
       if (!agg[shapes::kCntOverflow]) {
         stats.pairs = (int64_t)agg[shapes::kCntPairs];
         stats.contacts = (int64_t)agg[shapes::kCntContacts];
-        stats.cache_hits = (int64_t)agg[shapes::kCntHits];
+        stats.cache_hits = (int64_t)agg[shapes::kCntHits] - (int64_t)agg[shapes::kCntPredicted];
+        stats.predicted = (int64_t)agg[shapes::kCntPredicted];
+        stats.reverted = (int64_t)agg[shapes::kCntReverted];
         stats.solver_items = (int64_t)agg[shapes::kCntItems];
         stats.solver_levels = (int64_t)agg[shapes::kCntLevels];
         stats.retries = retries;
@@ -743,11 +910,14 @@ struct shapes_batch {
       if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
       alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
       ensure_items(solve ? cfg.iterations : 0);
+      if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
       if (solve) pose(0, 0.0);
     }
   }
 
   ~shapes_batch() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graphs();
     free_step_buffers();
     dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly);
     dfree(emin); dfree(emax);
@@ -766,6 +936,8 @@ struct shapes_batch {
     dfree(lw_bcnt); dfree(lw_bstart); dfree(lw_bh); dfree(lw_bn); dfree(lw_done); dfree(lw_color_cnt); dfree(lw_ctl);
     dfree(world_residual);
     dfree(world_depth);
+    dfree(learned_mask); dfree(judge_res); dfree(judge_depth);
+    dfree(ds_feat); dfree(ds_tgt); dfree(ds_count); dfree(snap_ds_count); dfree(snap_mask);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(snap_cwo);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
@@ -896,7 +1068,7 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       for (int k = 0; k < 2; ++k) h->cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
       h->last = dalloc<int32_t>(N, "cudaMalloc");
       h->world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
-      h->counters = dalloc<unsigned long long>(8, "cudaMalloc");
+      h->counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
       h->world_residual = dalloc<double>(n_worlds, "cudaMalloc");
       h->world_depth = dalloc<double>(n_worlds, "cudaMalloc");
       for (int k = 0; k < 6; ++k) h->snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
@@ -950,7 +1122,7 @@ static int check_cfg(const shapes_config* c) {
     return SHAPES_E_UNSUPPORTED;
   if (c->external != SHAPES_EXTERNAL_NONE && c->external != SHAPES_EXTERNAL_CONSTANT_ACCEL)
     return SHAPES_E_UNSUPPORTED;
-  if (c->flags & ~(SHAPES_FLAG_RESIDUAL | SHAPES_FLAG_COLOURED)) return SHAPES_E_INVALID_ARG;
+  if (c->flags & ~(SHAPES_FLAG_RESIDUAL | SHAPES_FLAG_COLOURED | SHAPES_FLAG_LEARNED)) return SHAPES_E_INVALID_ARG;
   return SHAPES_OK;
 }
 
@@ -962,7 +1134,7 @@ int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps)
   return guarded([&]() -> int {
     ck(cudaSetDevice(b->device), "cudaSetDevice");
     const int rc = b->run(*cfg, nsteps, true);
-    b->residual_valid = rc == SHAPES_OK && (cfg->flags & SHAPES_FLAG_RESIDUAL);
+    b->residual_valid = rc == SHAPES_OK && ((cfg->flags & SHAPES_FLAG_RESIDUAL) || b->learned_on(*cfg));
     return rc;
   });
 }
@@ -1208,7 +1380,9 @@ int shapes_batch_get_world_metrics(shapes_batch* b, double* residual, double* ma
     if (max_depth) {
       shapes_config cfg{};
       cfg.dt = 1.0;
+      const shapes_stats keep = b->stats; /* the counters stay those of the last step call */
       const int rc = b->run(cfg, 1, false);
+      b->stats = keep;
       if (rc != SHAPES_OK) return rc;
       Dev d = b->view(b->results_buf);
       shapes::k_world_depth<<<(b->W * 32 + 127) / 128, 128, 0, b->stream>>>(d);
@@ -1315,6 +1489,124 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     if (chosen_worlds_per_group) *chosen_worlds_per_group = b->worlds_per_group_override;
     if (chosen_threads) *chosen_threads = b->solve_threads;
     return rc;
+  });
+}
+
+int shapes_batch_set_graphs(shapes_batch* b, int32_t enabled) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->graphs_enabled = enabled != 0;
+    b->drop_graphs();
+    b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_mlp(shapes_batch* b, const shapes_mlp* m) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    if (m && !b->learned_mask) {
+      b->learned_mask = dalloc<uint8_t>(b->W, "cudaMalloc");
+      b->snap_mask = dalloc<uint8_t>(b->W, "cudaMalloc");
+    }
+    if (m) ck(cudaMemsetAsync(b->learned_mask, 1, b->W, b->stream), "memset");
+    if (m) ck(mlp::prepare_device(), "network set-up");
+    b->mlp_model = m;
+    b->invalidate_graphs();
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_learned_mask(shapes_batch* b, uint8_t* mask) {
+  if (!b || !mask) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    if (!b->learned_mask) {
+      std::fill(mask, mask + b->W, (uint8_t)0);
+      return SHAPES_OK;
+    }
+    ck(cudaMemcpyAsync(mask, b->learned_mask, b->W, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_learned_mask(shapes_batch* b, const uint8_t* mask) {
+  if (!b || !mask || !b->learned_mask) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    std::vector<uint8_t> m(b->W);
+    for (int32_t w = 0; w < b->W; ++w) m[w] = mask[w] ? 1 : 0;
+    ck(cudaMemcpyAsync(b->learned_mask, m.data(), b->W, cudaMemcpyHostToDevice, b->stream), "upload");
+    ck(cudaStreamSynchronize(b->stream), "upload");
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_judge(shapes_batch* b, const double* max_residual, const double* max_depth) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  for (int32_t w = 0; w < b->W; ++w)
+    if ((max_residual && std::isnan(max_residual[w])) || (max_depth && std::isnan(max_depth[w])))
+      return SHAPES_E_NAN;
+  return guarded([&]() -> int {
+    if (!b->judge_res) {
+      b->judge_res = dalloc<double>(b->W, "cudaMalloc");
+      b->judge_depth = dalloc<double>(b->W, "cudaMalloc");
+    }
+    const double inf = std::numeric_limits<double>::infinity();
+    std::vector<double> r(b->W, inf), dd(b->W, inf);
+    if (max_residual) std::copy(max_residual, max_residual + b->W, r.begin());
+    if (max_depth) std::copy(max_depth, max_depth + b->W, dd.begin());
+    ck(cudaMemcpyAsync(b->judge_res, r.data(), sizeof(double) * b->W, cudaMemcpyHostToDevice, b->stream), "upload");
+    ck(cudaMemcpyAsync(b->judge_depth, dd.data(), sizeof(double) * b->W, cudaMemcpyHostToDevice, b->stream),
+       "upload");
+    ck(cudaStreamSynchronize(b->stream), "upload");
+    b->judge_set = max_residual || max_depth;
+    b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_collect(shapes_batch* b, int64_t capacity) {
+  if (!b || capacity < 0 || capacity > INT32_MAX) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->invalidate_graphs();
+    dfree(b->ds_feat); dfree(b->ds_tgt); dfree(b->ds_count); dfree(b->snap_ds_count);
+    b->ds_feat = b->ds_tgt = nullptr;
+    b->ds_count = b->snap_ds_count = nullptr;
+    b->ds_cap = 0;
+    if (capacity == 0) return SHAPES_OK;
+    b->ds_feat = dalloc<float>((size_t)capacity * mlp::kIn, "cudaMalloc samples");
+    b->ds_tgt = dalloc<float>((size_t)capacity * mlp::kOut, "cudaMalloc samples");
+    b->ds_count = dalloc<unsigned long long>(1, "cudaMalloc samples");
+    b->snap_ds_count = dalloc<unsigned long long>(1, "cudaMalloc samples");
+    ck(cudaMemsetAsync(b->ds_count, 0, sizeof(unsigned long long), b->stream), "memset");
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->ds_cap = capacity;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_samples(shapes_batch* b, float* features, float* targets, int64_t capacity, int64_t* n) {
+  if (!b || !n || capacity < 0 || (capacity > 0 && (!features || !targets))) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    unsigned long long cnt = 0;
+    if (b->ds_count) {
+      ck(cudaMemcpyAsync(&cnt, b->ds_count, sizeof(cnt), cudaMemcpyDeviceToHost, b->stream), "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    *n = (int64_t)cnt;
+    const int64_t k = std::min<int64_t>((int64_t)cnt, capacity);
+    if (k > 0) {
+      ck(cudaMemcpyAsync(features, b->ds_feat, sizeof(float) * mlp::kIn * k, cudaMemcpyDeviceToHost, b->stream),
+         "download");
+      ck(cudaMemcpyAsync(targets, b->ds_tgt, sizeof(float) * mlp::kOut * k, cudaMemcpyDeviceToHost, b->stream),
+         "download");
+      ck(cudaStreamSynchronize(b->stream), "download");
+    }
+    return (int64_t)cnt > capacity ? SHAPES_E_BUFFER : SHAPES_OK;
   });
 }
 

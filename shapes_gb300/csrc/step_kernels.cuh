@@ -121,9 +121,19 @@ struct Dev {
   int32_t* group_depth;       /* [G] */
   const int32_t* group_world_off; /* [G+1] offsets into group_worlds */
   const int32_t* group_worlds;    /* [W] world ids, grouped */
-  unsigned long long* counters;   /* [8] see kCnt* */
+  unsigned long long* counters;   /* [kCntSlots] see kCnt* */
   double* world_residual;         /* [W] */
   double* world_depth;            /* [W] */
+  /* learned warm start (null / zero when off) */
+  uint8_t* learned_mask;       /* [W] 1 = contacts without a cache entry start from the network */
+  int32_t* miss_flag;          /* [contact_cap] 1 = contact gets a feature row */
+  int32_t* miss_off;           /* [contact_cap + 1] scanned miss_flag */
+  int32_t* miss_ids;           /* [contact_cap] contact of each row */
+  int32_t* miss_n;             /* [1] rows this step */
+  float* mfeat;                /* [contact_cap x 16] raw features */
+  int32_t collect_all;         /* 1 = rows for every world's misses (sample collection) */
+  const double* judge_res;     /* [W] residual limit of the judge */
+  const double* judge_depth;   /* [W] depth limit of the judge */
 };
 
 enum {
@@ -135,6 +145,10 @@ enum {
   kCntOverflow = 5,
   kCntBadInput = 6,
   kCntGroupAlloc = 7, /* bump allocator of the per-group regions (reset every step) */
+  kCntPredicted = 8,  /* contacts started from the network (summed over the call) */
+  kCntReverted = 9,   /* worlds the judge switched back to the plain start */
+  kCntMlpErr = 10,    /* set when a tensor-core wait of the network gave up */
+  kCntSlots = 16,
 };
 
 /* Flags any non-finite value among n bodies' ten state arrays. */
@@ -841,6 +855,8 @@ __global__ void k_build(Dev d, double dt, double beta, double slop, int warm_sta
         if (k > key) lo = mid + 1; else hi = mid - 1;
       }
     }
+    if (d.miss_flag)
+      d.miss_flag[c] = (warm_start && !hit && (d.collect_all || d.learned_mask[wld])) ? 1 : 0;
     uint8_t info = hit ? kInfoHit : 0;
     if (!(d.flags[ga] & kFlagStatic)) info |= kInfoDynA;
     if (!(d.flags[gb] & kFlagStatic)) info |= kInfoDynB;

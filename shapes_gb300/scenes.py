@@ -237,34 +237,66 @@ def batched_columns(seed: int = 2, n_worlds: int = 4096, nmin: int = 8, nmax: in
                     slop=DEFAULT_SLOP, accel=(0.0, -9.8), iterations=8, steps=steps)
 
 
-def mixed_pile_world(b: SceneBuilder, rng, n_bodies: int, cols: int = 16, size=(0.4, 1.5), mu=(0.2, 0.8),
-                     slab_w: float = 60.0):
-    """Static slab, then n_bodies-1 boxes and 3-8 vertex polygons of size
-    U[size] and friction U[mu], dropped from a jittered grid."""
-    b.add(rectangle_vertices(slab_w, 1.0), (0.0, -0.5), static=True)
+def batched_mixed(seed: int = 3, n_worlds: int = 1024, n_bodies: int = 256, steps: int = 300, cols: int = 16,
+                  size=(0.4, 1.5), mu=(0.2, 0.8), slab_w: float = 60.0) -> dict:
+    """n_worlds worlds of n_bodies: a static slab_w x 1 slab (friction 0.2),
+    then boxes (side s, aspect U[0.6, 1]) and perturbed 3-8 vertex polygons
+    (radius 0.6 s, vertex radii +-10%), half and half, s ~ U[size], friction
+    U[mu], density 1, dropped from a jittered grid `cols` wide with random
+    rotations; dt = 1/60, 8 sweeps."""
+    rng = np.random.default_rng(seed)
+    nb = n_bodies - 1
+    total = n_worlds * nb
+    s = rng.uniform(size[0], size[1], size=total)
+    is_box = rng.uniform(size=total) < 0.5
+    aspect = rng.uniform(0.6, 1.0, size=total)
+    nv = np.where(is_box, 4, rng.integers(3, 9, size=total))
+    start = np.zeros(total + 1, dtype=np.int64)
+    start[1:] = np.cumsum(nv)
+    owner = np.repeat(np.arange(total), nv)
+    k = np.arange(start[-1]) - start[owner]
+    rad = (0.6 * s)[owner] * rng.uniform(0.9, 1.1, size=start[-1])
+    ang = 2.0 * np.pi * k / nv[owner]
+    w2, h2 = (s / 2.0)[owner], (s * aspect / 2.0)[owner]
+    box = is_box[owner]
+    x = np.where(box, np.where((k == 0) | (k == 3), w2, -w2), rad * np.cos(ang))
+    y = np.where(box, np.where(k < 2, h2, -h2), rad * np.sin(ang))
+    nxt = np.arange(start[-1]) + 1
+    nxt[start[1:] - 1] = start[:-1]
+    x1, y1 = x[nxt], y[nxt]
+    cr = x * y1 - x1 * y
+    area = 0.5 * np.bincount(owner, cr, minlength=total)
+    inertia = np.bincount(owner, cr * (x * x + x * x1 + x1 * x1 + y * y + y * y1 + y1 * y1), minlength=total) / 12.0
+    j = np.tile(np.arange(nb), n_worlds)
     pitch = 2.0 * size[1] + 0.1
     left = -pitch * (cols - 1) / 2.0
-    for k in range(n_bodies - 1):
-        c, r = k % cols, k // cols
-        s = rng.uniform(*size)
-        if rng.uniform() < 0.5:
-            xy = rectangle_vertices(s, s * rng.uniform(0.6, 1.0))
-        else:
-            xy = perturbed_polygon(rng, int(rng.integers(3, 9)), s / 2.0 * 1.2)
-        pos = (left + c * pitch + rng.uniform(-0.1, 0.1), pitch * (r + 0.5) + rng.uniform(-0.1, 0.1))
-        b.add(xy, pos, rng.uniform(0.0, 2.0 * np.pi), mu=rng.uniform(*mu))
-    b.end_world()
-
-
-def batched_mixed(seed: int = 3, n_worlds: int = 1024, n_bodies: int = 256, steps: int = 300) -> dict:
-    """n_worlds worlds of n_bodies mixed boxes and polygons (sizes U[0.4,1.5],
-    friction U[0.2,0.8])."""
-    rng = np.random.default_rng(seed)
-    b = SceneBuilder()
-    for _ in range(n_worlds):
-        mixed_pile_world(b, rng, n_bodies)
-    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP, accel=(0.0, -9.8),
-                   iterations=8, steps=steps)
+    px = left + (j % cols) * pitch + rng.uniform(-0.1, 0.1, size=total)
+    py = pitch * (j // cols + 0.5) + rng.uniform(-0.1, 0.1, size=total)
+    rot = rng.uniform(0.0, 2.0 * np.pi, size=total)
+    mus = rng.uniform(mu[0], mu[1], size=total)
+    n = n_worlds * n_bodies
+    slab_pos = np.arange(n_worlds) * n_bodies
+    body_pos = np.flatnonzero(np.arange(n) % n_bodies != 0)
+    f = {kk: np.zeros(n) for kk in BODY_FIELDS}
+    f["pos_x"][body_pos], f["pos_y"][body_pos], f["rot"][body_pos] = px, py, rot
+    f["inv_mass_lin"][body_pos] = 1.0 / area
+    f["inv_mass_rot"][body_pos] = 1.0 / inertia
+    f["mu"][body_pos] = mus
+    f["pos_y"][slab_pos] = -0.5
+    f["mu"][slab_pos] = DEFAULT_MU
+    f["bounce"][:] = DEFAULT_BOUNCE
+    fnv = np.full(n, 4, dtype=np.int64)
+    fnv[body_pos] = nv
+    fvo = np.zeros(n + 1, dtype=np.int64)
+    fvo[1:] = np.cumsum(fnv)
+    verts = np.zeros((int(fvo[-1]), 2))
+    dst = fvo[body_pos][owner] + k
+    verts[dst, 0], verts[dst, 1] = x, y
+    slab = rectangle_vertices(slab_w, 1.0)
+    for q in range(4):
+        verts[fvo[slab_pos] + q] = slab[q]
+    return assemble(np.full(n_worlds, n_bodies), f, verts, fnv, dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE,
+                    slop=DEFAULT_SLOP, accel=(0.0, -9.8), iterations=8, steps=steps)
 
 
 def container_world(seed: int = 4, n: int = 262144, width: float = 1024.0, rmin=0.3, rmax=1.0,
