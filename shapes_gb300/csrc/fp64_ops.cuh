@@ -33,6 +33,24 @@ __device__ __forceinline__ bool f_lt(double a, double b) {
   return !nan_bits(a) && !nan_bits(b) && okey(a) < okey(b);
 }
 
+/* Finite (not infinite, not NaN). */
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((uint64_t)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+
+/* 0.0 * x for finite x: a zero with x's sign. */
+__device__ __forceinline__ double signed_zero(double x) {
+  return __longlong_as_double(__double_as_longlong(x) & (long long)0x8000000000000000ull);
+}
+
+/* x + z for finite x and a signed zero z: x unless x is a zero, and the sum
+ * of two zeros is -0 only when both are -0 (round to nearest). */
+__device__ __forceinline__ double add_zero(double x, double z) {
+  const uint64_t ux = (uint64_t)__double_as_longlong(x);
+  if (ux & 0x7fffffffffffffffull) return x;
+  return __longlong_as_double((long long)(ux & (uint64_t)__double_as_longlong(z)));
+}
+
 /* x + 0.0: only -0 changes (to +0); NaN stays NaN. */
 __device__ __forceinline__ double plus_zero(double x) {
   return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;

@@ -121,6 +121,8 @@ struct shapes_batch {
   int32_t* slot_off = nullptr;
   int32_t* slot_feat = nullptr;
   double* slot_val = nullptr;
+  int32_t* np_perm = nullptr;
+  int32_t* np_cls = nullptr; /* [2 * kNpClasses + 1] */
   int32_t* world_pair_off = nullptr;
   /* contacts: ping-pong between two buffers, the cache of step s is the
    * contact keys + Lagrangians of step s */
@@ -365,6 +367,8 @@ struct shapes_batch {
     d.slot_cnt = slot_cnt;
     d.slot_off = slot_off;
     d.slot_feat = slot_feat;
+    d.np_perm = np_perm;
+    d.np_cls = np_cls;
     d.slot_val = slot_val;
     d.c_key = c_key[write_buf];
     d.c_ga = c_ga;
@@ -427,6 +431,8 @@ struct shapes_batch {
 
   void free_step_buffers() {
     dfree(pair_a); dfree(pair_b); dfree(slot_cnt); dfree(slot_off); dfree(slot_feat); dfree(slot_val);
+    dfree(np_perm);
+    np_perm = nullptr;
     for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
     dfree(c_ga); dfree(c_gb); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
     dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist); dfree(gdesc); dfree(ghist); dfree(idesc);
@@ -479,6 +485,7 @@ struct shapes_batch {
     slot_off = dalloc<int32_t>((size_t)pair_cap + 1, "cudaMalloc slots");
     slot_feat = dalloc<int32_t>(2 * (size_t)pair_cap, "cudaMalloc slots");
     slot_val = dalloc<double>(10 * (size_t)pair_cap, "cudaMalloc slots");
+    np_perm = dalloc<int32_t>(pair_cap, "cudaMalloc slots");
     for (int k = 0; k < 2; ++k) {
       c_key[k] = dalloc<uint64_t>(contact_cap, "cudaMalloc contacts");
       lam[k] = dalloc<double>(2 * (size_t)contact_cap, "cudaMalloc contacts");
@@ -770,7 +777,13 @@ struct shapes_batch {
       }
     });
     stage(6, 1, [&]() { shapes::k_world_pair_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
-    stage(1, 1, [&]() { shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d); });
+    stage(1, 4, [&]() {
+      ck(cudaMemsetAsync(np_cls, 0, sizeof(int32_t) * shapes::kNpClasses, stream), "memset");
+      shapes::k_np_count<<<grid_for(pair_cap, 256), 256, 0, stream>>>(d);
+      shapes::k_np_offsets<<<1, 32, 0, stream>>>(d);
+      shapes::k_np_scatter<<<grid_for(pair_cap, 256), 256, 0, stream>>>(d);
+      shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d);
+    });
     scan(slot_cnt, pair_cap, counters + shapes::kCntPairs, slot_off);
     stage(6, 1, [&]() { shapes::k_world_contact_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
     stage(2, 1, [&]() {
@@ -933,6 +946,7 @@ struct shapes_batch {
     dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
     dfree(phase_clock);
     dfree(counters);
+    dfree(np_cls);
     dfree(lw_bcnt); dfree(lw_bstart); dfree(lw_bh); dfree(lw_bn); dfree(lw_done); dfree(lw_color_cnt); dfree(lw_ctl);
     dfree(world_residual);
     dfree(world_depth);
@@ -1069,6 +1083,7 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       h->last = dalloc<int32_t>(N, "cudaMalloc");
       h->world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
       h->counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
+      h->np_cls = dalloc<int32_t>(2 * shapes::kNpClasses + 1, "cudaMalloc");
       h->world_residual = dalloc<double>(n_worlds, "cudaMalloc");
       h->world_depth = dalloc<double>(n_worlds, "cudaMalloc");
       for (int k = 0; k < 6; ++k) h->snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
@@ -1177,7 +1192,11 @@ int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in) {
     ck(cudaMemcpyAsync(&bad, b->counters + shapes::kCntBadInput, sizeof(bad), cudaMemcpyDeviceToHost, b->stream), "download");
     ck(cudaStreamSynchronize(b->stream), "validate");
     if (bad) return SHAPES_E_NAN; /* live state untouched */
-    for (int k = 0; k < 10; ++k) std::swap(b->body[k], b->body_stage[k]);
+    /* copied, not swapped: the live arrays keep their addresses, which the
+     * captured step graphs hold */
+    for (int k = 0; k < 10; ++k)
+      ck(cudaMemcpyAsync(b->body[k], b->body_stage[k], sizeof(double) * b->N, cudaMemcpyDeviceToDevice, b->stream),
+         "upload");
     b->pose(0, 0.0);
     ck(cudaGetLastError(), "launch");
     ck(cudaStreamSynchronize(b->stream), "upload");

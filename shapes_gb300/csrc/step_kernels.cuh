@@ -94,6 +94,8 @@ struct Dev {
   int32_t* slot_cnt;   /* [pair_cap] contacts per pair (0..2) */
   int32_t* slot_off;   /* [pair_cap+1] scanned */
   int32_t* slot_feat;  /* [2*pair_cap] fa | fb<<12 | flip<<24 */
+  int32_t* np_perm;    /* [pair_cap] pairs in processing order, grouped by vertex-count class */
+  int32_t* np_cls;     /* [2 * kNpClasses + 1] class counts, then offsets and cursors */
   double* slot_val;    /* [2*pair_cap*5] nx ny px py depth */
   uint64_t* c_key;     /* [contact_cap] packed world-local key */
   int32_t* c_ga;       /* [contact_cap] */
@@ -150,6 +152,9 @@ enum {
   kCntMlpErr = 10,    /* set when a tensor-core wait of the network gave up */
   kCntSlots = 16,
 };
+
+/* Narrowphase work classes: (min(nv_a, 9) - 3) * 7 + (min(nv_b, 9) - 3). */
+constexpr int kNpClasses = 49;
 
 /* Flags any non-finite value among n bodies' ten state arrays. */
 __global__ void k_check_finite(const double* a0, const double* a1, const double* a2, const double* a3,
@@ -231,20 +236,37 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
     double s, c;
     shapes_sincos(th, &s, &c);
     const double ms = -s;
-    /* rows of translate(px,py) times columns of rotate(c,s) */
-    const double m00 = (1.0 * c + 0.0 * s) + px * 0.0;
-    const double m01 = (1.0 * ms + 0.0 * c) + px * 0.0;
-    const double m02 = (1.0 * 0.0 + 0.0 * 0.0) + px * 1.0;
-    const double m10 = (0.0 * c + 1.0 * s) + py * 0.0;
-    const double m11 = (0.0 * ms + 1.0 * c) + py * 0.0;
-    const double m12 = (0.0 * 0.0 + 1.0 * 0.0) + py * 1.0;
+    /* rows of translate(px,py) times columns of rotate(c,s), summed in the
+     * reference's order (joinTransforms, Transform.hs:73-77) */
+    double m00, m01, m02, m10, m11, m12;
+    if (finite_bits(c) && finite_bits(s) && finite_bits(px) && finite_bits(py)) {
+      /* every product by 1.0 or 0.0 is exact, so the sums reduce to
+       * signed-zero rules on the integer pipe */
+      const double zc = signed_zero(c), zs = signed_zero(s), zms = signed_zero(ms);
+      const double zpx = signed_zero(px), zpy = signed_zero(py);
+      m00 = add_zero(add_zero(c, zs), zpx);
+      m01 = add_zero(add_zero(ms, zc), zpx);
+      m02 = plus_zero(px);
+      m10 = add_zero(add_zero(s, zc), zpy);
+      m11 = add_zero(add_zero(c, zms), zpy);
+      m12 = plus_zero(py);
+    } else {
+      m00 = (1.0 * c + 0.0 * s) + px * 0.0;
+      m01 = (1.0 * ms + 0.0 * c) + px * 0.0;
+      m02 = (1.0 * 0.0 + 0.0 * 0.0) + px * 1.0;
+      m10 = (0.0 * c + 1.0 * s) + py * 0.0;
+      m11 = (0.0 * ms + 1.0 * c) + py * 0.0;
+      m12 = (0.0 * 0.0 + 1.0 * 0.0) + py * 1.0;
+    }
+    /* m02 * 1.0 == m02 and m12 * 1.0 == m12 unless NaN (then both are NaN) */
+    const bool t_nan = nan_bits(m02) || nan_bits(m12);
     const int b0 = d.vert_off[g], nv = d.vert_off[g + 1] - b0;
     double x0 = 0, y0 = 0, xp = 0, yp = 0;
     double bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
     for (int k = 0; k < nv; ++k) {
       const double lx = d.lx[b0 + k], ly = d.ly[b0 + k];
-      const double x = (m00 * lx + m01 * ly) + m02 * 1.0;
-      const double y = (m10 * lx + m11 * ly) + m12 * 1.0;
+      const double x = t_nan ? (m00 * lx + m01 * ly) + m02 * 1.0 : (m00 * lx + m01 * ly) + m02;
+      const double y = t_nan ? (m10 * lx + m11 * ly) + m12 * 1.0 : (m10 * lx + m11 * ly) + m12;
       d.wx[b0 + k] = x;
       d.wy[b0 + k] = y;
       if (k == 0) {
@@ -256,10 +278,10 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
         const double len = sqrt(ex * ex + ey * ey);
         d.nx[b0 + k - 1] = ex / len;
         d.ny[b0 + k - 1] = ey / len;
-        bx0 = bx0 < x ? bx0 : x;
-        bx1 = bx1 > x ? bx1 : x;
-        by0 = by0 < y ? by0 : y;
-        by1 = by1 > y ? by1 : y;
+        bx0 = f_lt(bx0, x) ? bx0 : x;
+        bx1 = f_lt(x, bx1) ? bx1 : x;
+        by0 = f_lt(by0, y) ? by0 : y;
+        by1 = f_lt(y, by1) ? by1 : y;
       }
       xp = x;
       yp = y;
@@ -281,7 +303,7 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
     d.boxk[4 * g + 3] = okey(by1);
     uint8_t f = 0;
     if (d.iml[g] == 0.0 && d.imr[g] == 0.0) f |= kFlagStatic;
-    if (is_nan(bx0) || is_nan(bx1) || is_nan(by0) || is_nan(by1)) f |= kFlagBoxNaN;
+    if (nan_bits(bx0) || nan_bits(bx1) || nan_bits(by0) || nan_bits(by1)) f |= kFlagBoxNaN;
     d.flags[g] = f;
   }
 }
@@ -589,21 +611,29 @@ __device__ __forceinline__ HullView hull_view(const Dev& d, int g) {
 /* overlap (SAT.hs:103-118): extentAlongSelf with the precomputed extent
  * indices (ConvexHull.hs:111-118), extentAlong over the penetrator
  * (ConvexHull.hs:81-100), overlapTest/overlapAmount (SAT.hs:74-95). */
+/* The comparisons run on the integer pipe through order-preserving keys; a
+ * NaN projection compares false exactly as in IEEE arithmetic (a NaN first
+ * projection pins lo and hi, later NaNs never replace them). */
 __device__ __forceinline__ bool sat_axis(const HullView& se, int e, const HullView& sp,
                                          double* depth, int* pen) {
   const double dx = se.nx[e], dy = se.ny[e];
   const int mi = se.emin[e], ma = se.emax[e];
   const double sa = se.wx[mi] * dx + se.wy[mi] * dy;
   const double sb = se.wx[ma] * dx + se.wy[ma] * dy;
-  double lo = sp.wx[0] * dx + sp.wy[0] * dy, hi = lo;
+  const double t0 = sp.wx[0] * dx + sp.wy[0] * dy;
+  double lo = t0, hi = t0;
+  uint64_t klo = okey(t0), khi = klo;
+  const bool pinned = nan_bits(t0);
   int pmin = 0;
   for (int k = 1; k < sp.nv; ++k) {
     const double t = sp.wx[k] * dx + sp.wy[k] * dy;
-    if (t < lo) { lo = t; pmin = k; }
-    if (t > hi) { hi = t; }
+    if (pinned || nan_bits(t)) continue;
+    const uint64_t kt = okey(t);
+    if (kt < klo) { lo = t; klo = kt; pmin = k; }
+    if (kt > khi) { hi = t; khi = kt; }
   }
   *pen = pmin;
-  if (lo > sb || hi < sa) return false; /* Separated */
+  if (f_lt(sb, lo) || f_lt(hi, sa)) return false; /* Separated */
   *depth = sb - lo;
   return true;
 }
@@ -618,7 +648,7 @@ __device__ __forceinline__ bool min_overlap(const HullView& se, const HullView& 
     double dep;
     int p;
     if (!sat_axis(se, e, sp, &dep, &p)) return false;
-    if (e == 0 || dep < best) { best = dep; be = e; bp = p; }
+    if (e == 0 || f_lt(dep, best)) { best = dep; be = e; bp = p; }
   }
   *edge = be;
   *depth = best;
@@ -646,8 +676,8 @@ __device__ __forceinline__ int clip_segment(double bpx, double bpy, double bnx, 
   const double a_ = ax * bnx + ay * bny;
   const double b_ = bx * bnx + by * bny;
   const double c_ = x * bnx + y * bny;
-  if (a_ < c_) return b_ < c_ ? kClipBoth : kClipLeft;
-  if (b_ < c_) return kClipRight;
+  if (f_lt(a_, c_)) return f_lt(b_, c_) ? kClipBoth : kClipLeft;
+  if (f_lt(b_, c_)) return kClipRight;
   return kClipNone;
 }
 
@@ -663,7 +693,7 @@ __device__ __forceinline__ int manifold(const HullView& se, int e, const HullVie
   const double abn = fabs((sp.wx[vb] - sp.wx[va]) * nx + (sp.wy[vb] - sp.wy[va]) * ny);
   const double bcn = fabs((sp.wx[vc] - sp.wx[vb]) * nx + (sp.wy[vc] - sp.wy[vb]) * ny);
   int ci, di;
-  if (bcn < abn) { ci = vb; di = vc; } else { ci = va; di = vb; }
+  if (f_lt(bcn, abn)) { ci = vb; di = vc; } else { ci = va; di = vb; }
   double cx = sp.wx[ci], cy = sp.wy[ci], dx = sp.wx[di], dy = sp.wy[di];
   const double lpx = cx, lpy = cy;
   const double lnx = dy - cy, lny = -(dx - cx);
@@ -690,19 +720,81 @@ __device__ __forceinline__ int manifold(const HullView& se, int e, const HullVie
   return 2;
 }
 
+/* Pairs are processed grouped by the vertex counts of their two hulls, so
+ * that the lanes of a warp run SAT loops of the same trip counts (one thread
+ * per pair, the warp pays for its longest loop).  The grouping is a
+ * permutation of the processing order only: every pair still writes its own
+ * slots, so the results do not depend on it. */
+__device__ __forceinline__ int np_class(const Dev& d, int p) {
+  const int ga = d.pair_a[p], gb = d.pair_b[p];
+  const int na = min(d.vert_off[ga + 1] - d.vert_off[ga], 9), nb = min(d.vert_off[gb + 1] - d.vert_off[gb], 9);
+  return (na - 3) * 7 + (nb - 3);
+}
+
+__global__ void k_np_count(Dev d) {
+  __shared__ int32_t h[kNpClasses];
+  for (int k = threadIdx.x; k < kNpClasses; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
+    atomicAdd(&h[np_class(d, p)], 1);
+  __syncthreads();
+  for (int k = threadIdx.x; k < kNpClasses; k += blockDim.x)
+    if (h[k]) atomicAdd(&d.np_cls[k], h[k]);
+}
+
+/* counts -> offsets (np_cls[kNpClasses + k]) and cursors (np_cls[k]). */
+__global__ void k_np_offsets(Dev d) {
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int k = 0; k < kNpClasses; ++k) {
+      const int c = d.np_cls[k];
+      d.np_cls[kNpClasses + k] = run;
+      d.np_cls[k] = run;
+      run += c;
+    }
+    d.np_cls[2 * kNpClasses] = run;
+  }
+}
+
+__global__ void k_np_scatter(Dev d) {
+  __shared__ int32_t h[kNpClasses];
+  __shared__ int32_t base[kNpClasses];
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  const int stride = gridDim.x * blockDim.x;
+  for (int p0 = blockIdx.x * blockDim.x; p0 < P; p0 += stride) {
+    for (int k = threadIdx.x; k < kNpClasses; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const int p = p0 + threadIdx.x;
+    int cls = -1, rank = 0;
+    if (p < P) {
+      cls = np_class(d, p);
+      rank = atomicAdd(&h[cls], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kNpClasses; k += blockDim.x)
+      base[k] = h[k] ? atomicAdd(&d.np_cls[k], h[k]) : 0;
+    __syncthreads();
+    if (cls >= 0) d.np_perm[base[cls] + rank] = p;
+    __syncthreads();
+  }
+}
+
 /* HullVsHull.generateContacts (HullVsHull.hs:54-90) over SAT.contact
- * (SAT.hs:238-258) for every broadphase pair.  One thread per pair; results
- * go to two fixed slots per pair and are compacted after a scan. */
+ * (SAT.hs:238-258) for every broadphase pair.  One thread per pair (taken
+ * in class order); results go to two fixed slots per pair and are compacted
+ * after a scan. */
 __global__ void k_narrowphase(Dev d) {
   const int P = min((int)d.counters[kCntPairs], d.pair_cap);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+    const int p = d.np_perm ? d.np_perm[i] : i;
     const int ga = d.pair_a[p], gb = d.pair_b[p];
     const HullView a = hull_view(d, ga), b = hull_view(d, gb);
     int cnt = 0;
     int e_ab, pen_ab, e_ba, pen_ba;
     double dep_ab, dep_ba;
     if (min_overlap(a, b, &e_ab, &dep_ab, &pen_ab) && min_overlap(b, a, &e_ba, &dep_ba, &pen_ba)) {
-      const bool flip = !(dep_ab < dep_ba);
+      const bool flip = !f_lt(dep_ab, dep_ba);
       const HullView& se = flip ? b : a;
       const HullView& sp = flip ? a : b;
       const int e = flip ? e_ba : e_ab;

@@ -216,3 +216,43 @@ def test_judge_reverts_worlds_over_the_limit(gpu):
     assert b.stats()["predicted"] == 0
     b.close()
     net.close()
+
+
+def test_trained_network_lowers_the_residual_of_new_contacts(gpu):
+    """What the network gains: trained on plain runs of one set of mixed
+    piles, it starts the new contacts of another set so that, at the same
+    sweep count, the solver residual over the impact phase (most contacts
+    new) is clearly lower than with the plain zero start."""
+    train = _mixed(n_worlds=128, n_bodies=64, seed=11)
+    b = _batch(gpu, train)
+    b.collect(2_000_000)
+    b.step(_cfg(gpu, train, iterations=8), 200)
+    feat, tgt = b.samples()
+    b.close()
+    assert len(feat) > 10000
+    net = gpu.Mlp(0)
+    net.fit_normalization(feat, tgt)
+    losses = net.train(feat, tgt, epochs=20, batch=4096, lr=2e-3, seed=0)
+    assert losses[-1] < 0.8 * losses[0]
+
+    test = _mixed(n_worlds=128, n_bodies=64, seed=12)
+
+    def mean_residual(learned, steps=60, iterations=2):
+        bb = _batch(gpu, test)
+        if learned:
+            bb.set_mlp(net)
+        tot, pred = 0.0, 0
+        for _ in range(steps):
+            bb.step(_cfg(gpu, test, iterations=iterations, learned=learned, residual=True), 1)
+            pred += bb.stats()["predicted"]
+            r = np.empty(bb.n_worlds)
+            gpu.check(gpu.lib().shapes_batch_get_world_metrics(bb.handle, r.ctypes.data_as(gpu._dp), None), "m")
+            tot += r.mean()
+        bb.close()
+        return tot / steps, pred
+
+    plain, _ = mean_residual(False)
+    learned, predicted = mean_residual(True)
+    assert predicted > 0
+    assert learned < 0.85 * plain, (learned, plain)
+    net.close()

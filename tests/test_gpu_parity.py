@@ -162,6 +162,26 @@ def test_cache_checkpoint_resume():
         h.close()
 
 
+def test_set_bodies_between_replayed_steps():
+    """A host round trip of the body state between graph-replayed steps (what
+    an FFI caller reading and writing PhysicalObj does every frame) changes
+    nothing: same bits as stepping straight through."""
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=24), list(range(24)))
+    cfg = config_of(sc)
+    a = batch_from_scene(sc)
+    a.step(cfg, 30)
+    b = batch_from_scene(sc)
+    b.step(cfg, 10)
+    for _ in range(20):
+        b.set_bodies(b.get_bodies())
+        b.step(cfg, 1)
+    ga, gb = a.get_bodies(), b.get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(ga[f], gb[f], f"round trip {f}")
+    a.close()
+    b.close()
+
+
 def test_warm_start_off_and_no_gravity():
     sc = scenes.stacks_make_scene((6, 6))
     for warm, ext in ((False, True), (True, False)):
