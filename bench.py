@@ -67,8 +67,13 @@ WORKLOADS = {
     "single": "1 world: 100x1 slab + 20x20 unit squares, dt 1/60, 4 sweeps, warm start",
     "mixed": "the learned workload's scene with the plain start only: 1024 worlds x 256 mixed boxes and "
              "polygons, dt 1/60, 8 sweeps, warm start, gravity (0,-9.8)",
+    "contacts": "1 world of 65,536 convex polygons (3-8 vertices, radius U[0.3,1.0], vertex radii +-10%, "
+                "random rotation) in a 512x512 box: broadphase + SAT + manifolds only (a step = one collide)",
+    "container": "1 world: a 1024-wide static U container holding 262,141 mixed convex polygons (3-8 vertices, "
+                 "radius U[0.3,1.0]) dropped from a grid, dt 1/120, 4 sweeps; order-preserving large-world "
+                 "solver (--coloured: graph-coloured sweep)",
 }
-PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4, "mixed": 8}
+PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4, "mixed": 8, "contacts": 0, "container": 4}
 
 
 def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
@@ -80,6 +85,10 @@ def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
         return scenes.single_world_boxes(seed=0 + seed_offset)
     if workload in ("learned", "mixed"):
         return scenes.batched_mixed(seed=3 + seed_offset, n_worlds=worlds or 1024)
+    if workload == "contacts":
+        return scenes.polygon_field(seed=1 + seed_offset, n=worlds or 65536)
+    if workload == "container":
+        return scenes.container_world(seed=4 + seed_offset, n=worlds or 262144)
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -236,6 +245,31 @@ def cpu_oracle_rate(scene, steps: int, warmup: int, nthreads: int, world_fractio
     return n * steps / secs, n, steps, secs
 
 
+def cpu_sample(workload, scene, steps, warmup, cores):
+    """The oracle on a bounded sample of the workload: (rate, description)."""
+    from oracle import oracle as O
+
+    n = int(scene["world_body_offsets"][-1])
+    if workload == "contacts":
+        w = O.world_from_scene(scene)
+        t0 = time.perf_counter()
+        w.collide()
+        secs = time.perf_counter() - t0
+        return n / secs, f"one collide of all {n} bodies, 1 thread (one world), {secs:.1f} s", 1
+    if workload in ("container", "single"):
+        w = O.world_from_scene(scene)
+        c = scene["config"]
+        k = min(steps, 3 if workload == "container" else 300)
+        t0 = time.perf_counter()
+        w.step(c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"], nsteps=k)
+        secs = time.perf_counter() - t0
+        return n * k / secs, f"{n} bodies x {k} steps from the initial state, 1 thread (one world), {secs:.1f} s", 1
+    cs = min(steps, 300)
+    rate, n, s_, secs = cpu_oracle_rate(scene, cs, warmup, cores)
+    return rate, (f"all {n} bodies x {s_} steps after {warmup} warm-up, plain start, "
+                  f"{int(scene['config']['iterations'])} sweeps, {secs:.1f} s on {cores} threads"), cores
+
+
 def run_reference(args, rank, world):
     """The reference's algorithm on the host cores (the oracle), same metric."""
     if rank != 0:
@@ -247,14 +281,14 @@ def run_reference(args, rank, world):
     O.build()
     cores = multiprocessing.cpu_count()
     scene = make_scene(args.workload, worlds=args.worlds)
-    rate, n, steps, secs = cpu_oracle_rate(scene, args.steps, args.warmup, cores)
+    n = int(scene["world_body_offsets"][-1])
+    rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, cores)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / rate, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "bodies": n},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"whole workload: {n} bodies x {steps} steps after {args.warmup} warm-up"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": used, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -371,11 +405,15 @@ def run_ours(args, rank, world, local):
             run_it, run_learned = min(matched), True
 
     def cfg_for(it, use_net):
-        return _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], it, learned=use_net)
+        return _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], it, learned=use_net,
+                                coloured=args.coloured)
+
+    if args.workload == "contacts":
+        return run_contacts(args, rank, world, local, scene, stream)
 
     # ---- autotune the solver packing on a settled copy (setup, untimed) ------
     tuned = None
-    if not args.no_tune:
+    if not args.no_tune and int(len(scene["world_body_offsets"]) - 1) > 1:
         t = new_batch(_lib, scene, stream)
         t.step(cfg_for(plain_it, False), args.tune_after)
         tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps)
@@ -494,12 +532,8 @@ def run_ours(args, rank, world, local):
     if world == 1 and rank == 0 and not args.no_cpu:
         import multiprocessing
 
-        cores = multiprocessing.cpu_count()
-        cs = min(args.steps, 300)
-        rate, n, s_, secs = cpu_oracle_rate(scene, cs, args.warmup, cores)
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"all {n} bodies x {s_} steps after {args.warmup} warm-up, plain start, "
-                         f"{int(c['iterations'])} sweeps, {secs:.1f} s on {cores} threads"}
+        rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, multiprocessing.cpu_count())
+        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port", "sample": sample}
 
     if rank == 0:
         line = {
@@ -509,6 +543,8 @@ def run_ours(args, rank, world, local):
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
                        "bodies_per_gpu": n_bodies, "worlds_per_gpu": int(len(scene["world_body_offsets"]) - 1),
                        "iterations": run_it, "start": "learned" if run_learned else "plain (previous-frame cache)",
+                       "large_world_solver": ("coloured" if args.coloured else "ordered")
+                       if args.workload == "container" else None,
                        "parallelism": f"worlds sharded, {world} rank(s)",
                        "l2": "inputs larger than L2 (state + contacts + constraints of all worlds)",
                        "launch": "CUDA graph per step",
@@ -529,6 +565,103 @@ def run_ours(args, rank, world, local):
         net.close()
     return 0
 
+
+def run_contacts(args, rank, world, local, scene, stream):
+    """Contact generation only: a step is one collide (pose already current:
+    broadphase, SAT, manifolds, compaction)."""
+    import torch
+
+    from shapes_gb300 import _lib
+
+    n_bodies = int(scene["world_body_offsets"][-1])
+    b = new_batch(_lib, scene, stream)
+    for _ in range(args.warmup):
+        b.collide()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0.record(stream)
+        for _ in range(args.steps):
+            b.collide()
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms_max = max_over_ranks(t0.elapsed_time(t1), world)
+    total = sum_over_ranks(float(n_bodies), world)
+    value = total * args.steps / (ms_max * 1e-3)
+    st = b.stats()
+    b.set_profiling(True)
+    prof_steps = min(args.steps, 10)
+    for _ in range(prof_steps):
+        b.collide()
+    prof = b.get_profile()
+    b.set_profiling(False)
+    # e2e: body state in from pinned host memory, contacts (keys + values) back
+    host = {f: torch.from_numpy(np.ascontiguousarray(scene["bodies"][f])).pin_memory() for f in _lib.BODY_FIELDS}
+    bin_ = _lib.Bodies(*[ctypes.cast(host[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS])
+    cap = int(st["contacts"] * 1.2) + 16
+    keys = torch.empty(5 * cap, dtype=torch.int32, pin_memory=True)
+    vals = torch.empty(5 * cap, dtype=torch.float64, pin_memory=True)
+    wc = np.empty(1, dtype=np.int32)
+    L = _lib.lib()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        _lib.check(L.shapes_batch_set_bodies(b.handle, ctypes.byref(bin_)), "set_bodies")
+        _lib.check(L.shapes_batch_collide(b.handle), "collide")
+        _lib.check(L.shapes_batch_get_contacts(b.handle, ctypes.cast(keys.data_ptr(), _lib._ip),
+                                               ctypes.cast(vals.data_ptr(), _lib._dp), cap,
+                                               wc.ctypes.data_as(_lib._ip)), "get_contacts")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    b.close()
+    np_ms, np_launches = prof["narrowphase"]
+    pairs = st["pairs"]
+    roof = None
+    if np_launches:
+        avg_ms = np_ms / prof_steps
+        bytes_per_launch = pairs * NARROWPHASE_BYTES_PER_PAIR + st["contacts"] * 57
+        achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+        peaks = measured_peaks()
+        roof = {"kernel": "k_narrowphase (+ class sort)", "bound": "hbm", "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "peak_source": peaks["source"], "traffic": None, "bytes_per_pair": NARROWPHASE_BYTES_PER_PAIR,
+                "pairs_per_launch": pairs, "avg_launch_ms": avg_ms,
+                "note": "FP64-bound: SAT projections are 2 multiplies + 1 add per vertex and edge"}
+    cpu = None
+    if world == 1 and rank == 0 and not args.no_cpu:
+        import multiprocessing
+
+        rate, sample, used = cpu_sample("contacts", scene, args.steps, args.warmup, multiprocessing.cpu_count())
+        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port", "sample": sample}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "contacts", "description": WORKLOADS["contacts"], "bodies_per_gpu": n_bodies,
+                       "step": "one collide", "l2": "inputs larger than L2 are not needed: 65,536 hulls (~30 MB)"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": total * args.steps / (e_ms * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": 10 * 8 * n_bodies, "d2h_bytes_per_step": st["contacts"] * 60},
+            "gpu_launches": int(round(sum(v[1] for v in prof.values()) / prof_steps * args.steps)),
+            "clocks": clocks.summary(),
+            "stages_ms_per_step": {k: v[0] / prof_steps for k, v in prof.items()},
+            "last_step": {"pairs": pairs, "contacts": st["contacts"]},
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+# Algorithmic bytes per broadphase pair in the narrowphase: both hulls' posed
+# vertices and edge normals (32 B per vertex, 5.5 vertices on average), the
+# pair's two body indices, and two fixed output slots (2 x (4 + 40) B).
+NARROWPHASE_BYTES_PER_PAIR = 32 * 11 + 8 + 2 * 44
 
 # FP64 lane-operations per solver update: ncu's dadd + dmul + dfma thread
 # instruction counts of one k_schedule_solve launch (26.9 M) divided by its
@@ -555,6 +688,7 @@ def main():
     ap.add_argument("--tune-steps", type=int, default=4, help="steps per autotuner trial")
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
+    ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
     ap.add_argument("--train-worlds", type=int, default=4096, help="worlds of the sample-collection run")
     ap.add_argument("--train-steps", type=int, default=300, help="steps of the sample-collection run")
     ap.add_argument("--train-samples", type=int, default=2_000_000, help="at most this many training samples")

@@ -353,6 +353,24 @@ int shapes_batch_collect(shapes_batch* b, int64_t capacity);
 int shapes_batch_get_samples(shapes_batch* b, float* features, float* targets, int64_t capacity,
                              int64_t* n);
 
+/* ------------------------------------------------------------------------ */
+/* Checkpoint file of the engine state                                        */
+/* ------------------------------------------------------------------------ */
+
+/* EngineState (Engine/Main.hs:32-33) = World + EngineCache, written as one
+ * little-endian file: "SHAPESCK", uint32 version (1), uint32 0x01020304,
+ * int32 n_worlds, int32 n_bodies, int64 n_vertices, int64 n_cache, then
+ * int32 world_body_offsets[n_worlds+1], int32 vert_offsets[n_bodies+1],
+ * double local_xy[2 n_vertices], double bodies[10][n_bodies] (the
+ * shapes_bodies fields in order), int32 cache_world_counts[n_worlds],
+ * int32 cache_keys[4 n_cache], double cache_lambdas[2 n_cache], and a uint64
+ * FNV-1a hash of everything before it.  save writes path + ".tmp" then
+ * renames it; load checks the hash and the sizes and builds a new handle that
+ * continues bit for bit where the saved one stopped.  The External and the
+ * step configuration are not part of it (they are passed to every step). */
+int shapes_batch_save(shapes_batch* b, const char* path);
+int shapes_batch_load(const char* path, shapes_batch** out);
+
 /* Single-world convenience wrappers over a batch of one world. */
 int shapes_world_create(int32_t n_bodies, const shapes_bodies* bodies, const int32_t* vert_offsets,
                         const double* local_verts_xy, const uint8_t* shape_kind,

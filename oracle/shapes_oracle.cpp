@@ -222,6 +222,65 @@ static void broadphase(World& w) {
   }
 }
 
+/* Grid.toGrid + Grid.culledKeys (Broadphase/Grid.hs:67-141), the broadphase
+ * the step calls (Engine/Main.hs:75) with gridAxes = GridAxis 20 1 (-10) on
+ * both axes (Engine/Main.hs:40-41): each body goes into every cell its box
+ * covers, cell (cx, cy) = (floor((x - (-10)) / 1), floor((y - (-10)) / 1)),
+ * keyed cx + 20 * cy (keys alias, as in the reference's IntMap); every cell's
+ * bodies in descending order give candidate pairs, aabbCheck and the
+ * not-both-static test keep the real ones, and sortBy descending + uniq
+ * makes the list.  The result equals the Aabb list above (see broadphase);
+ * boxes with a non-finite or huge coordinate take that path instead. */
+static void grid_broadphase(World& w) {
+  const int n = (int)w.bodies.size();
+  std::vector<Aabb> box(n);
+  for (int i = 0; i < n; ++i) {
+    box[i] = hull_aabb(w.hulls[i]);
+    const Aabb& a = box[i];
+    const double lim = 1e9;
+    if (!(std::fabs(a.x0) < lim && std::fabs(a.x1) < lim && std::fabs(a.y0) < lim && std::fabs(a.y1) < lim)) {
+      broadphase(w);
+      return;
+    }
+  }
+  auto axial = [](double v) { return (int64_t)std::floor((v - (-10.0)) / 1.0); };
+  std::vector<std::pair<int64_t, int>> entries; /* (cell key, body) */
+  for (int i = 0; i < n; ++i) {
+    const Aabb& a = box[i];
+    for (int64_t cx = axial(a.x0); cx <= axial(a.x1); ++cx)
+      for (int64_t cy = axial(a.y0); cy <= axial(a.y1); ++cy) entries.emplace_back(cx + cy * 20, i);
+  }
+  /* cells in key order, bodies descending within a cell, one entry per body */
+  std::sort(entries.begin(), entries.end(), [](const std::pair<int64_t, int>& p, const std::pair<int64_t, int>& q) {
+    return p.first != q.first ? p.first < q.first : p.second > q.second;
+  });
+  entries.erase(std::unique(entries.begin(), entries.end()), entries.end());
+  std::vector<std::pair<int, int>> found;
+  for (size_t s0 = 0; s0 < entries.size();) {
+    size_t s1 = s0;
+    while (s1 < entries.size() && entries[s1].first == entries[s0].first) ++s1;
+    for (size_t p = s0; p < s1; ++p)
+      for (size_t q = p + 1; q < s1; ++q) {
+        const int i = entries[p].second, j = entries[q].second; /* i > j */
+        if (is_static(w.bodies[i]) && is_static(w.bodies[j])) continue;
+        const Aabb& a = box[i];
+        const Aabb& b = box[j];
+        if (bounds_overlap(a.x0, a.x1, b.x0, b.x1) && bounds_overlap(a.y0, a.y1, b.y0, b.y1))
+          found.emplace_back(i, j);
+      }
+    s0 = s1;
+  }
+  std::sort(found.begin(), found.end(), [](const std::pair<int, int>& p, const std::pair<int, int>& q) {
+    return p > q;
+  });
+  found.erase(std::unique(found.begin(), found.end()), found.end());
+  w.pairs.clear();
+  for (const auto& pr : found) {
+    w.pairs.push_back(pr.first);
+    w.pairs.push_back(pr.second);
+  }
+}
+
 /* ---- A6/A7 SAT and manifold ---------------------------------------------- */
 
 struct SatResult {
@@ -528,7 +587,7 @@ static inline void improve_contact(const ContactConstraint& cc, CacheEntry& cach
 /* updateWorld (Engine/Main.hs:71-84). */
 static void step_world(World& w, const StepConfig& cfg) {
   /* 1. broadphase on the shapes posed at the end of the previous step */
-  broadphase(w);
+  grid_broadphase(w);
   /* 2. applyExternal (World.hs:156-158) with constantAccel (External.hs:23-28) */
   if (cfg.external) {
     for (Body& b : w.bodies) {
@@ -644,7 +703,7 @@ void oracle_world_step(void* h, const double* cfg5, int32_t iterations, int32_t 
  * worldContacts query, shapes-demo/src/Physics/Demo/IOWorld.hs:74-81). */
 void oracle_world_collide(void* h) {
   World& w = *static_cast<World*>(h);
-  broadphase(w);
+  grid_broadphase(w);
   narrowphase(w);
 }
 

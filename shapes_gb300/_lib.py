@@ -143,6 +143,8 @@ SIGNATURES = [
     ("shapes_mlp_train", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, ctypes.POINTER(TrainConfig),
                                         _fp]),
     ("shapes_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_save", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    ("shapes_batch_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     ("shapes_batch_set_mlp", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("shapes_batch_get_learned_mask", ctypes.c_int, [ctypes.c_void_p, _up]),
     ("shapes_batch_set_learned_mask", ctypes.c_int, [ctypes.c_void_p, _up]),
@@ -327,6 +329,25 @@ class Batch:
 
     def set_launch(self, target_bodies_per_group: int, threads: int) -> None:
         check(lib().shapes_batch_set_launch(self._h, target_bodies_per_group, threads), "shapes_batch_set_launch")
+
+    def save(self, path) -> None:
+        """Checkpoint file of the bodies, topology and contact cache."""
+        check(lib().shapes_batch_save(self._h, str(path).encode()), "shapes_batch_save")
+
+    @classmethod
+    def load(cls, path) -> "Batch":
+        """A new handle from a checkpoint file."""
+        h = ctypes.c_void_p()
+        check(lib().shapes_batch_load(str(path).encode(), ctypes.byref(h)), "shapes_batch_load")
+        self = cls.__new__(cls)
+        self._h = h
+        L = lib()
+        nw, nb, nv = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        check(L.shapes_batch_num_worlds(h, ctypes.byref(nw)), "num_worlds")
+        check(L.shapes_batch_num_bodies(h, ctypes.byref(nb)), "num_bodies")
+        check(L.shapes_batch_num_vertices(h, ctypes.byref(nv)), "num_vertices")
+        self.n_worlds, self.n_bodies, self.n_verts = nw.value, nb.value, nv.value
+        return self
 
     def set_graphs(self, enabled: bool) -> None:
         """CUDA-graph replay of the step (default on)."""

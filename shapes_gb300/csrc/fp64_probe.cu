@@ -103,6 +103,74 @@ __global__ void k_div_check(unsigned long long n, unsigned long long seed, unsig
   }
 }
 
+/* Operand classes for mul_rn_int: random mantissas with exponents straddling
+ * the fast range, short (sparse) mantissas whose products are exact or exact
+ * ties, all-ones / 2^k +- 1 mantissas, products next to overflow, zeros next
+ * to finite and non-finite values, and subnormal, infinite and NaN operands. */
+__device__ void mul_operands(unsigned long long k, unsigned long long seed, double* a, double* b) {
+  const unsigned long long r0 = mix64(k ^ seed), r1 = mix64(r0), r2 = mix64(r1), r3 = mix64(r2);
+  const int cls = (int)(r3 % 8);
+  int ea = 480 + (int)(r1 % 1091), eb = 480 + (int)(r2 % 1091); /* [480, 1570] */
+  unsigned long long ma = r0, mb = r2 >> 5;
+  if (cls == 1) {
+    ma &= ~((1ull << (r1 % 52)) - 1ull);
+    mb &= ~((1ull << (r2 % 52)) - 1ull);
+  }
+  if (cls == 2) {
+    ma = (r3 & 2) ? 0xfffffffffffffull : (1ull << (r1 % 52)) + ((r0 & 1) ? 1ull : 0xfffffffffffffull);
+    mb = (r3 & 4) ? 0xfffffffffffffull : (1ull << (r2 % 52)) - 1ull;
+  }
+  if (cls == 3) {
+    ea = 1500 + (int)(r1 % 40);
+    eb = 1500 + (int)(r2 % 40);
+  }
+  *a = make_double(r0 >> 63, ea, ma);
+  *b = make_double(r1 >> 63, eb, mb);
+  if (cls == 4) *a = (r3 & 8) ? -0.0 : 0.0;
+  if (cls == 5) {
+    const int pick = (int)((r3 >> 8) % 5);
+    const double sp = pick == 0 ? __longlong_as_double(0x7ff0000000000000ll)
+                    : pick == 1 ? __longlong_as_double((long long)0xfff0000000000000ull)
+                    : pick == 2 ? __longlong_as_double(0x7ff8000000000000ll)
+                    : pick == 3 ? make_double(r0 >> 63, 0, ma)        /* subnormal */
+                                : ((r3 & 16) ? -0.0 : 0.0);
+    if (r3 & 32) *a = sp; else *b = sp;
+  }
+  if (cls == 6) *b = make_double(r1 >> 63, 1023 + (int)(r2 % 3) - 1, mb & 0xff00000000000ull);
+}
+
+__global__ void k_mul_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                            double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    double a, b;
+    mul_operands(k, seed, &a, &b);
+    const double q = shapes::mul_rn_int(a, b);
+    const double ref = __dmul_rn(a, b);
+    const bool same = __double_as_longlong(q) == __double_as_longlong(ref) || (q != q && ref != ref);
+    if (!same && atomicAdd(bad, 1ull) == 0) {
+      first[0] = a;
+      first[1] = b;
+    }
+  }
+}
+
+/* Dependent-chain throughput of the hardware multiply and of mul_rn_int. */
+template <bool INT>
+__global__ void k_mul_chains(double* out, int iters) {
+  double a0 = 1.0 + threadIdx.x * 1e-6, a1 = a0 + 0.25, a2 = a0 + 0.5, a3 = a0 + 0.75;
+  const double c = 0.99999999999;
+  for (int i = 0; i < iters; ++i) {
+    if (INT) {
+      a0 = shapes::mul_rn_int(a0, c); a1 = shapes::mul_rn_int(a1, c);
+      a2 = shapes::mul_rn_int(a2, c); a3 = shapes::mul_rn_int(a3, c);
+    } else {
+      a0 = __dmul_rn(a0, c); a1 = __dmul_rn(a1, c); a2 = __dmul_rn(a2, c); a3 = __dmul_rn(a3, c);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3;
+}
+
 __global__ void k_cmp_check(const double* v, int n, unsigned long long* bad) {
   const int i = blockIdx.x, j = threadIdx.x;
   if (i >= n || j >= n) return;
@@ -130,6 +198,55 @@ extern "C" int shapes_probe_div_check(unsigned long long n, unsigned long long s
   const cudaError_t err = cudaGetLastError();
   cudaFree(d_bad);
   cudaFree(d_first);
+  return err == cudaSuccess ? 0 : -5;
+}
+
+/* Compares mul_rn_int with the hardware multiply on n generated pairs. */
+extern "C" int shapes_probe_mul_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                                      double* first_ab) {
+  unsigned long long* d_bad = nullptr;
+  double* d_first = nullptr;
+  if (cudaMalloc(&d_bad, sizeof(unsigned long long)) != cudaSuccess) return -5;
+  if (cudaMalloc(&d_first, 2 * sizeof(double)) != cudaSuccess) return -5;
+  cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  cudaMemset(d_first, 0, 2 * sizeof(double));
+  k_mul_check<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaMemcpy(first_ab, d_first, 2 * sizeof(double), cudaMemcpyDeviceToHost);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  return err == cudaSuccess ? 0 : -5;
+}
+
+/* Multiplies per second (whole GPU, 16 warps per SM, 4 chains per thread):
+ * out[0] hardware, out[1] mul_rn_int. */
+extern "C" int shapes_probe_mul_rate(double* out2) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -5;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -5;
+  const int threads = 256, blocks = sms * 2, iters = 4000;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * threads * blocks) != cudaSuccess) return -5;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int v = 0; v < 2; ++v) {
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) { /* first pass warms up */
+      cudaEventRecord(e0);
+      if (v == 0) k_mul_chains<false><<<blocks, threads>>>(d, iters);
+      else k_mul_chains<true><<<blocks, threads>>>(d, iters);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    out2[v] = ms > 0.f ? (double)blocks * threads * iters * 4.0 / (ms * 1e-3) : 0.0;
+  }
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
   return err == cudaSuccess ? 0 : -5;
 }
 

@@ -137,9 +137,12 @@ __global__ void k_lw_rank(Dev d, LW w) {
   }
 }
 
-__global__ void k_lw_hit_list(LW w, unsigned long long* hits) {
+__global__ void k_lw_hit_list(LW w, unsigned long long* hits, unsigned long long* items, int iterations) {
   lw_range(w);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(hits, (unsigned long long)w.hitoff[w.nc]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(hits, (unsigned long long)w.hitoff[w.nc]);
+    atomicAdd(items, (unsigned long long)w.hitoff[w.nc] + (unsigned long long)iterations * (unsigned long long)w.nc);
+  }
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < w.nc; k += gridDim.x * blockDim.x)
     if (w.hitflag[k]) w.hit_idx[w.hitoff[k]] = k;
 }

@@ -15,6 +15,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -658,7 +659,8 @@ struct shapes_batch {
       shapes::k_lw_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
       shapes::k_lw_rank<<<grid_for(w.nb, 128), 128, 0, stream>>>(d, w);
       scan_raw(w.hitflag, cap, w.ctl + 4, w.hitoff);
-      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w, counters + shapes::kCntHits);
+      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w, counters + shapes::kCntHits,
+                                                                    counters + shapes::kCntItems, cfg.iterations);
     });
     stage(4, 1, [&]() {
       if (cfg.external)
@@ -1509,6 +1511,188 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     if (chosen_threads) *chosen_threads = b->solve_threads;
     return rc;
   });
+}
+
+/* ---- checkpoint file (EngineState: World + EngineCache) ------------------ */
+
+}  // extern "C"
+
+namespace {
+
+constexpr char kCkMagic[8] = {'S', 'H', 'A', 'P', 'E', 'S', 'C', 'K'};
+constexpr uint32_t kCkVersion = 1;
+constexpr uint32_t kCkEndian = 0x01020304u;
+
+uint64_t fnv1a(const unsigned char* p, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+  for (size_t k = 0; k < n; ++k) {
+    h ^= p[k];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+struct CkWriter {
+  std::vector<unsigned char> buf;
+  template <class T>
+  void put(const T* p, size_t n) {
+    const unsigned char* c = reinterpret_cast<const unsigned char*>(p);
+    buf.insert(buf.end(), c, c + sizeof(T) * n);
+  }
+  template <class T>
+  void put1(T v) { put(&v, 1); }
+};
+
+struct CkReader {
+  const std::vector<unsigned char>& buf;
+  size_t at = 0;
+  bool ok = true;
+  template <class T>
+  void get(T* p, size_t n) {
+    const size_t bytes = sizeof(T) * n;
+    if (!ok || buf.size() - at < bytes) {
+      ok = false;
+      return;
+    }
+    std::memcpy(p, buf.data() + at, bytes);
+    at += bytes;
+  }
+  template <class T>
+  T get1() {
+    T v{};
+    get(&v, 1);
+    return v;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int shapes_batch_save(shapes_batch* b, const char* path) {
+  if (!b || !path) return SHAPES_E_INVALID_ARG;
+  const int32_t W = b->W, N = b->N;
+  const int64_t V = b->V;
+  std::vector<double> body(10 * (size_t)N);
+  shapes_bodies out{};
+  double* bp[10];
+  for (int k = 0; k < 10; ++k) bp[k] = body.data() + (size_t)k * N;
+  out.vel_x = bp[0]; out.vel_y = bp[1]; out.rot_vel = bp[2]; out.pos_x = bp[3]; out.pos_y = bp[4];
+  out.rot = bp[5]; out.inv_mass_lin = bp[6]; out.inv_mass_rot = bp[7]; out.mu = bp[8]; out.bounce = bp[9];
+  int rc = shapes_batch_get_bodies(b, &out);
+  if (rc != SHAPES_OK) return rc;
+  int64_t nc = 0;
+  rc = shapes_batch_num_cache(b, &nc);
+  if (rc != SHAPES_OK) return rc;
+  std::vector<int32_t> keys(4 * (size_t)std::max<int64_t>(nc, 1)), wc(W);
+  std::vector<double> lam(2 * (size_t)std::max<int64_t>(nc, 1));
+  rc = shapes_batch_get_cache(b, keys.data(), lam.data(), nc, wc.data());
+  if (rc != SHAPES_OK) return rc;
+  std::vector<int32_t> vo(N + 1);
+  std::vector<double> lx(V), ly(V);
+  rc = guarded([&]() -> int {
+    ck(cudaMemcpyAsync(vo.data(), b->vert_off, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(lx.data(), b->lx, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(ly.data(), b->ly, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    return SHAPES_OK;
+  });
+  if (rc != SHAPES_OK) return rc;
+  CkWriter w;
+  w.put(kCkMagic, 8);
+  w.put1(kCkVersion);
+  w.put1(kCkEndian);
+  w.put1(W);
+  w.put1(N);
+  w.put1(V);
+  w.put1(nc);
+  w.put(b->h_world_body_off.data(), (size_t)W + 1);
+  w.put(vo.data(), (size_t)N + 1);
+  for (int64_t k = 0; k < V; ++k) {
+    w.put1(lx[k]);
+    w.put1(ly[k]);
+  }
+  w.put(body.data(), body.size());
+  w.put(wc.data(), (size_t)W);
+  w.put(keys.data(), 4 * (size_t)nc);
+  w.put(lam.data(), 2 * (size_t)nc);
+  w.put1(fnv1a(w.buf.data(), w.buf.size()));
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) {
+    g_last_error = "cannot open " + tmp;
+    return SHAPES_E_INVALID_ARG;
+  }
+  const bool wrote = std::fwrite(w.buf.data(), 1, w.buf.size(), f) == w.buf.size();
+  const bool closed = std::fclose(f) == 0;
+  if (!wrote || !closed || std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    g_last_error = std::string("cannot write ") + path;
+    return SHAPES_E_INVALID_ARG;
+  }
+  return SHAPES_OK;
+}
+
+int shapes_batch_load(const char* path, shapes_batch** out) {
+  if (!path || !out) return SHAPES_E_INVALID_ARG;
+  *out = nullptr;
+  std::vector<unsigned char> buf;
+  {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+      g_last_error = std::string("cannot open ") + path;
+      return SHAPES_E_INVALID_ARG;
+    }
+    unsigned char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+    std::fclose(f);
+  }
+  auto bad = [&](const char* why) {
+    g_last_error = std::string("checkpoint ") + path + ": " + why;
+    return SHAPES_E_INVALID_ARG;
+  };
+  if (buf.size() < 48 + sizeof(uint64_t)) return bad("too short");
+  uint64_t sum = 0;
+  std::memcpy(&sum, buf.data() + buf.size() - sizeof(uint64_t), sizeof sum);
+  if (fnv1a(buf.data(), buf.size() - sizeof(uint64_t)) != sum) return bad("checksum mismatch");
+  CkReader r{buf};
+  char magic[8];
+  r.get(magic, 8);
+  if (std::memcmp(magic, kCkMagic, 8) != 0) return bad("not a shapes checkpoint");
+  if (r.get1<uint32_t>() != kCkVersion) return bad("unsupported version");
+  if (r.get1<uint32_t>() != kCkEndian) return bad("byte order differs");
+  const int32_t W = r.get1<int32_t>(), N = r.get1<int32_t>();
+  const int64_t V = r.get1<int64_t>(), nc = r.get1<int64_t>();
+  if (!r.ok || W < 1 || N < 1 || V < 3 || nc < 0 || V > (int64_t)INT32_MAX || nc > (int64_t)INT32_MAX)
+    return bad("bad sizes");
+  const uint64_t need = 48ull + 4ull * (W + 1) + 4ull * (N + 1) + 16ull * V + 80ull * N + 4ull * W + 16ull * nc +
+                        16ull * nc + 8ull;
+  if (buf.size() != need) return bad("size does not match the header");
+  std::vector<int32_t> off(W + 1), vo(N + 1), wc(W), keys(4 * (size_t)std::max<int64_t>(nc, 1));
+  std::vector<double> xy(2 * (size_t)V), body(10 * (size_t)N), lam(2 * (size_t)std::max<int64_t>(nc, 1));
+  r.get(off.data(), off.size());
+  r.get(vo.data(), vo.size());
+  r.get(xy.data(), xy.size());
+  r.get(body.data(), body.size());
+  r.get(wc.data(), wc.size());
+  r.get(keys.data(), 4 * (size_t)nc);
+  r.get(lam.data(), 2 * (size_t)nc);
+  if (!r.ok) return bad("truncated");
+  shapes_bodies in{};
+  double* bp[10];
+  for (int k = 0; k < 10; ++k) bp[k] = body.data() + (size_t)k * N;
+  in.vel_x = bp[0]; in.vel_y = bp[1]; in.rot_vel = bp[2]; in.pos_x = bp[3]; in.pos_y = bp[4];
+  in.rot = bp[5]; in.inv_mass_lin = bp[6]; in.inv_mass_rot = bp[7]; in.mu = bp[8]; in.bounce = bp[9];
+  shapes_batch* h = nullptr;
+  int rc = shapes_batch_create(W, off.data(), &in, vo.data(), xy.data(), nullptr, &h);
+  if (rc != SHAPES_OK) return rc;
+  rc = shapes_batch_set_cache(h, wc.data(), keys.data(), lam.data());
+  if (rc != SHAPES_OK) {
+    shapes_batch_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return SHAPES_OK;
 }
 
 int shapes_batch_set_graphs(shapes_batch* b, int32_t enabled) {

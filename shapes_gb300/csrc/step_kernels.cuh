@@ -265,8 +265,9 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
     double bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
     for (int k = 0; k < nv; ++k) {
       const double lx = d.lx[b0 + k], ly = d.ly[b0 + k];
-      const double x = t_nan ? (m00 * lx + m01 * ly) + m02 * 1.0 : (m00 * lx + m01 * ly) + m02;
-      const double y = t_nan ? (m10 * lx + m11 * ly) + m12 * 1.0 : (m10 * lx + m11 * ly) + m12;
+      /* one product per coordinate on the integer pipe (exact), as in SAT */
+      const double x = t_nan ? (m00 * lx + m01 * ly) + m02 * 1.0 : (mul_rn_int(m00, lx) + m01 * ly) + m02;
+      const double y = t_nan ? (m10 * lx + m11 * ly) + m12 * 1.0 : (mul_rn_int(m10, lx) + m11 * ly) + m12;
       d.wx[b0 + k] = x;
       d.wy[b0 + k] = y;
       if (k == 0) {
@@ -620,13 +621,16 @@ __device__ __forceinline__ bool sat_axis(const HullView& se, int e, const HullVi
   const int mi = se.emin[e], ma = se.emax[e];
   const double sa = se.wx[mi] * dx + se.wy[mi] * dy;
   const double sb = se.wx[ma] * dx + se.wy[ma] * dy;
-  const double t0 = sp.wx[0] * dx + sp.wy[0] * dy;
+  /* one product of each projection on the integer pipe (mul_rn_int, exact),
+   * the other on the FP64 pipe: the kernel is bound by FP64 throughput at
+   * high occupancy, so the two pipes share the work */
+  const double t0 = mul_rn_int(sp.wx[0], dx) + sp.wy[0] * dy;
   double lo = t0, hi = t0;
   uint64_t klo = okey(t0), khi = klo;
   const bool pinned = nan_bits(t0);
   int pmin = 0;
   for (int k = 1; k < sp.nv; ++k) {
-    const double t = sp.wx[k] * dx + sp.wy[k] * dy;
+    const double t = mul_rn_int(sp.wx[k], dx) + sp.wy[k] * dy;
     if (pinned || nan_bits(t)) continue;
     const uint64_t kt = okey(t);
     if (kt < klo) { lo = t; klo = kt; pmin = k; }
@@ -1002,6 +1006,7 @@ __device__ __forceinline__ void apply_impulse(const double j[6], double l, doubl
   for (int k = 0; k < 6; ++k) v[k] = v[k] + (j[k] * l) * m[k];
 }
 
+/* J . v as a left fold (Shapes/Linear/Template.hs:108-110). */
 __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
   double s = j[0] * v[0];
 #pragma unroll

@@ -23,6 +23,8 @@ def probe(built):
                                            ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_double)]
     lib.shapes_probe_cmp_check.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_ulonglong)]
+    lib.shapes_probe_mul_check.argtypes = lib.shapes_probe_div_check.argtypes
+    lib.shapes_probe_mul_rate.argtypes = [ctypes.POINTER(ctypes.c_double)]
     return lib
 
 
@@ -45,3 +47,18 @@ def test_integer_comparisons_match_ieee(probe):
     assert probe.shapes_probe_cmp_check(vals.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(vals),
                                         ctypes.byref(bad)) == 0
     assert bad.value == 0
+
+
+@pytest.mark.parametrize("seed", [21, 22, 23, 24])
+def test_integer_pipe_multiply_matches_hardware(probe, seed):
+    bad = ctypes.c_ulonglong()
+    first = (ctypes.c_double * 2)()
+    assert probe.shapes_probe_mul_check(1 << 28, seed, ctypes.byref(bad), first) == 0
+    assert bad.value == 0, f"{bad.value} mismatches, first a={first[0]!r} b={first[1]!r}"
+
+
+def test_integer_pipe_multiply_rate(probe):
+    rates = (ctypes.c_double * 2)()
+    assert probe.shapes_probe_mul_rate(rates) == 0
+    assert rates[0] > 0 and rates[1] > 0
+    print(f"multiplies/s: hardware {rates[0]:.3e}, integer pipe {rates[1]:.3e}")

@@ -140,6 +140,27 @@ def test_grid_broadphase_equals_aabb_pairs(O, seed):
     want = grid_culled_keys(xy, sc["vert_offsets"], static)
     assert got == want
     assert len(got) > 50
+    # and the Grid list is the Aabb list (Aabb.culledKeys over unorderedPairs)
+    assert got == aabb_culled_keys(xy, sc["vert_offsets"], static)
+
+
+def aabb_culled_keys(world_xy, vert_off, static):
+    """Aabb.culledKeys over unorderedPairs (Broadphase/Aabb.hs:155-183):
+    every (i, j), i > j, descending, not both static, closed boxes overlap."""
+    n = len(vert_off) - 1
+    boxes = []
+    for i in range(n):
+        pts = world_xy[vert_off[i]:vert_off[i + 1]]
+        boxes.append((pts[:, 0].min(), pts[:, 0].max(), pts[:, 1].min(), pts[:, 1].max()))
+    out = []
+    for i in range(n - 1, 0, -1):
+        for j in range(i - 1, -1, -1):
+            if static[i] and static[j]:
+                continue
+            a, b = boxes[i], boxes[j]
+            if not (b[0] > a[1] or b[1] < a[0]) and not (b[2] > a[3] or b[3] < a[2]):
+                out.append((i, j))
+    return out
 
 
 def test_pairs_descending_and_contacts_descending(O):
