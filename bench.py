@@ -303,14 +303,14 @@ def new_batch(_lib, scene, stream, tuned=None):
     return b
 
 
-def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10):
+def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10, coloured=False):
     """Steps a fresh copy with the residual flag: (mean over steps of the
     world-mean residual, mean over sampled steps of the world-mean largest
     depth, per-world max residual, per-world max depth, contacts started by
     the network)."""
     c = scene["config"]
     cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], iterations, residual=True,
-                           learned=net is not None)
+                           learned=net is not None, coloured=coloured)
     b = new_batch(_lib, scene, stream)
     if net is not None:
         b.set_mlp(net)
@@ -470,6 +470,34 @@ def run_ours(args, rank, world, local):
         learned["timed"] = {"start": "learned" if run_learned else "plain", "iterations": run_it,
                             "predicted_per_step": st["predicted"] / args.steps, "reverted": st["reverted"]}
 
+    # ---- large world: ordered vs coloured, each with and without the network
+    large = None
+    if args.workload == "container" and args.large_quality:
+        lnet, linfo = train_network(_lib, stream, args, rank)
+        qs = args.quality_steps
+        large = {"steps": qs, "iterations": plain_it, "training": linfo, "runs": []}
+        for coloured in (False, True):
+            for use_net in (False, True):
+                r_, d_, _, _, pred = quality_run(_lib, scene, stream, plain_it, qs, net=lnet if use_net else None,
+                                                 coloured=coloured)
+                bq = new_batch(_lib, scene, stream)
+                if use_net:
+                    bq.set_mlp(lnet)
+                cq = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], plain_it, learned=use_net,
+                                      coloured=coloured)
+                q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                q0.record(stream)
+                bq.step(cq, qs)
+                q1.record(stream)
+                torch.cuda.synchronize()
+                bq.close()
+                large["runs"].append({"solver": "coloured" if coloured else "ordered", "start": "learned" if use_net
+                                      else "plain", "mean_residual": r_, "mean_max_depth": d_,
+                                      "predicted_per_step": pred / qs,
+                                      "body_steps_per_s": n_bodies * qs / (q0.elapsed_time(q1) * 1e-3)})
+        lnet.close()
+
     # ---- e2e: host buffers through the C ABI every step --------------------
     b = new_batch(_lib, scene, stream, tuned)
     if run_learned:
@@ -560,6 +588,8 @@ def run_ours(args, rank, world, local):
         }
         if learned is not None:
             line["learned"] = learned
+        if large is not None:
+            line["large_world"] = large
         print(json.dumps(line), flush=True)
     if net is not None:
         net.close()
@@ -689,6 +719,8 @@ def main():
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
+    ap.add_argument("--large-quality", action="store_true",
+                    help="container: residual, depth and speed of ordered vs coloured, with and without the network")
     ap.add_argument("--train-worlds", type=int, default=4096, help="worlds of the sample-collection run")
     ap.add_argument("--train-steps", type=int, default=300, help="steps of the sample-collection run")
     ap.add_argument("--train-samples", type=int, default=2_000_000, help="at most this many training samples")

@@ -354,6 +354,27 @@ int shapes_batch_get_samples(shapes_batch* b, float* features, float* targets, i
                              int64_t* n);
 
 /* ------------------------------------------------------------------------ */
+/* World mutation                                                             */
+/* ------------------------------------------------------------------------ */
+
+/* World.delete (World.hs:90-91) = EmptiesVector.safeDelete
+ * (Utils/EmptiesVector.hs:57-69): the slot (world-local index) must be filled
+ * (else SHAPES_E_INVALID_ARG); it becomes empty and the top of the world's
+ * empty-slot stack.  An empty slot keeps its last state, takes no part in the
+ * step and keeps its index, so contact keys of the other bodies do not change. */
+int shapes_batch_delete_body(shapes_batch* b, int32_t world, int32_t slot);
+/* World.append (World.hs:83-89) = EmptiesVector.append
+ * (Utils/EmptiesVector.hs:72-86): fills the top of the world's empty-slot
+ * stack (the slot freed last); with no empty slot the world grows by one slot
+ * at its end (the reference's fixed-capacity vector would be full).  body10
+ * holds the ten shapes_bodies fields of the new body in order; the hull is
+ * posed at once (makeWorldObj, World.hs:142-149).  *slot receives the slot. */
+int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body10, int32_t n_verts,
+                             const double* local_verts_xy, int32_t* slot);
+/* Filled (1) or empty (0) per slot, over all worlds' slots (n_bodies bytes). */
+int shapes_batch_get_active(shapes_batch* b, uint8_t* out);
+
+/* ------------------------------------------------------------------------ */
 /* Checkpoint file of the engine state                                        */
 /* ------------------------------------------------------------------------ */
 
@@ -363,8 +384,10 @@ int shapes_batch_get_samples(shapes_batch* b, float* features, float* targets, i
  * int32 world_body_offsets[n_worlds+1], int32 vert_offsets[n_bodies+1],
  * double local_xy[2 n_vertices], double bodies[10][n_bodies] (the
  * shapes_bodies fields in order), int32 cache_world_counts[n_worlds],
- * int32 cache_keys[4 n_cache], double cache_lambdas[2 n_cache], and a uint64
- * FNV-1a hash of everything before it.  save writes path + ".tmp" then
+ * int32 cache_keys[4 n_cache], double cache_lambdas[2 n_cache], uint8
+ * filled[n_bodies] (World.delete / append), int32 empty_count[n_worlds], the
+ * worlds' empty-slot stacks (int32, bottom to top, world by world), and a
+ * uint64 FNV-1a hash of everything before it.  save writes path + ".tmp" then
  * renames it; load checks the hash and the sizes and builds a new handle that
  * continues bit for bit where the saved one stopped.  The External and the
  * step configuration are not part of it (they are passed to every step). */

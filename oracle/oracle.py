@@ -67,6 +67,11 @@ def lib() -> ctypes.CDLL:
         L.oracle_unordered_pairs_count.restype = ctypes.c_int64
         L.oracle_unordered_pairs_count.argtypes = [ctypes.c_int32]
         L.oracle_sincos.argtypes = [_dp, _dp, _dp, ctypes.c_int64]
+        L.oracle_world_delete.restype = ctypes.c_int32
+        L.oracle_world_delete.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.oracle_world_append.restype = ctypes.c_int32
+        L.oracle_world_append.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32, _dp]
+        L.oracle_world_get_active.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8)]
         _LIB = L
     return _LIB
 
@@ -105,6 +110,23 @@ class OracleWorld:
 
     def collide(self):
         lib().oracle_world_collide(self._h)
+
+    def delete(self, slot: int) -> int:
+        """World.delete: 0, or -1 for an empty slot."""
+        return int(lib().oracle_world_delete(self._h, slot))
+
+    def append(self, body10, local_xy) -> int:
+        """World.append: the slot filled (last freed first, else a new one)."""
+        b = np.ascontiguousarray(body10, dtype=np.float64)
+        xy = np.ascontiguousarray(local_xy, dtype=np.float64).reshape(-1)
+        slot = int(lib().oracle_world_append(self._h, _p(b, _dp), len(xy) // 2, _p(xy, _dp)))
+        self.n = int(lib().oracle_world_num_bodies(self._h))
+        return slot
+
+    def active(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.uint8)
+        lib().oracle_world_get_active(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        return out
 
     def residual(self) -> float:
         """RMS of what one more sweep would apply after the last step."""

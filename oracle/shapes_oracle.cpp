@@ -91,6 +91,11 @@ struct ContactConstraint {
 struct World {
   double residual = 0.0; /* RMS of one non-applying sweep after the last step */
   std::vector<Body> bodies;
+  /* EmptiesVector (Utils/EmptiesVector.hs): filled slots, and the empty
+   * slots as a stack (delete pushes, append pops: the last slot freed is the
+   * next one filled) */
+  std::vector<uint8_t> active;
+  std::vector<int32_t> empties;
   std::vector<Hull> hulls;
   std::vector<CacheEntry> cache;
   std::vector<int32_t> pairs; /* flattened (i, j) */
@@ -210,7 +215,9 @@ static void broadphase(World& w) {
   for (int i = 0; i < n; ++i) box[i] = hull_aabb(w.hulls[i]);
   w.pairs.clear();
   for (int i = n - 1; i >= 1; --i) {
+    if (!w.active[i]) continue;
     for (int j = i - 1; j >= 0; --j) {
+      if (!w.active[j]) continue;
       if (is_static(w.bodies[i]) && is_static(w.bodies[j])) continue;
       const Aabb& a = box[i];
       const Aabb& b = box[j];
@@ -238,7 +245,7 @@ static void grid_broadphase(World& w) {
     box[i] = hull_aabb(w.hulls[i]);
     const Aabb& a = box[i];
     const double lim = 1e9;
-    if (!(std::fabs(a.x0) < lim && std::fabs(a.x1) < lim && std::fabs(a.y0) < lim && std::fabs(a.y1) < lim)) {
+    if (w.active[i] && !(std::fabs(a.x0) < lim && std::fabs(a.x1) < lim && std::fabs(a.y0) < lim && std::fabs(a.y1) < lim)) {
       broadphase(w);
       return;
     }
@@ -246,6 +253,7 @@ static void grid_broadphase(World& w) {
   auto axial = [](double v) { return (int64_t)std::floor((v - (-10.0)) / 1.0); };
   std::vector<std::pair<int64_t, int>> entries; /* (cell key, body) */
   for (int i = 0; i < n; ++i) {
+    if (!w.active[i]) continue; /* empty slots are not traversed (EmptiesVector.mapM_) */
     const Aabb& a = box[i];
     for (int64_t cx = axial(a.x0); cx <= axial(a.x1); ++cx)
       for (int64_t cy = axial(a.y0); cy <= axial(a.y1); ++cy) entries.emplace_back(cx + cy * 20, i);
@@ -590,8 +598,9 @@ static void step_world(World& w, const StepConfig& cfg) {
   grid_broadphase(w);
   /* 2. applyExternal (World.hs:156-158) with constantAccel (External.hs:23-28) */
   if (cfg.external) {
-    for (Body& b : w.bodies) {
-      if (!(0.0 == b.iml)) {
+    for (size_t i = 0; i < w.bodies.size(); ++i) {
+      Body& b = w.bodies[i];
+      if (w.active[i] && !(0.0 == b.iml)) {
         b.vx = b.vx + cfg.ax * cfg.dt;
         b.vy = b.vy + cfg.ay * cfg.dt;
       }
@@ -651,13 +660,16 @@ static void step_world(World& w, const StepConfig& cfg) {
   }
   w.cache.swap(lag);
   /* 6. advance (World.hs:167-169) → advanceObj (Constraint.hs:225-229) */
-  for (Body& b : w.bodies) {
+  for (size_t i = 0; i < w.bodies.size(); ++i) {
+    if (!w.active[i]) continue;
+    Body& b = w.bodies[i];
     b.px = (b.vx * cfg.dt) + b.px;
     b.py = (b.vy * cfg.dt) + b.py;
     b.th = (cfg.dt * b.w) + b.th;
   }
   /* 7. moveShapes (World.hs:136-140) */
-  for (size_t i = 0; i < w.bodies.size(); ++i) pose_hull(w.bodies[i], w.hulls[i]);
+  for (size_t i = 0; i < w.bodies.size(); ++i)
+    if (w.active[i]) pose_hull(w.bodies[i], w.hulls[i]);
 }
 
 static StepConfig make_cfg(const double* c5, int32_t iterations, int32_t warm_start, int32_t external) {
@@ -680,6 +692,7 @@ void* oracle_world_create(int32_t n, const double* bodies10, const int32_t* vert
   World* w = new World();
   w->bodies.resize(n);
   w->hulls.resize(n);
+  w->active.assign(n, 1);
   for (int32_t i = 0; i < n; ++i) {
     const double* r = bodies10 + 10 * (size_t)i;
     w->bodies[i] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
@@ -690,6 +703,46 @@ void* oracle_world_create(int32_t n, const double* bodies10, const int32_t* vert
 }
 
 void oracle_world_destroy(void* h) { delete static_cast<World*>(h); }
+
+/* World.delete (World.hs:90-91) = EmptiesVector.safeDelete: the slot must be
+ * filled; it becomes the top of the empty-slot stack.  Returns 0, or -1 for
+ * an empty or out-of-range slot. */
+int32_t oracle_world_delete(void* h, int32_t slot) {
+  World& w = *static_cast<World*>(h);
+  if (slot < 0 || slot >= (int32_t)w.bodies.size() || !w.active[slot]) return -1;
+  w.active[slot] = 0;
+  w.empties.push_back(slot);
+  return 0;
+}
+
+/* World.append (World.hs:83-89) = EmptiesVector.append: fills the top of the
+ * empty-slot stack; with no empty slot the world grows by one slot at the end
+ * (the reference's vector would be full).  The shape is posed at once
+ * (makeWorldObj, World.hs:142-149).  Returns the slot. */
+int32_t oracle_world_append(void* h, const double* body10, int32_t nv, const double* local_xy) {
+  World& w = *static_cast<World*>(h);
+  int32_t slot;
+  if (!w.empties.empty()) {
+    slot = w.empties.back();
+    w.empties.pop_back();
+  } else {
+    slot = (int32_t)w.bodies.size();
+    w.bodies.emplace_back();
+    w.hulls.emplace_back();
+    w.active.push_back(0);
+  }
+  const double* r = body10;
+  w.bodies[slot] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
+  init_hull(w.hulls[slot], nv, local_xy);
+  pose_hull(w.bodies[slot], w.hulls[slot]);
+  w.active[slot] = 1;
+  return slot;
+}
+
+void oracle_world_get_active(void* h, uint8_t* out) {
+  World& w = *static_cast<World*>(h);
+  for (size_t i = 0; i < w.active.size(); ++i) out[i] = w.active[i];
+}
 
 /* cfg5 = (dt, baumgarte, slop, accel_x, accel_y). */
 void oracle_world_step(void* h, const double* cfg5, int32_t iterations, int32_t warm_start,

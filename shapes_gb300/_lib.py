@@ -143,6 +143,9 @@ SIGNATURES = [
     ("shapes_mlp_train", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, ctypes.POINTER(TrainConfig),
                                         _fp]),
     ("shapes_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_delete_body", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    ("shapes_batch_append_body", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.c_int32, _dp, _ip]),
+    ("shapes_batch_get_active", ctypes.c_int, [ctypes.c_void_p, _up]),
     ("shapes_batch_save", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     ("shapes_batch_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     ("shapes_batch_set_mlp", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -329,6 +332,29 @@ class Batch:
 
     def set_launch(self, target_bodies_per_group: int, threads: int) -> None:
         check(lib().shapes_batch_set_launch(self._h, target_bodies_per_group, threads), "shapes_batch_set_launch")
+
+    def delete_body(self, world: int, slot: int) -> None:
+        """World.delete: the slot becomes empty (its index stays)."""
+        check(lib().shapes_batch_delete_body(self._h, world, slot), "shapes_batch_delete_body")
+
+    def append_body(self, world: int, body: dict | list, local_xy) -> int:
+        """World.append: returns the slot (the last one freed, else a new one)."""
+        vals = [float(body[f]) for f in BODY_FIELDS] if isinstance(body, dict) else [float(x) for x in body]
+        b = np.ascontiguousarray(vals, dtype=np.float64)
+        xy = np.ascontiguousarray(local_xy, dtype=np.float64).reshape(-1)
+        slot = ctypes.c_int32()
+        check(lib().shapes_batch_append_body(self._h, world, _ptr(b, _dp), len(xy) // 2, _ptr(xy, _dp),
+                                             ctypes.byref(slot)), "shapes_batch_append_body")
+        nb, nv = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().shapes_batch_num_bodies(self._h, ctypes.byref(nb)), "num_bodies")
+        check(lib().shapes_batch_num_vertices(self._h, ctypes.byref(nv)), "num_vertices")
+        self.n_bodies, self.n_verts = nb.value, nv.value
+        return slot.value
+
+    def active(self) -> np.ndarray:
+        out = np.empty(self.n_bodies, dtype=np.uint8)
+        check(lib().shapes_batch_get_active(self._h, _ptr(out, _up)), "shapes_batch_get_active")
+        return out
 
     def save(self, path) -> None:
         """Checkpoint file of the bodies, topology and contact cache."""

@@ -53,8 +53,21 @@ struct LW {
   int32_t* color;           /* [nc] */
   int32_t* color_cnt;       /* [kMaxColors + 1] then scanned */
   int32_t* color_list;      /* [nc] contacts grouped by colour */
-  unsigned long long* ctl;  /* [8] ticket, timeout flag, uncoloured count, colours used, nc, c0 */
+  int32_t* seqflag;         /* [nc] 1 = left over by the colouring */
+  int32_t* seqoff;          /* [nc + 1] scanned seqflag */
+  int32_t* seq_list;        /* [nc] left-over contacts in contact order */
+  unsigned long long* ctl;  /* [8] ticket, timeout flag, round counter, colours used, nc, c0, round counters */
 };
+
+__device__ __forceinline__ int32_t ld_acquire_gpu(const int32_t* p) {
+  int32_t v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_gpu_add(int32_t* p, int32_t v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 constexpr int kMaxColors = 64;
 constexpr int kSeqColor = kMaxColors - 1; /* contacts left over by the colouring: updated one by one */
@@ -150,7 +163,7 @@ __global__ void k_lw_hit_list(LW w, unsigned long long* hits, unsigned long long
 __global__ void k_lw_gravity(Dev d, LW w, double ax, double ay, double dt) {
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < w.nb; b += gridDim.x * blockDim.x) {
     const int g = w.b0 + b;
-    if (!(0.0 == d.iml[g])) {
+    if (!(0.0 == d.iml[g]) && !(d.flags[g] & kFlagInactive)) {
       d.vx[g] = d.vx[g] + ax * dt;
       d.vy[g] = d.vy[g] + ay * dt;
     }
@@ -260,27 +273,29 @@ __global__ void k_lw_ordered(Dev d, LW w, int iterations, int warm_start) {
           want[s] = pass == 0 ? w.hrank[ref] : w.bh[body[s]] + (pass - 1) * w.bn[body[s]] + w.rank[ref];
         }
       }
+      /* acquire loads of the predecessors' counters (their velocity writes,
+       * released with the counter increment, are visible after the load
+       * that sees the wanted count); a short tight spin, then backing off */
       bool ok = true;
       for (int s = 0; s < 2 && ok; ++s) {
         if (body[s] < 0) continue;
-        volatile int32_t* cnt = w.done + body[s];
+        const int32_t* cnt = w.done + body[s];
         long long spins = 0;
-        while (*cnt != want[s]) {
+        while (ld_acquire_gpu(cnt) != want[s]) {
           if (++spins > kSpinLimit) {
             ok = false;
             break;
           }
-          __nanosleep(32);
+          if (spins > 64) __nanosleep(32);
         }
       }
       if (!ok) {
         atomicExch(&w.ctl[1], 1ull);
       } else {
-        __threadfence(); /* acquire: the predecessors' writes are visible */
         lw_solve_item(d, (uint32_t)(w.c0 + k) | (pass == 0 ? kWarmBit : 0u), L2Vel{&d});
-        __threadfence(); /* release: this update's writes before the counters move */
+        /* release: this update's velocity writes before the counters move */
         for (int s = 0; s < 2; ++s)
-          if (body[s] >= 0) atomicAdd(&w.done[body[s]], 1);
+          if (body[s] >= 0) red_release_gpu_add(w.done + body[s], 1);
       }
     }
     __syncwarp();
@@ -296,8 +311,20 @@ __device__ __forceinline__ uint32_t lw_prio(int k) {
   return x;
 }
 
-__global__ void k_lw_color_round(Dev d, LW w) {
+/* Round r of the colouring counts the contacts it leaves uncoloured in
+ * ctl[slot(r)], slots rotating over ctl[2], ctl[6], ctl[7]: round r reads
+ * slot(r - 1) (a round after one that left none returns at once, so the host
+ * can launch a generous number of rounds), counts into slot(r), and clears
+ * slot(r + 1), which no block of round r reads. */
+__device__ __forceinline__ unsigned long long* lw_round_slot(const LW& w, int round) {
+  const int m = round % 3;
+  return w.ctl + (m == 0 ? 2 : (m == 1 ? 6 : 7));
+}
+
+__global__ void k_lw_color_round(Dev d, LW w, int round) {
   lw_range(w);
+  if (round > 0 && *lw_round_slot(w, round - 1) == 0) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *lw_round_slot(w, round + 1) = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < w.nc; k += gridDim.x * blockDim.x) {
     if (w.color[k] >= 0) continue;
     const uint64_t mine = ((uint64_t)lw_prio(k) << 32) | (uint32_t)k;
@@ -323,7 +350,7 @@ __global__ void k_lw_color_round(Dev d, LW w) {
       }
     }
     if (!top) {
-      atomicAdd(&w.ctl[2], 1ull);
+      atomicAdd(lw_round_slot(w, round), 1ull);
       continue;
     }
     int col = __ffsll((long long)~used) - 1;
@@ -339,6 +366,7 @@ __global__ void k_lw_color_count(LW w) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < w.nc; k += gridDim.x * blockDim.x) {
     if (w.color[k] < 0) w.color[k] = kSeqColor;
     atomicAdd(&w.color_cnt[w.color[k]], 1);
+    w.seqflag[k] = w.color[k] == kSeqColor ? 1 : 0;
   }
 }
 
@@ -369,14 +397,22 @@ struct GlobalVel {
   }
 };
 
+/* The left-over contacts, in contact order (ordered compaction of seqflag). */
+__global__ void k_lw_seq_list(LW w) {
+  lw_range(w);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < w.nc; k += gridDim.x * blockDim.x)
+    if (w.seqflag[k]) w.seq_list[w.seqoff[k]] = k;
+}
+
 /* One colour of one pass: contacts [lo, hi) of the colour list.  The
- * sequential colour runs on one thread in contact order. */
+ * left-over contacts run on one thread in contact order. */
 __global__ void k_lw_color_seq(Dev d, LW w, int warm) {
   if (d.counters[kCntOverflow]) return;
   lw_range(w);
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  for (int k = 0; k < w.nc; ++k) {
-    if (w.color[k] != kSeqColor) continue;
+  const int n = w.seqoff[w.nc];
+  for (int t = 0; t < n; ++t) {
+    const int k = w.seq_list[t];
     const int c = w.c0 + k;
     if (warm && !(d.c_hit[c] & kInfoHit)) continue;
     lw_solve_item(d, (uint32_t)c | (warm ? kWarmBit : 0u), GlobalVel{&d});

@@ -175,6 +175,9 @@ struct shapes_batch {
   int32_t* lw_color = nullptr;
   int32_t* lw_color_cnt = nullptr;
   int32_t* lw_color_list = nullptr;
+  int32_t* lw_seqflag = nullptr;
+  int32_t* lw_seqoff = nullptr;
+  int32_t* lw_seq_list = nullptr;
   unsigned long long* lw_ctl = nullptr; /* 8 per large world */
   int32_t worlds_per_group_override = 0;
   int32_t target_group_bodies = 0;
@@ -186,6 +189,12 @@ struct shapes_batch {
   double* world_residual = nullptr;
   double* world_depth = nullptr;
   bool residual_valid = false;
+  /* world mutation: filled slots (device copy allocated on the first delete)
+   * and each world's stack of empty slots (world-local slot ids) */
+  uint8_t* active = nullptr;
+  std::vector<uint8_t> h_active;
+  std::vector<int32_t> h_vert_off;
+  std::vector<std::vector<int32_t>> h_empties;
   /* learned warm start */
   const shapes_mlp* mlp_model = nullptr;
   uint8_t* learned_mask = nullptr; /* [W] */
@@ -400,6 +409,7 @@ struct shapes_batch {
     d.counters = counters;
     d.world_residual = world_residual;
     d.world_depth = world_depth;
+    d.active = active;
     return d;
   }
 
@@ -442,8 +452,9 @@ struct shapes_batch {
     dfree(snap_key); dfree(snap_lam);
     free_row_buffers();
     dfree(lw_refs); dfree(lw_rank); dfree(lw_hrank); dfree(lw_hitflag); dfree(lw_hitoff); dfree(lw_hit_idx);
-    dfree(lw_color); dfree(lw_color_list);
+    dfree(lw_color); dfree(lw_color_list); dfree(lw_seqflag); dfree(lw_seqoff); dfree(lw_seq_list);
     lw_refs = lw_rank = lw_hrank = lw_hitflag = lw_hitoff = lw_hit_idx = lw_color = lw_color_list = nullptr;
+    lw_seqflag = lw_seqoff = lw_seq_list = nullptr;
     pair_a = pair_b = slot_cnt = slot_off = slot_feat = nullptr;
     slot_val = nullptr;
     c_key[0] = c_key[1] = nullptr;
@@ -516,6 +527,9 @@ struct shapes_batch {
       lw_hit_idx = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
       lw_color = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
       lw_color_list = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_seqflag = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_seqoff = dalloc<int32_t>((size_t)contact_cap + 1, "cudaMalloc large world");
+      lw_seq_list = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
     }
     snap_cap = contact_cap;
     snap_key = dalloc<uint64_t>(snap_cap, "cudaMalloc snapshot");
@@ -605,6 +619,9 @@ struct shapes_batch {
   /* Worlds with at least large_world_bodies bodies are solved by the
    * large-world paths; their per-body scratch is sized for the largest. */
   void setup_large_worlds() {
+    dfree(lw_bcnt); dfree(lw_bstart); dfree(lw_bh); dfree(lw_bn); dfree(lw_done); dfree(lw_color_cnt); dfree(lw_ctl);
+    lw_bcnt = lw_bstart = lw_bh = lw_bn = lw_done = lw_color_cnt = nullptr;
+    lw_ctl = nullptr;
     large_worlds.clear();
     lw_nb_max = 0;
     for (int w = 0; w < W; ++w) {
@@ -643,6 +660,9 @@ struct shapes_batch {
     w.color = lw_color;
     w.color_cnt = lw_color_cnt;
     w.color_list = lw_color_list;
+    w.seqflag = lw_seqflag;
+    w.seqoff = lw_seqoff;
+    w.seq_list = lw_seq_list;
     w.ctl = lw_ctl + 8 * k;
     return w;
   }
@@ -670,10 +690,15 @@ struct shapes_batch {
         return;
       }
       shapes::k_lw_color_init<<<grid_for(cap, 256), 256, 0, stream>>>(w);
-      for (int r = 0; r < 24; ++r) shapes::k_lw_color_round<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+      /* Jones-Plassmann rounds until every contact has a colour (rounds after
+       * that return at once; whatever is left after the last goes to the
+       * sequential colour) */
+      for (int r = 0; r < 128; ++r) shapes::k_lw_color_round<<<grid_for(cap, 256), 256, 0, stream>>>(d, w, r);
       shapes::k_lw_color_count<<<grid_for(cap, 256), 256, 0, stream>>>(w);
       scan_raw(w.color_cnt, shapes::kMaxColors, nullptr, w.color_cnt);
       shapes::k_lw_color_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+      scan_raw(w.seqflag, cap, w.ctl + 4, w.seqoff);
+      shapes::k_lw_seq_list<<<grid_for(cap, 256), 256, 0, stream>>>(w);
       for (int pass = cfg.warm_start ? 0 : 1; pass <= cfg.iterations; ++pass) {
         for (int col = 0; col < shapes::kSeqColor; ++col)
           shapes::k_lw_color_pass<<<grid_for(cap / 8 + 1, 128), 128, 0, stream>>>(d, w, col, pass == 0);
@@ -930,6 +955,112 @@ struct shapes_batch {
     }
   }
 
+  /* (Re)builds everything sized by the bodies and vertices from host arrays:
+   * world offsets [W+1], the ten body arrays, vertex offsets [N+1] and local
+   * vertices [2V].  Used by creation and by appends that change the
+   * topology; settings, the stream, the network and the judge stay.  The
+   * contact cache comes back empty (the caller restores it). */
+  void init_topology(const int32_t* world_body_offsets, double* const bp[10], const int32_t* vert_offsets,
+                     const double* local_verts_xy) {
+    if (stream) ck(cudaStreamSynchronize(stream), "sync");
+    invalidate_graphs();
+    free_step_buffers();
+    dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly); dfree(emin); dfree(emax);
+    for (int k = 0; k < 10; ++k) {
+      dfree(body[k]);
+      dfree(body_stage[k]);
+    }
+    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
+    dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(world_items);
+    for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
+    dfree(active);
+    active = nullptr;
+    const int32_t n_worlds = W;
+    N = world_body_offsets[n_worlds];
+    V = vert_offsets[N];
+    h_world_body_off.assign(world_body_offsets, world_body_offsets + n_worlds + 1);
+    h_vert_off.assign(vert_offsets, vert_offsets + N + 1);
+    h_active.assign(N, 1);
+    h_body_world.resize(N);
+    for (int w = 0; w < n_worlds; ++w)
+      for (int32_t b = world_body_offsets[w]; b < world_body_offsets[w + 1]; ++b) h_body_world[b] = w;
+    world_body_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+    body_world = dalloc<int32_t>(N, "cudaMalloc");
+    vert_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
+    lx = dalloc<double>(V, "cudaMalloc");
+    ly = dalloc<double>(V, "cudaMalloc");
+    emin = dalloc<int32_t>(V, "cudaMalloc");
+    emax = dalloc<int32_t>(V, "cudaMalloc");
+    for (int k = 0; k < 10; ++k) body[k] = dalloc<double>(N, "cudaMalloc bodies");
+    for (int k = 0; k < 10; ++k) body_stage[k] = dalloc<double>(N, "cudaMalloc bodies");
+    wx = dalloc<double>(V, "cudaMalloc");
+    wy = dalloc<double>(V, "cudaMalloc");
+    nx = dalloc<double>(V, "cudaMalloc");
+    ny = dalloc<double>(V, "cudaMalloc");
+    box = dalloc<double>(4 * (size_t)N, "cudaMalloc");
+    boxk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc");
+    flags = dalloc<uint8_t>(N, "cudaMalloc");
+    row_cnt = dalloc<int32_t>(N, "cudaMalloc");
+    row_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
+    world_pair_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+    if (!cwo[0])
+      for (int k = 0; k < 2; ++k) cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
+    last = dalloc<int32_t>(N, "cudaMalloc");
+    world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
+    if (!counters) counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
+    if (!np_cls) np_cls = dalloc<int32_t>(2 * shapes::kNpClasses + 1, "cudaMalloc");
+    if (!world_residual) world_residual = dalloc<double>(n_worlds, "cudaMalloc");
+    if (!world_depth) world_depth = dalloc<double>(n_worlds, "cudaMalloc");
+    for (int k = 0; k < 6; ++k) snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
+    if (!snap_cwo) snap_cwo = dalloc<int32_t>(n_worlds + 1, "cudaMalloc snapshot");
+    ck(cudaMemcpy(world_body_off, world_body_offsets, sizeof(int32_t) * (n_worlds + 1), cudaMemcpyHostToDevice),
+       "upload");
+    ck(cudaMemcpy(body_world, h_body_world.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
+    ck(cudaMemcpy(vert_off, vert_offsets, sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "upload");
+    std::vector<double> tmp(V);
+    for (int32_t v = 0; v < V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v];
+    ck(cudaMemcpy(lx, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice), "upload");
+    for (int32_t v = 0; v < V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v + 1];
+    ck(cudaMemcpy(ly, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice), "upload");
+    for (int k = 0; k < 10; ++k) ck(cudaMemcpy(body[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice), "upload bodies");
+    /* empty cache: every world offset 0 */
+    for (int k = 0; k < 2; ++k) ck(cudaMemset(cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
+    cache_buf = 0;
+    results_buf = 0;
+    have_results = false;
+    residual_valid = false;
+    setup_grid();
+    setup_large_worlds();
+    contact_cap = 0;
+    item_cap = 0;
+    const int32_t pcap = (int32_t)std::min<int64_t>(std::max<int64_t>(1024, 8LL * N), INT32_MAX / 4);
+    alloc_step_buffers(pcap, 2 * pcap, 8);
+    make_groups(grouped_iterations > 0 ? grouped_iterations : 2);
+    Dev d = view(0);
+    shapes::k_init_extents<<<grid_for(V, 128), 128, 0, stream>>>(d);
+    pose(0, 0.0);
+    ck(cudaGetLastError(), "launch");
+    ck(cudaStreamSynchronize(stream), "create");
+  }
+
+  /* Uploads the filled-slot flags (allocated on first use; the step graphs
+   * hold the array, so its first allocation re-captures them) and re-poses,
+   * which recomputes every body's broadphase flags. */
+  void upload_active() {
+    bool all = true;
+    for (uint8_t a : h_active) all = all && a;
+    if (all && !active) return;
+    if (!active) {
+      if (stream) ck(cudaStreamSynchronize(stream), "sync");
+      active = dalloc<uint8_t>(N, "cudaMalloc");
+      invalidate_graphs();
+    }
+    ck(cudaMemcpyAsync(active, h_active.data(), N, cudaMemcpyHostToDevice, stream), "upload");
+    pose(0, 0.0);
+    ck(cudaStreamSynchronize(stream), "upload");
+    have_results = false;
+  }
+
   ~shapes_batch() {
     if (stream) cudaStreamSynchronize(stream);
     drop_graphs();
@@ -953,6 +1084,7 @@ struct shapes_batch {
     dfree(world_residual);
     dfree(world_depth);
     dfree(learned_mask); dfree(judge_res); dfree(judge_depth);
+    dfree(active);
     dfree(ds_feat); dfree(ds_tgt); dfree(ds_count); dfree(snap_ds_count); dfree(snap_mask);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(snap_cwo);
@@ -1056,62 +1188,8 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
       ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
       h->stream = h->own_stream;
       h->W = n_worlds;
-      h->N = N;
-      h->V = vert_offsets[N];
-      h->h_world_body_off.assign(world_body_offsets, world_body_offsets + n_worlds + 1);
-      h->h_body_world.resize(N);
-      for (int w = 0; w < n_worlds; ++w)
-        for (int32_t b = world_body_offsets[w]; b < world_body_offsets[w + 1]; ++b) h->h_body_world[b] = w;
-      h->world_body_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
-      h->body_world = dalloc<int32_t>(N, "cudaMalloc");
-      h->vert_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
-      h->lx = dalloc<double>(h->V, "cudaMalloc");
-      h->ly = dalloc<double>(h->V, "cudaMalloc");
-      h->emin = dalloc<int32_t>(h->V, "cudaMalloc");
-      h->emax = dalloc<int32_t>(h->V, "cudaMalloc");
-      for (int k = 0; k < 10; ++k) h->body[k] = dalloc<double>(N, "cudaMalloc bodies");
-      for (int k = 0; k < 10; ++k) h->body_stage[k] = dalloc<double>(N, "cudaMalloc bodies");
-      h->wx = dalloc<double>(h->V, "cudaMalloc");
-      h->wy = dalloc<double>(h->V, "cudaMalloc");
-      h->nx = dalloc<double>(h->V, "cudaMalloc");
-      h->ny = dalloc<double>(h->V, "cudaMalloc");
-      h->box = dalloc<double>(4 * (size_t)N, "cudaMalloc");
-      h->boxk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc");
-      h->flags = dalloc<uint8_t>(N, "cudaMalloc");
-      h->row_cnt = dalloc<int32_t>(N, "cudaMalloc");
-      h->row_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
-      h->world_pair_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
-      for (int k = 0; k < 2; ++k) h->cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
-      h->last = dalloc<int32_t>(N, "cudaMalloc");
-      h->world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
-      h->counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
-      h->np_cls = dalloc<int32_t>(2 * shapes::kNpClasses + 1, "cudaMalloc");
-      h->world_residual = dalloc<double>(n_worlds, "cudaMalloc");
-      h->world_depth = dalloc<double>(n_worlds, "cudaMalloc");
-      for (int k = 0; k < 6; ++k) h->snap_body[k] = dalloc<double>(N, "cudaMalloc snapshot");
-      h->snap_cwo = dalloc<int32_t>(n_worlds + 1, "cudaMalloc snapshot");
-      ck(cudaMemcpy(h->world_body_off, world_body_offsets, sizeof(int32_t) * (n_worlds + 1), cudaMemcpyHostToDevice), "upload");
-      ck(cudaMemcpy(h->body_world, h->h_body_world.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
-      ck(cudaMemcpy(h->vert_off, vert_offsets, sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "upload");
-      std::vector<double> tmp(h->V);
-      for (int32_t v = 0; v < h->V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v];
-      ck(cudaMemcpy(h->lx, tmp.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice), "upload");
-      for (int32_t v = 0; v < h->V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v + 1];
-      ck(cudaMemcpy(h->ly, tmp.data(), sizeof(double) * h->V, cudaMemcpyHostToDevice), "upload");
-      for (int k = 0; k < 10; ++k)
-        ck(cudaMemcpy(h->body[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice), "upload bodies");
-      /* empty cache: every world offset 0 */
-      for (int k = 0; k < 2; ++k) ck(cudaMemset(h->cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
-      h->setup_grid();
-      h->setup_large_worlds();
-      const int32_t pcap = (int32_t)std::min<int64_t>(std::max<int64_t>(1024, 8LL * N), INT32_MAX / 4);
-      h->alloc_step_buffers(pcap, 2 * pcap, 8);
-      h->make_groups(2);
-      Dev d = h->view(0);
-      shapes::k_init_extents<<<grid_for(h->V, 128), 128, 0, h->stream>>>(d);
-      h->pose(0, 0.0);
-      ck(cudaGetLastError(), "launch");
-      ck(cudaStreamSynchronize(h->stream), "create");
+      h->h_empties.assign(n_worlds, {});
+      h->init_topology(world_body_offsets, bp, vert_offsets, local_verts_xy);
     } catch (...) {
       delete h;
       throw;
@@ -1513,6 +1591,129 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
   });
 }
 
+/* ---- world mutation (World.append / World.delete) ------------------------ */
+
+int shapes_batch_delete_body(shapes_batch* b, int32_t world, int32_t slot) {
+  if (!b || world < 0 || world >= b->W) return SHAPES_E_INVALID_ARG;
+  const int32_t n = b->h_world_body_off[world + 1] - b->h_world_body_off[world];
+  if (slot < 0 || slot >= n) return SHAPES_E_INVALID_ARG;
+  const int32_t g = b->h_world_body_off[world] + slot;
+  if (!b->h_active[g]) return SHAPES_E_INVALID_ARG; /* safeDelete: the slot must be filled */
+  return guarded([&]() -> int {
+    b->h_active[g] = 0;
+    b->h_empties[world].push_back(slot);
+    b->upload_active();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body10, int32_t n_verts,
+                             const double* local_verts_xy, int32_t* slot_out) {
+  if (!b || !body10 || !local_verts_xy || !slot_out || world < 0 || world >= b->W) return SHAPES_E_INVALID_ARG;
+  for (int k = 0; k < 10; ++k)
+    if (!std::isfinite(body10[k])) return SHAPES_E_NAN;
+  const int hrc = check_hull(n_verts, local_verts_xy);
+  if (hrc != SHAPES_OK) return hrc;
+  return guarded([&]() -> int {
+    const int32_t W = b->W, N = b->N;
+    const int32_t w0 = b->h_world_body_off[world];
+    auto& empties = b->h_empties[world];
+    const bool reuse = !empties.empty();
+    const int32_t slot = reuse ? empties.back() : b->h_world_body_off[world + 1] - w0;
+    if (slot >= (1 << 20)) return SHAPES_E_CAPACITY;
+    if (reuse) {
+      const int32_t g = w0 + slot;
+      const int32_t v0 = b->h_vert_off[g];
+      if (b->h_vert_off[g + 1] - v0 == n_verts) { /* same vertex count: in place */
+        ck(cudaStreamSynchronize(b->stream), "sync");
+        for (int k = 0; k < 10; ++k)
+          ck(cudaMemcpyAsync(b->body[k] + g, body10 + k, sizeof(double), cudaMemcpyHostToDevice, b->stream), "upload");
+        std::vector<double> xs(n_verts), ys(n_verts);
+        for (int32_t v = 0; v < n_verts; ++v) {
+          xs[v] = local_verts_xy[2 * v];
+          ys[v] = local_verts_xy[2 * v + 1];
+        }
+        ck(cudaMemcpyAsync(b->lx + v0, xs.data(), sizeof(double) * n_verts, cudaMemcpyHostToDevice, b->stream), "upload");
+        ck(cudaMemcpyAsync(b->ly + v0, ys.data(), sizeof(double) * n_verts, cudaMemcpyHostToDevice, b->stream), "upload");
+        Dev d = b->view(0);
+        shapes::k_init_extents<<<grid_for(b->V, 128), 128, 0, b->stream>>>(d);
+        ck(cudaGetLastError(), "launch");
+        empties.pop_back();
+        b->h_active[g] = 1;
+        b->upload_active();
+        if (!b->active) { /* every slot filled again: the in-place shape still needs its pose */
+          b->pose(0, 0.0);
+          ck(cudaStreamSynchronize(b->stream), "upload");
+        }
+        *slot_out = slot;
+        return SHAPES_OK;
+      }
+    }
+    /* the topology changes: rebuild from the host copies, keeping state and cache */
+    std::vector<double> body(10 * (size_t)N);
+    shapes_bodies cur{};
+    double* bp[10];
+    for (int k = 0; k < 10; ++k) bp[k] = body.data() + (size_t)k * N;
+    cur.vel_x = bp[0]; cur.vel_y = bp[1]; cur.rot_vel = bp[2]; cur.pos_x = bp[3]; cur.pos_y = bp[4];
+    cur.rot = bp[5]; cur.inv_mass_lin = bp[6]; cur.inv_mass_rot = bp[7]; cur.mu = bp[8]; cur.bounce = bp[9];
+    int rc = shapes_batch_get_bodies(b, &cur);
+    if (rc != SHAPES_OK) return rc;
+    int64_t nc = 0;
+    rc = shapes_batch_num_cache(b, &nc);
+    if (rc != SHAPES_OK) return rc;
+    std::vector<int32_t> keys(4 * (size_t)std::max<int64_t>(nc, 1)), wc(W);
+    std::vector<double> lam(2 * (size_t)std::max<int64_t>(nc, 1));
+    rc = shapes_batch_get_cache(b, keys.data(), lam.data(), nc, wc.data());
+    if (rc != SHAPES_OK) return rc;
+    const int64_t V = b->V;
+    std::vector<double> lxh(V), lyh(V);
+    ck(cudaMemcpyAsync(lxh.data(), b->lx, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaMemcpyAsync(lyh.data(), b->ly, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
+    const int32_t g = w0 + slot; /* replaced or inserted body */
+    const int32_t N2 = reuse ? N : N + 1;
+    std::vector<int32_t> off(W + 1);
+    for (int w = 0; w <= W; ++w) off[w] = b->h_world_body_off[w] + ((!reuse && w > world) ? 1 : 0);
+    std::vector<double> body2(10 * (size_t)N2);
+    std::vector<uint8_t> act2(N2);
+    std::vector<int32_t> vo2(N2 + 1, 0);
+    std::vector<double> xy2;
+    xy2.reserve(2 * (size_t)(V + n_verts));
+    for (int32_t i = 0; i < N2; ++i) {
+      const bool is_new = i == g;
+      const int32_t src = (!reuse && i > g) ? i - 1 : i; /* old index */
+      for (int k = 0; k < 10; ++k) body2[(size_t)k * N2 + i] = is_new ? body10[k] : body[(size_t)k * N + src];
+      act2[i] = is_new ? 1 : b->h_active[src];
+      if (is_new) {
+        for (int32_t v = 0; v < 2 * n_verts; ++v) xy2.push_back(local_verts_xy[v]);
+        vo2[i + 1] = vo2[i] + n_verts;
+      } else {
+        for (int32_t v = b->h_vert_off[src]; v < b->h_vert_off[src + 1]; ++v) {
+          xy2.push_back(lxh[v]);
+          xy2.push_back(lyh[v]);
+        }
+        vo2[i + 1] = vo2[i] + (b->h_vert_off[src + 1] - b->h_vert_off[src]);
+      }
+    }
+    double* bp2[10];
+    for (int k = 0; k < 10; ++k) bp2[k] = body2.data() + (size_t)k * N2;
+    b->init_topology(off.data(), bp2, vo2.data(), xy2.data());
+    if (reuse) empties.pop_back();
+    b->h_active = act2;
+    b->upload_active();
+    rc = shapes_batch_set_cache(b, wc.data(), keys.data(), lam.data());
+    if (rc != SHAPES_OK) return rc;
+    *slot_out = slot;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_active(shapes_batch* b, uint8_t* out) {
+  if (!b || !out) return SHAPES_E_INVALID_ARG;
+  std::copy(b->h_active.begin(), b->h_active.end(), out);
+  return SHAPES_OK;
+}
+
 /* ---- checkpoint file (EngineState: World + EngineCache) ------------------ */
 
 }  // extern "C"
@@ -1615,6 +1816,9 @@ int shapes_batch_save(shapes_batch* b, const char* path) {
   w.put(wc.data(), (size_t)W);
   w.put(keys.data(), 4 * (size_t)nc);
   w.put(lam.data(), 2 * (size_t)nc);
+  w.put(b->h_active.data(), (size_t)N);
+  for (int32_t k = 0; k < W; ++k) w.put1((int32_t)b->h_empties[k].size());
+  for (int32_t k = 0; k < W; ++k) w.put(b->h_empties[k].data(), b->h_empties[k].size());
   w.put1(fnv1a(w.buf.data(), w.buf.size()));
   const std::string tmp = std::string(path) + ".tmp";
   FILE* f = std::fopen(tmp.c_str(), "wb");
@@ -1651,7 +1855,7 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
     g_last_error = std::string("checkpoint ") + path + ": " + why;
     return SHAPES_E_INVALID_ARG;
   };
-  if (buf.size() < 48 + sizeof(uint64_t)) return bad("too short");
+  if (buf.size() < 40 + sizeof(uint64_t)) return bad("too short"); /* 40-byte header + hash */
   uint64_t sum = 0;
   std::memcpy(&sum, buf.data() + buf.size() - sizeof(uint64_t), sizeof sum);
   if (fnv1a(buf.data(), buf.size() - sizeof(uint64_t)) != sum) return bad("checksum mismatch");
@@ -1665,9 +1869,9 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
   const int64_t V = r.get1<int64_t>(), nc = r.get1<int64_t>();
   if (!r.ok || W < 1 || N < 1 || V < 3 || nc < 0 || V > (int64_t)INT32_MAX || nc > (int64_t)INT32_MAX)
     return bad("bad sizes");
-  const uint64_t need = 48ull + 4ull * (W + 1) + 4ull * (N + 1) + 16ull * V + 80ull * N + 4ull * W + 16ull * nc +
-                        16ull * nc + 8ull;
-  if (buf.size() != need) return bad("size does not match the header");
+  const uint64_t need = 40ull + 4ull * (W + 1) + 4ull * (N + 1) + 16ull * V + 80ull * N + 4ull * W + 16ull * nc +
+                        16ull * nc + 1ull * N + 4ull * W + 8ull; /* + the empty-slot stacks */
+  if (buf.size() < need) return bad("size does not match the header");
   std::vector<int32_t> off(W + 1), vo(N + 1), wc(W), keys(4 * (size_t)std::max<int64_t>(nc, 1));
   std::vector<double> xy(2 * (size_t)V), body(10 * (size_t)N), lam(2 * (size_t)std::max<int64_t>(nc, 1));
   r.get(off.data(), off.size());
@@ -1677,7 +1881,22 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
   r.get(wc.data(), wc.size());
   r.get(keys.data(), 4 * (size_t)nc);
   r.get(lam.data(), 2 * (size_t)nc);
-  if (!r.ok) return bad("truncated");
+  std::vector<uint8_t> act(N);
+  r.get(act.data(), act.size());
+  std::vector<int32_t> elen(W);
+  r.get(elen.data(), elen.size());
+  std::vector<std::vector<int32_t>> empties(W);
+  uint64_t total_empty = 0;
+  for (int32_t k = 0; k < W && r.ok; ++k) {
+    const int32_t nw = off[k + 1] - off[k];
+    if (elen[k] < 0 || elen[k] > nw) return bad("bad empty-slot stack");
+    total_empty += (uint64_t)elen[k];
+    empties[k].resize(elen[k]);
+    r.get(empties[k].data(), empties[k].size());
+    for (int32_t e : empties[k])
+      if (e < 0 || e >= nw || act[off[k] + e]) return bad("bad empty-slot stack");
+  }
+  if (!r.ok || buf.size() != need + 4ull * total_empty) return bad("size does not match the header");
   shapes_bodies in{};
   double* bp[10];
   for (int k = 0; k < 10; ++k) bp[k] = body.data() + (size_t)k * N;
@@ -1687,6 +1906,13 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
   int rc = shapes_batch_create(W, off.data(), &in, vo.data(), xy.data(), nullptr, &h);
   if (rc != SHAPES_OK) return rc;
   rc = shapes_batch_set_cache(h, wc.data(), keys.data(), lam.data());
+  if (rc == SHAPES_OK)
+    rc = guarded([&]() -> int {
+      for (int32_t i = 0; i < N; ++i) h->h_active[i] = act[i] ? 1 : 0;
+      h->h_empties = empties;
+      h->upload_active();
+      return SHAPES_OK;
+    });
   if (rc != SHAPES_OK) {
     shapes_batch_destroy(h);
     return rc;

@@ -23,6 +23,7 @@ constexpr int kMaxVerts = 64;
 constexpr uint32_t kWarmBit = 0x80000000u;
 constexpr uint8_t kFlagStatic = 1;
 constexpr uint8_t kFlagBoxNaN = 2;
+constexpr uint8_t kFlagInactive = 4; /* empty slot (World.delete): no pairs, no motion */
 /* per-contact info byte */
 constexpr uint8_t kInfoHit = 1;
 constexpr uint8_t kInfoDynA = 2;
@@ -136,6 +137,7 @@ struct Dev {
   int32_t collect_all;         /* 1 = rows for every world's misses (sample collection) */
   const double* judge_res;     /* [W] residual limit of the judge */
   const double* judge_depth;   /* [W] depth limit of the judge */
+  const uint8_t* active;       /* [N] 0 = empty slot (World.delete); null when every slot is filled */
 };
 
 enum {
@@ -223,6 +225,10 @@ __global__ void k_init_extents(Dev d) {
  * One thread per body. */
 __global__ void k_integrate_pose(Dev d, double dt, int advance) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (d.active && !d.active[g]) { /* empty slot: left as it was, out of the broadphase */
+      d.flags[g] = kFlagInactive;
+      continue;
+    }
     double px = d.px[g], py = d.py[g], th = d.th[g];
     if (advance) {
       const double vx = d.vx[g], vy = d.vy[g], w = d.w[g];
@@ -319,6 +325,7 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
 __device__ __forceinline__ bool pair_overlaps(const Dev& d, int gi, int gj, uint8_t fi,
                                               const uint64_t ki[4]) {
   const uint8_t fj = d.flags[gj];
+  if ((fi | fj) & kFlagInactive) return false;
   if ((fi & fj & kFlagStatic)) return false;
   if ((fi | fj) & kFlagBoxNaN) {
     const double* a = d.box + 4 * gi;
@@ -1167,7 +1174,7 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
       const int wld = d.group_worlds[o0 + k];
       const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
       for (int g = b0 + lane; g < b1; g += 32) {
-        if (external && !(0.0 == d.iml[g])) {
+        if (external && !(0.0 == d.iml[g]) && !(d.flags[g] & kFlagInactive)) {
           d.vx[g] = d.vx[g] + ax * dt;
           d.vy[g] = d.vy[g] + ay * dt;
         }
@@ -1181,6 +1188,10 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
   /* 2b. lane l scans world l */
   int my_depth = 0, my_items = 0, my_hits = 0;
   size_t my_region = 0;
+  int pass = iterations + 1, c = 0, c0 = 0, c1 = 0;
+  uint8_t info_n = 0;
+  int ga_n = 0, gb_n = 0;
+  int32_t* last = d.last;
   if (lane < nw) {
     const int wld = d.group_worlds[o0 + lane];
     int base = 0;
@@ -1189,16 +1200,12 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
       base += d.world_body_off[w2 + 1] - d.world_body_off[w2];
     }
     const int b0 = d.world_body_off[wld];
-    int32_t* last = smem_last ? s_last + base - b0 : d.last;
-    const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+    last = smem_last ? s_last + base - b0 : d.last;
+    c0 = d.world_contact_off[wld];
+    c1 = d.world_contact_off[wld + 1];
     my_region = (size_t)stride * c0;
-    /* The only loop-carried dependency is through last[]; the next contact's
-     * info and bodies are loaded one iteration ahead so their latency hides
-     * behind the current update's shared-memory work. */
-    int pass = warm_start ? 0 : 1;
-    int c = c0;
-    uint8_t info_n = 0;
-    int ga_n = 0, gb_n = 0;
+    pass = warm_start ? 0 : 1;
+    c = c0;
     if (c0 < c1) {
       info_n = d.c_hit[c0];
       ga_n = d.c_ga[c0];
@@ -1206,7 +1213,14 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
     } else {
       pass = iterations + 1;
     }
-    while (pass <= iterations) {
+  }
+  /* Sequential scan of this lane's world while pass <= pass_end.  The only
+   * loop-carried dependency is through last[]; the next contact's info and
+   * bodies are loaded one iteration ahead so their latency hides behind the
+   * current update's shared-memory work. */
+  auto scan_until = [&](int pass_end) {
+    if (lane >= nw) return;
+    while (pass <= pass_end) {
       const uint8_t info = info_n;
       const int ga = ga_n, gb = gb_n, cur_c = c, cur_pass = pass;
       if (++c == c1) {
@@ -1231,7 +1245,8 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
       my_depth = lvl > my_depth ? lvl : my_depth;
       my_hits += cur_pass == 0;
     }
-  }
+  };
+  scan_until(iterations);
   if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 1] = clock64();
   /* 3. the group's updates counting-sorted by level into a region of gdesc /
    *    ghist taken from a bump allocator, as packed descriptors, so that a

@@ -209,3 +209,31 @@ def test_warm_start_off_differs_and_cache_roundtrip(O):
     d = O.world_from_scene(sc)
     d.step(*args, warm_start=False, nsteps=140)
     assert not np.array_equal(a.bodies()["vel_y"], d.bodies()["vel_y"])
+
+
+def test_world_mutation_slots(O):
+    """World.delete / World.append over EmptiesVector: the last slot freed is
+    the next one filled; with none free the world grows; deleted slots take
+    no part in the step and keep their state."""
+    sc = scenes.stacks_make_scene((3, 4))
+    w = O.world_from_scene(sc)
+    cfg = sc["config"]
+    step = lambda n: w.step(cfg["dt"], cfg["baumgarte"], cfg["slop"], cfg["accel"], cfg["iterations"], nsteps=n)
+    step(10)
+    n0 = w.n
+    assert w.delete(5) == 0 and w.delete(7) == 0
+    assert w.delete(5) == -1  # already empty
+    frozen = w.bodies()
+    step(10)
+    after = w.bodies()
+    for f in ("pos_x", "pos_y", "vel_x", "vel_y"):
+        assert after[f][5] == frozen[f][5] and after[f][7] == frozen[f][7]
+    pairs = w.pairs()
+    assert not np.isin(pairs, [5, 7]).any()
+    box = scenes.rectangle_vertices(0.2, 0.2)
+    body = [0, 0, 0, 0.0, 3.0, 0.0, 0.5, 1.0, 0.2, 0.0]
+    assert w.append(body, box) == 7   # last freed first
+    assert w.append(body, box) == 5
+    assert w.append(body, box) == n0  # none free: a new slot
+    assert list(w.active()) == [1] * (n0 + 1)
+    step(5)
