@@ -72,8 +72,11 @@ WORKLOADS = {
     "container": "1 world: a 1024-wide static U container holding 262,141 mixed convex polygons (3-8 vertices, "
                  "radius U[0.3,1.0]) dropped from a grid, dt 1/120, 4 sweeps; order-preserving large-world "
                  "solver (--coloured: graph-coloured sweep)",
+    "balls": "2048 worlds x 128 bodies in a static U container, half circles (radius U[0.25,0.5], bounce "
+             "U[0,0.5]) and half 3-8 vertex polygons, dt 1/60, 8 sweeps, warm start, gravity (0,-9.8)",
 }
-PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4, "mixed": 8, "contacts": 0, "container": 4}
+PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4, "mixed": 8, "contacts": 0, "container": 4,
+                    "balls": 8}
 
 
 def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
@@ -89,6 +92,8 @@ def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
         return scenes.polygon_field(seed=1 + seed_offset, n=worlds or 65536)
     if workload == "container":
         return scenes.container_world(seed=4 + seed_offset, n=worlds or 262144)
+    if workload == "balls":
+        return scenes.batched_balls(seed=5 + seed_offset, n_worlds=worlds or 2048, n_bodies=128)
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -295,9 +300,15 @@ def run_reference(args, rank, world):
     return 0
 
 
+INCREMENTAL_PAIRS = True  # --no-incremental turns the fat-box pair lists off
+
+
 def new_batch(_lib, scene, stream, tuned=None):
-    b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
+    b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"],
+                   scene.get("shape_kind"))
     b.set_stream(stream.cuda_stream)
+    if not INCREMENTAL_PAIRS:
+        b.set_incremental(False)
     if tuned:
         b.set_launch_groups(*tuned)
     return b
@@ -534,13 +545,19 @@ def run_ours(args, rank, world, local):
     # ---- roofline of the dominant kernel (profiled pass) -------------------
     solve_ms, solve_launches = prof["solve"]
     items = st_prof["solver_items"]
+    solver_kernel = "k_schedule_solve"
+    if items == 0 and st_prof["contacts"] > 0:
+        # large-world solvers count no items: the last step's contacts x (sweeps + warm-start pass)
+        # per profiled step; the stage holds every kernel of the solve (ordered: one launch a step)
+        items = st_prof["contacts"] * (run_it + 1) * prof_steps
+        solver_kernel = "k_lw_color_pass + k_lw_color_seq" if args.coloured else "k_lw_ordered"
     peaks = measured_peaks()
     roof = None
     if solve_launches and solve_ms > 0:
         avg_ms = solve_ms / solve_launches
         bytes_per_launch = items / solve_launches * SOLVER_BYTES_PER_ITEM
         achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-        roof = {"kernel": "k_schedule_solve", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+        roof = {"kernel": solver_kernel, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                 "traffic": items / solve_launches * SOLVER_DRAM_BYTES_PER_ITEM,
                 "traffic_source": "ncu dram bytes per update (512-world capture) x updates per launch",
@@ -548,7 +565,7 @@ def run_ours(args, rank, world, local):
                 "items_per_launch": items / solve_launches, "avg_launch_ms": avg_ms}
         fp64_peak = measure_fp64_peak()
         if fp64_peak:
-            fp64 = {"kernel": "k_schedule_solve", "peak_lane_ops_per_s": fp64_peak,
+            fp64 = {"kernel": solver_kernel, "peak_lane_ops_per_s": fp64_peak,
                     "peak_source": "measured by this script (fp64 add/mul chains)",
                     "ops_per_item": SOLVER_FP64_OPS_PER_ITEM,
                     "achieved_lane_ops_per_s": items * SOLVER_FP64_OPS_PER_ITEM / (solve_ms * 1e-3)}
@@ -576,6 +593,8 @@ def run_ours(args, rank, world, local):
                        "parallelism": f"worlds sharded, {world} rank(s)",
                        "l2": "inputs larger than L2 (state + contacts + constraints of all worlds)",
                        "launch": "CUDA graph per step",
+                       "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
+                       else "grid, full 3x3 search every frame",
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1]} if tuned else "default"},
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -719,6 +738,8 @@ def main():
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
+    ap.add_argument("--no-incremental", action="store_true",
+                    help="grid worlds search every body's 3x3 cells every frame (no fat-box pair lists)")
     ap.add_argument("--large-quality", action="store_true",
                     help="container: residual, depth and speed of ordered vs coloured, with and without the network")
     ap.add_argument("--train-worlds", type=int, default=4096, help="worlds of the sample-collection run")
@@ -728,6 +749,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    global INCREMENTAL_PAIRS
+    INCREMENTAL_PAIRS = not args.no_incremental
     rank, world, local = dist_init()
     if args.impl == "reference":
         return run_reference(args, rank, world)

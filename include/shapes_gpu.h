@@ -40,6 +40,10 @@ extern "C" {
 #define SHAPES_E_NAN (-7)         /* non-finite body state passed in */
 #define SHAPES_E_BUFFER (-8)      /* caller's out-buffer too small */
 
+/* Shapes (Contact.hs:19-20 `data Shape`).  A hull is 3..64 counter-clockwise
+ * local vertices (makeHull, Engine.hs:47-51).  A circle (makeCircle,
+ * Engine.hs:53-54) is ONE local point (radius, 0) with 0 < radius < 2^500;
+ * its centre is the body's position (circleWithRadius, Contact/Circle.hs:24-25). */
 #define SHAPES_SHAPE_HULL 0
 #define SHAPES_SHAPE_CIRCLE 1
 
@@ -119,9 +123,11 @@ typedef struct shapes_batch shapes_batch;
 /* Build `n_worlds` independent worlds in one handle.
  *   world_body_offsets[n_worlds+1]: bodies of world w are [off[w], off[w+1]).
  *   bodies: SoA arrays of length off[n_worlds].
- *   vert_offsets[n_bodies+1]: hull vertices of body b are
+ *   vert_offsets[n_bodies+1]: local points of body b are
  *     local_verts_xy[2*vert_offsets[b] .. 2*vert_offsets[b+1]).
- *   shape_kind: per body SHAPES_SHAPE_*, or NULL for all hulls.
+ *   shape_kind: per body SHAPES_SHAPE_*, or NULL for all hulls.  A body whose
+ *     kind does not match its points (a circle with other than one point
+ *     (radius, 0), a hull with fewer than 3) is SHAPES_E_INVALID_ARG.
  * Shapes are posed from the bodies' positions on creation (makeWorldObj,
  * World.hs:142-149) and the contact cache starts empty (initEngine,
  * Engine/Main.hs:43-46).
@@ -229,6 +235,16 @@ int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream);
  * legacy default stream or already capturing.  Results are identical either
  * way. */
 int shapes_batch_set_graphs(shapes_batch* b, int32_t enabled);
+
+/* Incremental grid pairs (on by default).  Worlds on the grid broadphase
+ * keep, per body, a fat box (its AABB grown by 1/32 of the world's cell size)
+ * and the list of bodies whose fat boxes overlap it; only bodies whose AABB
+ * left their fat box are searched again, and each row's pairs are the listed
+ * bodies whose current AABBs overlap.  The pair list is identical either way;
+ * off = every grid body searches its 3x3 cells every frame.
+ * Replaces: nothing in the reference (Broadphase/Grid.hs:67-141 rebuilds the
+ * grid every frame); the pair contract of culledKeys (Aabb.hs:168-183) stays. */
+int shapes_batch_set_incremental(shapes_batch* b, int32_t enabled);
 
 /* Per-stage device timing.  While enabled, CUDA events on the handle's stream
  * bracket each stage of every step; get_profile returns the accumulated
@@ -367,8 +383,9 @@ int shapes_batch_delete_body(shapes_batch* b, int32_t world, int32_t slot);
  * (Utils/EmptiesVector.hs:72-86): fills the top of the world's empty-slot
  * stack (the slot freed last); with no empty slot the world grows by one slot
  * at its end (the reference's fixed-capacity vector would be full).  body10
- * holds the ten shapes_bodies fields of the new body in order; the hull is
- * posed at once (makeWorldObj, World.hs:142-149).  *slot receives the slot. */
+ * holds the ten shapes_bodies fields of the new body in order; n_verts 1 is a
+ * circle (local point (radius, 0)), 3..64 a hull; the shape is posed at once
+ * (makeWorldObj, World.hs:142-149).  *slot receives the slot. */
 int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body10, int32_t n_verts,
                              const double* local_verts_xy, int32_t* slot);
 /* Filled (1) or empty (0) per slot, over all worlds' slots (n_bodies bytes). */

@@ -72,6 +72,7 @@ def lib() -> ctypes.CDLL:
         L.oracle_world_append.restype = ctypes.c_int32
         L.oracle_world_append.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int32, _dp]
         L.oracle_world_get_active.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8)]
+        L.oracle_world_set_bodies.argtypes = [ctypes.c_void_p, _dp]
         _LIB = L
     return _LIB
 
@@ -136,6 +137,12 @@ class OracleWorld:
         out = np.empty((self.n, 10), dtype=np.float64)
         lib().oracle_world_get_bodies(self._h, _p(out, _dp))
         return {f: out[:, k].copy() for k, f in enumerate(BODY_FIELDS)}
+
+    def set_bodies(self, bodies: dict) -> None:
+        """Overwrites every body's fields and re-poses the shapes."""
+        rows = np.ascontiguousarray(np.stack([np.asarray(bodies[f], dtype=np.float64) for f in BODY_FIELDS], 1))
+        assert rows.shape[0] == self.n
+        lib().oracle_world_set_bodies(self._h, _p(rows, _dp))
 
     def shapes(self):
         xy = np.empty(2 * self.n_verts)

@@ -48,6 +48,7 @@ struct Body {
  * and the world-space vertices and unit edge normals of the current pose. */
 struct Hull {
   int nv = 0;
+  double radius = 0.0; /* > 0: a Circle (Contact/Circle.hs:19-22), nv = 1, local centre (0, 0) */
   std::vector<double> lx, ly;
   std::vector<int> emin, emax;
   std::vector<double> wx, wy, nx, ny;
@@ -137,6 +138,15 @@ static inline void extent_along(const double* xs, const double* ys, int nv, doub
 /* listToHull (ConvexHull.hs:151-167): local normals from local vertices, then
  * the (min, max) extent indices of the hull along each of its own normals. */
 static void init_hull(Hull& h, int nv, const double* xy) {
+  if (nv == 1) { /* a circle: one local point (radius, 0) */
+    h.nv = 1;
+    h.radius = xy[0];
+    h.lx.assign(1, 0.0); h.ly.assign(1, 0.0);
+    h.emin.assign(1, 0); h.emax.assign(1, 0);
+    h.wx.assign(1, 0.0); h.wy.assign(1, 0.0); h.nx.assign(1, 0.0); h.ny.assign(1, 0.0);
+    return;
+  }
+  h.radius = 0.0;
   h.nv = nv;
   h.lx.resize(nv); h.ly.resize(nv);
   for (int k = 0; k < nv; ++k) { h.lx[k] = xy[2 * k]; h.ly[k] = xy[2 * k + 1]; }
@@ -169,6 +179,7 @@ static void pose_hull(const Body& b, Hull& h) {
     h.wx[k] = (M[0][0] * x + M[0][1] * y) + M[0][2] * 1.0;
     h.wy[k] = (M[1][0] * x + M[1][1] * y) + M[1][2] * 1.0;
   }
+  if (h.radius > 0.0) return; /* setCircleTransform (Circle.hs:60-64): the centre only */
   for (int e = 0; e < h.nv; ++e) {
     int n1 = e < h.nv - 1 ? e + 1 : 0;
     unit_edge_normal(h.wx[e], h.wy[e], h.wx[n1], h.wy[n1], &h.nx[e], &h.ny[e]);
@@ -184,6 +195,10 @@ struct Aabb {
 /* hullToAabb (Aabb.hs:81-84): foldl1 mergeAabb over the vertex points, with
  * mergeRange (Aabb.hs:106-110) = (if a < c then a else c, if b > d then b else d). */
 static Aabb hull_aabb(const Hull& h) {
+  if (h.radius > 0.0) { /* circleToAabb (Aabb.hs:86-89) */
+    const double x = h.wx[0], y = h.wy[0], r = h.radius;
+    return Aabb{x - r, x + r, y - r, y + r};
+  }
   Aabb a{h.wx[0], h.wx[0], h.wy[0], h.wy[0]};
   for (int k = 1; k < h.nv; ++k) {
     double x = h.wx[k], y = h.wy[k];
@@ -446,6 +461,173 @@ static void hull_contacts(int32_t i, int32_t j, const Hull& a, const Hull& b,
   }
 }
 
+/* ---- circles (N2) --------------------------------------------------------- */
+
+static inline double dot2(double ax, double ay, double bx, double by) { return ax * bx + ay * by; }
+
+/* Circle.contact (Contact/Circle.hs:27-56): a is penetrated, b penetrates. */
+static bool circle_circle(const Hull& a, const Hull& b, double* nx, double* ny, double* px, double* py,
+                          double* depth) {
+  const double ax = a.wx[0], ay = a.wy[0], bx = b.wx[0], by = b.wy[0];
+  const double abx = bx - ax, aby = by - ay;
+  const double ra = a.radius, rb = b.radius;
+  const double rab = ra + rb;
+  const double ab_sq = abx * abx + aby * aby;
+  if (!(rab * rab >= ab_sq)) return false;
+  const double len = std::sqrt(ab_sq);
+  const double ux = abx / len, uy = aby / len;
+  const double a1x = ux * ra + ax, a1y = uy * ra + ay;
+  const double b1x = ux * (-rb) + bx, b1y = uy * (-rb) + by;
+  *nx = ux;
+  *ny = uy;
+  *px = (a1x + b1x) / 2.0;
+  *py = (a1y + b1y) / 2.0;
+  *depth = ra + rb - len;
+  return true;
+}
+
+/* crossV2V2 (Linear.hs:135-139): (a x b) x c. */
+static inline void cross3(double ax, double ay, double bx, double by, double cx, double cy, double* x,
+                          double* y) {
+  const double abz = ax * by - ay * bx;
+  *x = -(abz * cy);
+  *y = abz * cx;
+}
+
+/* support (ConvexHull.hs:124-128): the first vertex of largest projection. */
+static int support(const Hull& h, double dx, double dy) {
+  int best = 0;
+  double bd = dot2(h.wx[0], h.wy[0], dx, dy);
+  for (int k = 1; k < h.nv; ++k) {
+    const double t = dot2(h.wx[k], h.wy[k], dx, dy);
+    if (t > bd) { bd = t; best = k; }
+  }
+  return best;
+}
+
+/* GJK.closestSimplex (GJK.hs:52-66) from vertex 0 toward the point (ox, oy).
+ * Returns the simplex size (1, 2, or 3 = encloses the point) with s[0] the
+ * vertex added last.  The reference loop has no bound; this one stops after
+ * 4 nv + 8 extensions (treated as a failed search), a bound an ordinary
+ * convex hull never reaches. */
+static int closest_simplex(const Hull& h, double ox, double oy, int s[3]) {
+  int n = 1;
+  s[0] = 0;
+  double dx = ox - h.wx[0], dy = oy - h.wy[0];
+  for (int it = 0; it < 4 * h.nv + 8; ++it) {
+    const int a = support(h, dx, dy);
+    if (n == 1) { /* extendSimplex1 */
+      if (a == s[0]) return 1;
+      s[1] = s[0];
+      s[0] = a;
+      n = 2;
+      /* shiftSimplex2 (GJK.hs:95-107) */
+      const double abx = h.wx[s[1]] - h.wx[a], aby = h.wy[s[1]] - h.wy[a];
+      const double aox = ox - h.wx[a], aoy = oy - h.wy[a];
+      if (dot2(abx, aby, aox, aoy) > 0.0) {
+        cross3(abx, aby, aox, aoy, abx, aby, &dx, &dy);
+      } else {
+        n = 1;
+        dx = aox;
+        dy = aoy;
+      }
+      continue;
+    }
+    /* extendSimplex2 */
+    if (a == s[0] || a == s[1]) return 2;
+    const int b = s[0], c = s[1];
+    /* shiftSimplex3 (GJK.hs:109-135) on (a, b, c) */
+    const double ax = h.wx[a], ay = h.wy[a];
+    const double abx = h.wx[b] - ax, aby = h.wy[b] - ay;
+    const double acx = h.wx[c] - ax, acy = h.wy[c] - ay;
+    const double aox = ox - ax, aoy = oy - ay;
+    const double abc = abx * acy - aby * acx;
+    const double abcacx = -(abc * acy), abcacy = abc * acx;
+    const double ababcx = aby * abc, ababcy = -(abx * abc);
+    auto star = [&]() {
+      if (dot2(abx, aby, aox, aoy) > 0.0) {
+        s[0] = a; s[1] = b; n = 2;
+        cross3(abx, aby, aox, aoy, abx, aby, &dx, &dy);
+      } else {
+        s[0] = a; n = 1;
+        dx = aox; dy = aoy;
+      }
+    };
+    if (dot2(abcacx, abcacy, aox, aoy) > 0.0) {
+      if (dot2(acx, acy, aox, aoy) > 0.0) {
+        s[0] = a; s[1] = c; n = 2;
+        cross3(acx, acy, aox, aoy, acx, acy, &dx, &dy);
+      } else {
+        star();
+      }
+    } else if (dot2(ababcx, ababcy, aox, aoy) > 0.0) {
+      star();
+    } else {
+      s[0] = a; s[1] = b; s[2] = c;
+      return 3;
+    }
+  }
+  return n;
+}
+
+/* CircleVsHull.generateContacts (CircleVsHull.hs:18-69): the circle
+ * penetrates; one contact at the closest hull point, keyed by the feature
+ * (vertex) the GJK simplex ended on; none for a 3-point simplex. */
+static bool circle_hull(const Hull& circ, const Hull& hull, int* feature, double* nx, double* ny, double* px,
+                        double* py, double* depth) {
+  const double ox = circ.wx[0], oy = circ.wy[0];
+  int s[3];
+  const int n = closest_simplex(hull, ox, oy, s);
+  if (n == 3) return false;
+  double qx, qy;
+  if (n == 1) {
+    qx = hull.wx[s[0]];
+    qy = hull.wy[s[0]];
+  } else { /* closestAlong (CircleVsHull.hs:61-69) */
+    const double ax = hull.wx[s[0]], ay = hull.wy[s[0]];
+    const double aox = ox - ax, aoy = oy - ay;
+    const double abx = hull.wx[s[1]] - ax, aby = hull.wy[s[1]] - ay;
+    const double l = std::sqrt(abx * abx + aby * aby);
+    const double ux = abx / l, uy = aby / l;
+    const double t = dot2(aox, aoy, ux, uy);
+    qx = ux * t + ax;
+    qy = uy * t + ay;
+  }
+  /* processSimplex_ (CircleVsHull.hs:44-59) */
+  const double r = circ.radius;
+  const double bx = ox - qx, by = oy - qy;
+  const double ab_sq = bx * bx + by * by;
+  if (r * r < ab_sq) return false;
+  const double len = std::sqrt(ab_sq);
+  *feature = s[0];
+  *nx = -(bx / len);
+  *ny = -(by / len);
+  *px = qx;
+  *py = qy;
+  *depth = r - len;
+  return true;
+}
+
+/* Contact.generateContacts (Contact.hs:22-40) for pairs with a circle. */
+static void circle_contacts(int32_t i, int32_t j, const Hull& a, const Hull& b, std::vector<Contact>& out) {
+  Contact ct;
+  ct.key.i = i;
+  ct.key.j = j;
+  int f = 0;
+  bool hit;
+  if (a.radius > 0.0 && b.radius > 0.0) {
+    hit = circle_circle(a, b, &ct.nx, &ct.ny, &ct.px, &ct.py, &ct.depth);
+    ct.key.fa = 0; ct.key.fb = 0; ct.flip = 0;
+  } else if (a.radius > 0.0) {
+    hit = circle_hull(a, b, &f, &ct.nx, &ct.ny, &ct.px, &ct.py, &ct.depth);
+    ct.key.fa = 0; ct.key.fb = f; ct.flip = 0;
+  } else {
+    hit = circle_hull(b, a, &f, &ct.nx, &ct.ny, &ct.px, &ct.py, &ct.depth);
+    ct.key.fa = f; ct.key.fb = 0; ct.flip = 1;
+  }
+  if (hit) out.push_back(ct);
+}
+
 /* prepareFrame (Solvers/Contact.hs:40-52) via keyedContacts
  * (Constraints/Contact.hs:49-57): contacts of every broadphase pair, in pair
  * order, concatenated. */
@@ -454,7 +636,10 @@ static void narrowphase(World& w) {
   const size_t np = w.pairs.size() / 2;
   for (size_t p = 0; p < np; ++p) {
     int32_t i = w.pairs[2 * p], j = w.pairs[2 * p + 1];
-    hull_contacts(i, j, w.hulls[i], w.hulls[j], w.contacts);
+    if (w.hulls[i].radius > 0.0 || w.hulls[j].radius > 0.0)
+      circle_contacts(i, j, w.hulls[i], w.hulls[j], w.contacts);
+    else
+      hull_contacts(i, j, w.hulls[i], w.hulls[j], w.contacts);
   }
 }
 
@@ -737,6 +922,18 @@ int32_t oracle_world_append(void* h, const double* body10, int32_t nv, const dou
   pose_hull(w.bodies[slot], w.hulls[slot]);
   w.active[slot] = 1;
   return slot;
+}
+
+/* Overwrites every body's ten fields (rows as in oracle_world_create) and
+ * re-poses the shapes: updatePhysObj (World.hs:96-97) on every body, with the
+ * shapes moved as the next step's moveShape would (World.hs:132-133). */
+void oracle_world_set_bodies(void* h, const double* bodies10) {
+  World& w = *static_cast<World*>(h);
+  for (size_t i = 0; i < w.bodies.size(); ++i) {
+    const double* r = bodies10 + 10 * i;
+    w.bodies[i] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
+    pose_hull(w.bodies[i], w.hulls[i]);
+  }
 }
 
 void oracle_world_get_active(void* h, uint8_t* out) {

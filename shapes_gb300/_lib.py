@@ -25,6 +25,9 @@ SHAPES_E_TIMEOUT = -6
 SHAPES_E_NAN = -7
 SHAPES_E_BUFFER = -8
 
+SHAPE_HULL = 0
+SHAPE_CIRCLE = 1
+
 SHAPES_EXTERNAL_NONE = 0
 SHAPES_EXTERNAL_CONSTANT_ACCEL = 1
 SHAPES_WARM_START_OFF = 0
@@ -143,6 +146,7 @@ SIGNATURES = [
     ("shapes_mlp_train", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, ctypes.POINTER(TrainConfig),
                                         _fp]),
     ("shapes_batch_set_graphs", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_set_incremental", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_delete_body", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_append_body", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _dp, ctypes.c_int32, _dp, _ip]),
     ("shapes_batch_get_active", ctypes.c_int, [ctypes.c_void_p, _up]),
@@ -378,6 +382,10 @@ class Batch:
     def set_graphs(self, enabled: bool) -> None:
         """CUDA-graph replay of the step (default on)."""
         check(lib().shapes_batch_set_graphs(self._h, int(bool(enabled))), "shapes_batch_set_graphs")
+
+    def set_incremental(self, enabled: bool) -> None:
+        """Incremental grid pairs (fat boxes, default on); the pairs are identical either way."""
+        check(lib().shapes_batch_set_incremental(self._h, int(bool(enabled))), "shapes_batch_set_incremental")
 
     # ---- learned warm start ----
     def set_mlp(self, net: "Mlp | None") -> None:

@@ -83,6 +83,7 @@ struct shapes_batch {
   int32_t* vert_off = nullptr;
   double* lx = nullptr;
   double* ly = nullptr;
+  double* radius = nullptr; /* [N] circle radii (0 for hulls); null when there is no circle */
   int32_t* emin = nullptr;
   int32_t* emax = nullptr;
   /* state */
@@ -116,6 +117,18 @@ struct shapes_batch {
   uint8_t* row_mode = nullptr;
   int32_t* large_cnt = nullptr;
   int32_t* large_ids = nullptr;
+  double* metric_part = nullptr; /* [kMetricParts] partial metrics of one large world */
+  /* incremental grid pairs (fat boxes and adjacency lists) */
+  bool incremental = true;
+  int32_t nbr_cap = 24;
+  uint64_t* fatk = nullptr;
+  int32_t* nbr = nullptr;
+  int32_t* nbr_cnt = nullptr;
+  uint8_t* moved = nullptr;
+  int32_t* inc_state = nullptr;
+  int32_t* inc_rebuild = nullptr;
+  int32_t* inc_moved = nullptr;
+  double* inc_margin = nullptr;
   int32_t* pair_a = nullptr;
   int32_t* pair_b = nullptr;
   int32_t* slot_cnt = nullptr;
@@ -194,6 +207,7 @@ struct shapes_batch {
   uint8_t* active = nullptr;
   std::vector<uint8_t> h_active;
   std::vector<int32_t> h_vert_off;
+  std::vector<double> h_radius; /* [N] circle radii, 0 for hulls */
   std::vector<std::vector<int32_t>> h_empties;
   /* learned warm start */
   const shapes_mlp* mlp_model = nullptr;
@@ -338,6 +352,7 @@ struct shapes_batch {
     d.vert_off = vert_off;
     d.lx = lx;
     d.ly = ly;
+    d.radius = radius;
     d.emin = emin;
     d.emax = emax;
     d.vx = body[0];
@@ -370,6 +385,17 @@ struct shapes_batch {
     d.large_cnt = large_cnt;
     d.large_ids = large_ids;
     d.n_buckets = n_buckets;
+    if (incremental && nbr) {
+      d.fatk = fatk;
+      d.nbr = nbr;
+      d.nbr_cnt = nbr_cnt;
+      d.moved = moved;
+      d.inc_state = inc_state;
+      d.inc_rebuild = inc_rebuild;
+      d.inc_moved = inc_moved;
+      d.inc_margin = inc_margin;
+      d.nbr_cap = nbr_cap;
+    }
     d.row_cnt = row_cnt;
     d.row_off = row_off;
     d.pair_a = pair_a;
@@ -639,6 +665,7 @@ struct shapes_batch {
     lw_done = dalloc<int32_t>(lw_nb_max, "cudaMalloc large world");
     lw_color_cnt = dalloc<int32_t>(shapes::kMaxColors + 1, "cudaMalloc large world");
     lw_ctl = dalloc<unsigned long long>(8 * large_worlds.size(), "cudaMalloc large world");
+    if (!metric_part) metric_part = dalloc<double>(shapes::kMetricParts, "cudaMalloc large world");
   }
 
   shapes::LW lw_view(size_t k) const {
@@ -669,6 +696,25 @@ struct shapes_batch {
 
   /* Solve one large world: ranks of every contact on its bodies, then the
    * ordered dataflow kernel, or the coloured sweep. */
+  /* Per-world residual (or largest depth): one warp per world, and for each
+   * large world kMetricParts warps plus an ordered combine. */
+  void world_metric_kernels(const Dev& d, bool residual) {
+    const int split = large_worlds.empty() ? INT32_MAX : large_world_bodies;
+    if (residual)
+      shapes::k_residual<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d, split);
+    else
+      shapes::k_world_depth<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d, split);
+    for (int wld : large_worlds) {
+      if (residual) {
+        shapes::k_metric_part<true><<<shapes::kMetricParts / 4, 128, 0, stream>>>(d, wld, metric_part);
+        shapes::k_metric_final<true><<<1, 32, 0, stream>>>(d, wld, metric_part);
+      } else {
+        shapes::k_metric_part<false><<<shapes::kMetricParts / 4, 128, 0, stream>>>(d, wld, metric_part);
+        shapes::k_metric_final<false><<<1, 32, 0, stream>>>(d, wld, metric_part);
+      }
+    }
+  }
+
   void solve_large_world(const Dev& d, size_t k, const shapes_config& cfg) {
     shapes::LW w = lw_view(k);
     const int cap = contact_cap;
@@ -707,6 +753,36 @@ struct shapes_batch {
     });
   }
 
+  void free_incremental() {
+    dfree(fatk); dfree(nbr); dfree(nbr_cnt); dfree(moved); dfree(inc_state); dfree(inc_rebuild); dfree(inc_moved);
+    dfree(inc_margin);
+    fatk = nullptr;
+    nbr = nullptr;
+    nbr_cnt = nullptr;
+    moved = nullptr;
+    inc_state = inc_rebuild = inc_moved = nullptr;
+    inc_margin = nullptr;
+  }
+
+  /* Adjacency lists of nbr_cap entries per body; every world rebuilds next frame. */
+  void setup_incremental() {
+    free_incremental();
+    if (!any_grid) return;
+    fatk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc grid");
+    nbr = dalloc<int32_t>((size_t)N * nbr_cap, "cudaMalloc grid");
+    nbr_cnt = dalloc<int32_t>(N, "cudaMalloc grid");
+    moved = dalloc<uint8_t>(N, "cudaMalloc grid");
+    inc_state = dalloc<int32_t>(W, "cudaMalloc grid");
+    inc_rebuild = dalloc<int32_t>(W, "cudaMalloc grid");
+    inc_moved = dalloc<int32_t>(W, "cudaMalloc grid");
+    inc_margin = dalloc<double>(W, "cudaMalloc grid");
+    reset_incremental();
+  }
+
+  void reset_incremental() {
+    if (inc_state) ck(cudaMemsetAsync(inc_state, 0, sizeof(int32_t) * W, stream), "memset");
+  }
+
   /* Worlds with at least grid_min_bodies bodies use the grid broadphase. */
   void setup_grid() {
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
@@ -743,6 +819,7 @@ struct shapes_batch {
     ck(cudaMemcpy(grid_T, T.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
     ck(cudaMemcpy(grid_base, base.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
     ck(cudaMemset(row_mode, 0, N), "memset");
+    setup_incremental();
   }
   int32_t smem_last_cap = 0; /* bodies whose last level fits the solver's shared memory */
 
@@ -782,7 +859,22 @@ struct shapes_batch {
      * levels add up over the call */
     ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2, stream), "memset");
     ck(cudaMemsetAsync(counters + shapes::kCntGroupAlloc, 0, sizeof(unsigned long long), stream), "memset");
-    if (any_grid) {
+    const bool inc = any_grid && d.nbr != nullptr;
+    if (inc) {
+      stage(0, 6, [&]() {
+        ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
+        shapes::k_inc_stats<<<W, 256, 0, stream>>>(d);
+        shapes::k_inc_mark<<<grid_for(N, 256), 256, 0, stream>>>(d);
+        shapes::k_inc_decide<<<grid_for(W, 128), 128, 0, stream>>>(d);
+        shapes::k_inc_remove<<<grid_for(N, 128), 128, 0, stream>>>(d);
+        shapes::k_inc_refat<<<grid_for(N, 256), 256, 0, stream>>>(d);
+      });
+      scan(bucket_cnt, n_buckets, nullptr, bucket_off);
+      stage(0, 2, [&]() {
+        shapes::k_inc_scatter<<<grid_for(N, 256), 256, 0, stream>>>(d);
+        shapes::k_inc_query<<<grid_for(N, 128), 128, 0, stream>>>(d);
+      });
+    } else if (any_grid) {
       stage(0, 3, [&]() {
         ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
         shapes::k_grid_stats<<<W, 256, 0, stream>>>(d);
@@ -793,15 +885,19 @@ struct shapes_batch {
     }
     stage(0, any_grid ? 2 : 1, [&]() {
       shapes::k_broadphase<true><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
-      if (any_grid) shapes::k_grid_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
+      if (inc)
+        shapes::k_inc_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
+      else if (any_grid)
+        shapes::k_grid_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
     });
     scan(row_cnt, N, nullptr, row_off);
     stage(0, any_grid ? 3 : 1, [&]() {
       shapes::k_broadphase<false><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
-      if (any_grid) {
+      if (inc)
+        shapes::k_inc_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
+      else if (any_grid)
         shapes::k_grid_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
-        shapes::k_grid_sort_rows<<<grid_for(N, 128), 128, 0, stream>>>(d);
-      }
+      if (any_grid) shapes::k_grid_sort_rows<<<grid_for(N, 128), 128, 0, stream>>>(d);
     });
     stage(6, 1, [&]() { shapes::k_world_pair_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
     stage(1, 4, [&]() {
@@ -829,7 +925,7 @@ struct shapes_batch {
                                           counters + shapes::kCntPredicted,
                                           reinterpret_cast<int*>(counters + shapes::kCntMlpErr), contact_cap, stream),
              "k_mlp_predict");
-          shapes::k_world_depth<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d);
+          if (judge_set) world_metric_kernels(d, false);
         }
       });
     }
@@ -844,8 +940,8 @@ struct shapes_batch {
                                              cfg.accel_y, cfg.dt, G, per_warp);
       });
     for (size_t k = 0; k < large_worlds.size(); ++k) solve_large_world(d, k, cfg);
-    if ((cfg.flags & SHAPES_FLAG_RESIDUAL) || learn)
-      stage(4, 1, [&]() { shapes::k_residual<<<(W * 32 + 127) / 128, 128, 0, stream>>>(d); });
+    if ((cfg.flags & SHAPES_FLAG_RESIDUAL) || (learn && judge_set))
+      stage(4, 1 + 2 * (int)large_worlds.size(), [&]() { world_metric_kernels(d, true); });
     if (learn && judge_set)
       stage(7, 1, [&]() { shapes::k_learned_judge<<<grid_for(W, 128), 128, 0, stream>>>(d); });
     if (collect)
@@ -945,14 +1041,38 @@ struct shapes_batch {
       cache_buf = saved_cache_buf;
       if (solve) restore(saved_cap);
       ck(cudaStreamSynchronize(stream), "restore");
-      const int64_t np = (int64_t)pair_cap * ((agg[shapes::kCntOverflow] & 1ull) ? 2 : 1);
-      const int64_t nc = (int64_t)contact_cap * 2;
-      if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
-      alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
+      if (agg[shapes::kCntOverflow] & 4ull) { /* an adjacency list was full */
+        if (nbr_cap > (1 << 14)) return SHAPES_E_CAPACITY;
+        nbr_cap *= 2;
+        invalidate_graphs();
+        setup_incremental();
+      }
+      reset_incremental(); /* the lists follow the undone steps' poses */
+      if (agg[shapes::kCntOverflow] & ~4ull) {
+        const int64_t np = (int64_t)pair_cap * ((agg[shapes::kCntOverflow] & 1ull) ? 2 : 1);
+        const int64_t nc = (int64_t)contact_cap * 2;
+        if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
+        alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
+      }
       ensure_items(solve ? cfg.iterations : 0);
       if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
       if (solve) pose(0, 0.0);
     }
+  }
+
+  /* The local points in the caller's convention (a circle as (radius, 0)). */
+  std::vector<double> local_xy_host() {
+    std::vector<double> xs(V), ys(V), xy(2 * (size_t)V);
+    ck(cudaMemcpyAsync(xs.data(), lx, sizeof(double) * V, cudaMemcpyDeviceToHost, stream), "download");
+    ck(cudaMemcpyAsync(ys.data(), ly, sizeof(double) * V, cudaMemcpyDeviceToHost, stream), "download");
+    ck(cudaStreamSynchronize(stream), "download");
+    for (int64_t v = 0; v < V; ++v) {
+      xy[2 * v] = xs[v];
+      xy[2 * v + 1] = ys[v];
+    }
+    for (int32_t b = 0; b < N; ++b)
+      if (h_radius[b] > 0.0) xy[2 * (size_t)h_vert_off[b]] = h_radius[b];
+    return xy;
   }
 
   /* (Re)builds everything sized by the bodies and vertices from host arrays:
@@ -966,6 +1086,8 @@ struct shapes_batch {
     invalidate_graphs();
     free_step_buffers();
     dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly); dfree(emin); dfree(emax);
+    dfree(radius);
+    radius = nullptr;
     for (int k = 0; k < 10; ++k) {
       dfree(body[k]);
       dfree(body_stage[k]);
@@ -1017,11 +1139,28 @@ struct shapes_batch {
        "upload");
     ck(cudaMemcpy(body_world, h_body_world.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
     ck(cudaMemcpy(vert_off, vert_offsets, sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "upload");
+    /* a circle's one local point (radius, 0) becomes radius[b] and the local
+     * centre (0, 0) (circleWithRadius, Contact/Circle.hs:24-25) */
+    h_radius.assign(N, 0.0);
+    bool any_circle = false;
+    for (int32_t b = 0; b < N; ++b)
+      if (vert_offsets[b + 1] - vert_offsets[b] == 1) {
+        h_radius[b] = local_verts_xy[2 * (size_t)vert_offsets[b]];
+        any_circle = true;
+      }
     std::vector<double> tmp(V);
     for (int32_t v = 0; v < V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v];
+    for (int32_t b = 0; b < N; ++b)
+      if (h_radius[b] > 0.0) tmp[vert_offsets[b]] = 0.0;
     ck(cudaMemcpy(lx, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice), "upload");
     for (int32_t v = 0; v < V; ++v) tmp[v] = local_verts_xy[2 * (size_t)v + 1];
+    for (int32_t b = 0; b < N; ++b)
+      if (h_radius[b] > 0.0) tmp[vert_offsets[b]] = 0.0;
     ck(cudaMemcpy(ly, tmp.data(), sizeof(double) * V, cudaMemcpyHostToDevice), "upload");
+    if (any_circle) {
+      radius = dalloc<double>(N, "cudaMalloc");
+      ck(cudaMemcpy(radius, h_radius.data(), sizeof(double) * N, cudaMemcpyHostToDevice), "upload");
+    }
     for (int k = 0; k < 10; ++k) ck(cudaMemcpy(body[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice), "upload bodies");
     /* empty cache: every world offset 0 */
     for (int k = 0; k < 2; ++k) ck(cudaMemset(cwo[k], 0, sizeof(int32_t) * (n_worlds + 1)), "memset");
@@ -1075,6 +1214,9 @@ struct shapes_batch {
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
+    free_incremental();
+    dfree(radius);
+    dfree(metric_part);
     for (int k = 0; k < 2; ++k) dfree(cwo[k]);
     dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
     dfree(phase_clock);
@@ -1122,6 +1264,24 @@ int check_hull(int nv, const double* xy) {
   return SHAPES_OK;
 }
 
+/* A circle is one local point (radius, 0) with 0 < radius < 2^500. */
+int check_shape(uint8_t kind, int nv, const double* xy) {
+  if (kind == SHAPES_SHAPE_HULL) {
+    const int rc = check_hull(nv, xy);
+    if (rc != SHAPES_OK) g_last_error = "a hull needs 3..64 finite, strictly convex, counter-clockwise vertices";
+    return rc;
+  }
+  g_last_error = "a circle is one local point (radius, 0) with 0 < radius < 2^500";
+  if (kind != SHAPES_SHAPE_CIRCLE || nv != 1) {
+    if (kind != SHAPES_SHAPE_CIRCLE) g_last_error = "unknown shape kind";
+    return SHAPES_E_INVALID_ARG;
+  }
+  if (!std::isfinite(xy[0]) || !std::isfinite(xy[1])) return SHAPES_E_NAN;
+  if (!(xy[0] > 0.0) || xy[0] >= 0x1p500 || xy[1] != 0.0) return SHAPES_E_INVALID_ARG;
+  g_last_error.clear();
+  return SHAPES_OK;
+}
+
 template <typename F>
 int guarded(F&& f) {
   try {
@@ -1158,6 +1318,7 @@ const char* shapes_last_error_detail(void) { return g_last_error.c_str(); }
 int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, const shapes_bodies* bodies,
                         const int32_t* vert_offsets, const double* local_verts_xy, const uint8_t* shape_kind,
                         shapes_batch** out) {
+  g_last_error.clear();
   if (!out || n_worlds < 1 || !world_body_offsets || !vert_offsets || !local_verts_xy || !body_arrays_ok(bodies))
     return SHAPES_E_INVALID_ARG;
   *out = nullptr;
@@ -1170,10 +1331,9 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets, con
   if (N < 1) return SHAPES_E_INVALID_ARG;
   if (vert_offsets[0] != 0) return SHAPES_E_INVALID_ARG;
   for (int32_t b = 0; b < N; ++b) {
-    if (shape_kind && shape_kind[b] == SHAPES_SHAPE_CIRCLE) return SHAPES_E_UNSUPPORTED;
-    if (shape_kind && shape_kind[b] != SHAPES_SHAPE_HULL) return SHAPES_E_INVALID_ARG;
     const int32_t nv = vert_offsets[b + 1] - vert_offsets[b];
-    const int rc = check_hull(nv, local_verts_xy + 2 * (size_t)vert_offsets[b]);
+    const int rc = check_shape(shape_kind ? shape_kind[b] : (uint8_t)SHAPES_SHAPE_HULL, nv,
+                               local_verts_xy + 2 * (size_t)vert_offsets[b]);
     if (rc != SHAPES_OK) return rc;
   }
   double* bp[10];
@@ -1484,7 +1644,7 @@ int shapes_batch_get_world_metrics(shapes_batch* b, double* residual, double* ma
       b->stats = keep;
       if (rc != SHAPES_OK) return rc;
       Dev d = b->view(b->results_buf);
-      shapes::k_world_depth<<<(b->W * 32 + 127) / 128, 128, 0, b->stream>>>(d);
+      b->world_metric_kernels(d, false);
       ck(cudaGetLastError(), "launch");
       ck(cudaMemcpyAsync(max_depth, b->world_depth, sizeof(double) * b->W, cudaMemcpyDeviceToHost, b->stream), "download");
       ck(cudaStreamSynchronize(b->stream), "download");
@@ -1612,7 +1772,7 @@ int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body1
   if (!b || !body10 || !local_verts_xy || !slot_out || world < 0 || world >= b->W) return SHAPES_E_INVALID_ARG;
   for (int k = 0; k < 10; ++k)
     if (!std::isfinite(body10[k])) return SHAPES_E_NAN;
-  const int hrc = check_hull(n_verts, local_verts_xy);
+  const int hrc = check_shape(n_verts == 1 ? SHAPES_SHAPE_CIRCLE : SHAPES_SHAPE_HULL, n_verts, local_verts_xy);
   if (hrc != SHAPES_OK) return hrc;
   return guarded([&]() -> int {
     const int32_t W = b->W, N = b->N;
@@ -1632,6 +1792,12 @@ int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body1
         for (int32_t v = 0; v < n_verts; ++v) {
           xs[v] = local_verts_xy[2 * v];
           ys[v] = local_verts_xy[2 * v + 1];
+        }
+        if (n_verts == 1) { /* a circle into a circle's slot */
+          b->h_radius[g] = xs[0];
+          xs[0] = ys[0] = 0.0;
+          ck(cudaMemcpyAsync(b->radius + g, &b->h_radius[g], sizeof(double), cudaMemcpyHostToDevice, b->stream),
+             "upload");
         }
         ck(cudaMemcpyAsync(b->lx + v0, xs.data(), sizeof(double) * n_verts, cudaMemcpyHostToDevice, b->stream), "upload");
         ck(cudaMemcpyAsync(b->ly + v0, ys.data(), sizeof(double) * n_verts, cudaMemcpyHostToDevice, b->stream), "upload");
@@ -1666,10 +1832,7 @@ int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body1
     rc = shapes_batch_get_cache(b, keys.data(), lam.data(), nc, wc.data());
     if (rc != SHAPES_OK) return rc;
     const int64_t V = b->V;
-    std::vector<double> lxh(V), lyh(V);
-    ck(cudaMemcpyAsync(lxh.data(), b->lx, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
-    ck(cudaMemcpyAsync(lyh.data(), b->ly, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
-    ck(cudaStreamSynchronize(b->stream), "download");
+    const std::vector<double> xyh = b->local_xy_host();
     const int32_t g = w0 + slot; /* replaced or inserted body */
     const int32_t N2 = reuse ? N : N + 1;
     std::vector<int32_t> off(W + 1);
@@ -1689,8 +1852,8 @@ int shapes_batch_append_body(shapes_batch* b, int32_t world, const double* body1
         vo2[i + 1] = vo2[i] + n_verts;
       } else {
         for (int32_t v = b->h_vert_off[src]; v < b->h_vert_off[src + 1]; ++v) {
-          xy2.push_back(lxh[v]);
-          xy2.push_back(lyh[v]);
+          xy2.push_back(xyh[2 * (size_t)v]);
+          xy2.push_back(xyh[2 * (size_t)v + 1]);
         }
         vo2[i + 1] = vo2[i] + (b->h_vert_off[src + 1] - b->h_vert_off[src]);
       }
@@ -1788,13 +1951,10 @@ int shapes_batch_save(shapes_batch* b, const char* path) {
   std::vector<double> lam(2 * (size_t)std::max<int64_t>(nc, 1));
   rc = shapes_batch_get_cache(b, keys.data(), lam.data(), nc, wc.data());
   if (rc != SHAPES_OK) return rc;
-  std::vector<int32_t> vo(N + 1);
-  std::vector<double> lx(V), ly(V);
+  const std::vector<int32_t>& vo = b->h_vert_off;
+  std::vector<double> xy;
   rc = guarded([&]() -> int {
-    ck(cudaMemcpyAsync(vo.data(), b->vert_off, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost, b->stream), "download");
-    ck(cudaMemcpyAsync(lx.data(), b->lx, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
-    ck(cudaMemcpyAsync(ly.data(), b->ly, sizeof(double) * V, cudaMemcpyDeviceToHost, b->stream), "download");
-    ck(cudaStreamSynchronize(b->stream), "download");
+    xy = b->local_xy_host();
     return SHAPES_OK;
   });
   if (rc != SHAPES_OK) return rc;
@@ -1808,10 +1968,7 @@ int shapes_batch_save(shapes_batch* b, const char* path) {
   w.put1(nc);
   w.put(b->h_world_body_off.data(), (size_t)W + 1);
   w.put(vo.data(), (size_t)N + 1);
-  for (int64_t k = 0; k < V; ++k) {
-    w.put1(lx[k]);
-    w.put1(ly[k]);
-  }
+  w.put(xy.data(), 2 * (size_t)V);
   w.put(body.data(), body.size());
   w.put(wc.data(), (size_t)W);
   w.put(keys.data(), 4 * (size_t)nc);
@@ -1867,7 +2024,7 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
   if (r.get1<uint32_t>() != kCkEndian) return bad("byte order differs");
   const int32_t W = r.get1<int32_t>(), N = r.get1<int32_t>();
   const int64_t V = r.get1<int64_t>(), nc = r.get1<int64_t>();
-  if (!r.ok || W < 1 || N < 1 || V < 3 || nc < 0 || V > (int64_t)INT32_MAX || nc > (int64_t)INT32_MAX)
+  if (!r.ok || W < 1 || N < 1 || V < 1 || nc < 0 || V > (int64_t)INT32_MAX || nc > (int64_t)INT32_MAX)
     return bad("bad sizes");
   const uint64_t need = 40ull + 4ull * (W + 1) + 4ull * (N + 1) + 16ull * V + 80ull * N + 4ull * W + 16ull * nc +
                         16ull * nc + 1ull * N + 4ull * W + 8ull; /* + the empty-slot stacks */
@@ -1902,8 +2059,14 @@ int shapes_batch_load(const char* path, shapes_batch** out) {
   for (int k = 0; k < 10; ++k) bp[k] = body.data() + (size_t)k * N;
   in.vel_x = bp[0]; in.vel_y = bp[1]; in.rot_vel = bp[2]; in.pos_x = bp[3]; in.pos_y = bp[4];
   in.rot = bp[5]; in.inv_mass_lin = bp[6]; in.inv_mass_rot = bp[7]; in.mu = bp[8]; in.bounce = bp[9];
+  if (vo[0] != 0 || vo[N] != V) return bad("bad vertex offsets");
+  std::vector<uint8_t> kind(N);
+  for (int32_t i = 0; i < N && r.ok; ++i) {
+    if (vo[i + 1] < vo[i] || vo[i + 1] > V) return bad("bad vertex offsets");
+    kind[i] = vo[i + 1] - vo[i] == 1 ? SHAPES_SHAPE_CIRCLE : SHAPES_SHAPE_HULL;
+  }
   shapes_batch* h = nullptr;
-  int rc = shapes_batch_create(W, off.data(), &in, vo.data(), xy.data(), nullptr, &h);
+  int rc = shapes_batch_create(W, off.data(), &in, vo.data(), xy.data(), kind.data(), &h);
   if (rc != SHAPES_OK) return rc;
   rc = shapes_batch_set_cache(h, wc.data(), keys.data(), lam.data());
   if (rc == SHAPES_OK)
@@ -2044,6 +2207,17 @@ int shapes_batch_set_stream(shapes_batch* b, void* cuda_stream) {
   return guarded([&]() -> int {
     ck(cudaStreamSynchronize(b->stream), "sync");
     b->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : b->own_stream;
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_incremental(shapes_batch* b, int32_t enabled) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->incremental = enabled != 0;
+    b->invalidate_graphs();
+    b->reset_incremental();
     return SHAPES_OK;
   });
 }

@@ -24,6 +24,7 @@ constexpr uint32_t kWarmBit = 0x80000000u;
 constexpr uint8_t kFlagStatic = 1;
 constexpr uint8_t kFlagBoxNaN = 2;
 constexpr uint8_t kFlagInactive = 4; /* empty slot (World.delete): no pairs, no motion */
+constexpr uint8_t kFlagCircle = 8;
 /* per-contact info byte */
 constexpr uint8_t kInfoHit = 1;
 constexpr uint8_t kInfoDynA = 2;
@@ -88,6 +89,16 @@ struct Dev {
   int32_t* large_cnt;       /* [W] bodies of the world off the grid */
   int32_t* large_ids;       /* [N] per-world region at world_body_off[w] */
   int32_t n_buckets;
+  /* incremental grid pairs (fat boxes); null when off */
+  uint64_t* fatk;        /* [4N] ordered keys of each grid body's fat box */
+  int32_t* nbr;          /* [N * nbr_cap] bodies whose fat boxes overlap (either index); -1 = removed */
+  int32_t* nbr_cnt;      /* [N] entries used in nbr */
+  uint8_t* moved;        /* [N] kMoved* bits of this frame */
+  int32_t* inc_state;    /* [W] 0 = rebuild the adjacency next frame, 1 = valid */
+  int32_t* inc_rebuild;  /* [W] this frame rebuilds the world's adjacency */
+  int32_t* inc_moved;    /* [W] bodies re-inserted this frame */
+  double* inc_margin;    /* [W] fat-box margin */
+  int32_t nbr_cap;
   int32_t* row_cnt; /* [N] mirrored per-row pair counts */
   int32_t* row_off; /* [N+1] scanned */
   int32_t* pair_a;  /* [pair_cap] global body index, the larger */
@@ -138,6 +149,7 @@ struct Dev {
   const double* judge_res;     /* [W] residual limit of the judge */
   const double* judge_depth;   /* [W] depth limit of the judge */
   const uint8_t* active;       /* [N] 0 = empty slot (World.delete); null when every slot is filled */
+  const double* radius;        /* [N] > 0: a circle (one local point, the centre); 0: a hull */
 };
 
 enum {
@@ -200,6 +212,11 @@ __global__ void k_init_extents(Dev d) {
       if (d.vert_off[mid] <= v) lo = mid; else hi = mid - 1;
     }
     const int b0 = d.vert_off[lo], nv = d.vert_off[lo + 1] - b0, e = v - b0;
+    if (nv < 3) { /* a circle: no edges */
+      d.emin[v] = 0;
+      d.emax[v] = 0;
+      continue;
+    }
     const int n1 = e < nv - 1 ? e + 1 : 0;
     const double ddx = d.lx[b0 + n1] - d.lx[b0 + e], ddy = d.ly[b0 + n1] - d.ly[b0 + e];
     const double ex = ddy, ey = -ddx;
@@ -267,6 +284,32 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance) {
     /* m02 * 1.0 == m02 and m12 * 1.0 == m12 unless NaN (then both are NaN) */
     const bool t_nan = nan_bits(m02) || nan_bits(m12);
     const int b0 = d.vert_off[g], nv = d.vert_off[g + 1] - b0;
+    const double rad = d.radius ? d.radius[g] : 0.0;
+    if (rad > 0.0) {
+      /* setCircleTransform (Circle.hs:60-64): the transformed local origin;
+       * circleToAabb (Aabb.hs:86-89): centre -+ radius */
+      const double lx = d.lx[b0], ly = d.ly[b0];
+      const double x = t_nan ? (m00 * lx + m01 * ly) + m02 * 1.0 : (mul_rn_int(m00, lx) + m01 * ly) + m02;
+      const double y = t_nan ? (m10 * lx + m11 * ly) + m12 * 1.0 : (mul_rn_int(m10, lx) + m11 * ly) + m12;
+      d.wx[b0] = x;
+      d.wy[b0] = y;
+      d.nx[b0] = 0.0;
+      d.ny[b0] = 0.0;
+      const double cb0 = x - rad, cb1 = x + rad, cb2 = y - rad, cb3 = y + rad;
+      d.box[4 * g + 0] = cb0;
+      d.box[4 * g + 1] = cb1;
+      d.box[4 * g + 2] = cb2;
+      d.box[4 * g + 3] = cb3;
+      d.boxk[4 * g + 0] = okey(cb0);
+      d.boxk[4 * g + 1] = okey(cb1);
+      d.boxk[4 * g + 2] = okey(cb2);
+      d.boxk[4 * g + 3] = okey(cb3);
+      uint8_t f = kFlagCircle;
+      if (d.iml[g] == 0.0 && d.imr[g] == 0.0) f |= kFlagStatic;
+      if (nan_bits(cb0) || nan_bits(cb1) || nan_bits(cb2) || nan_bits(cb3)) f |= kFlagBoxNaN;
+      d.flags[g] = f;
+      continue;
+    }
     double x0 = 0, y0 = 0, xp = 0, yp = 0;
     double bx0 = 0, bx1 = 0, by0 = 0, by1 = 0;
     for (int k = 0; k < nv; ++k) {
@@ -576,6 +619,309 @@ __global__ void k_grid_sort_rows(Dev d) {
   }
 }
 
+/* ---- incremental grid pairs ------------------------------------------------
+ * The grid rows above search the 3x3 cells of every body every frame.  Most
+ * bodies move far less than a cell per frame, so the incremental variant keeps
+ * for each grid body a fat box (its box grown by a margin of s/32, s the
+ * world's cell size) and the list of bodies whose fat boxes overlap it (an
+ * adjacency, symmetric: each overlap is listed at both bodies).  While a
+ * body's box stays inside its fat box nothing about it is searched again:
+ * boxes inside overlapping-or-not fat boxes overlap only if the fat boxes do,
+ * so the exact pairs of a row are its adjacency entries j < i whose current
+ * boxes overlap (pair_overlaps, the same test as every other path).  A body
+ * whose box left its fat box (or that changed between grid and large) is
+ * "moved": it is removed from its old neighbours' lists, gets a new fat box,
+ * searches the 3x3 cells of the fat-box grid (binned only in worlds with
+ * moved bodies) and is appended to each unmoved neighbour's list.  A world
+ * with more than a quarter of its bodies moved, a new world, and every world
+ * after a retry rebuild the whole adjacency.  Large bodies (fat box not
+ * small, or a non-finite box) stay on the per-world large list as before.
+ * Rows come out unordered and are sorted like grid rows, so the pair list is
+ * exactly the brute-force rows' list.  A list that would exceed nbr_cap sets
+ * overflow bit 4 and the host retries with a larger capacity. */
+
+constexpr uint8_t kMovedBit = 1;     /* re-inserted this frame */
+constexpr uint8_t kMovedWasGrid = 2; /* was in the adjacency before this frame */
+constexpr uint8_t kMovedNowGrid = 4; /* is in the adjacency after this frame */
+
+/* Fat box of a body's current box, its cell, and whether it is small enough
+ * for the grid (the same finiteness and size rules as k_grid_bin, on the fat
+ * box). */
+__device__ __forceinline__ bool fat_box(const Dev& d, int g, int wld, double fb[4], int* cx, int* cy) {
+  const double inv_s = d.grid_inv_s[wld];
+  if (!(inv_s > 0.0) || (d.flags[g] & kFlagBoxNaN)) return false;
+  const double m = d.inc_margin[wld];
+  fb[0] = d.box[4 * g + 0] - m;
+  fb[1] = d.box[4 * g + 1] + m;
+  fb[2] = d.box[4 * g + 2] - m;
+  fb[3] = d.box[4 * g + 3] + m;
+  const double lim = d.grid_lim[wld];
+  const double qx = fb[0] * inv_s, qy = fb[2] * inv_s;
+  if (!(small_mag(fb[0]) && small_mag(fb[1]) && small_mag(fb[2]) && small_mag(fb[3]) && (fb[1] - fb[0]) < lim &&
+        (fb[3] - fb[2]) < lim && fabs(qx) < 0x1p30 && fabs(qy) < 0x1p30))
+    return false;
+  *cx = (int)floor(qx);
+  *cy = (int)floor(qy);
+  return true;
+}
+
+/* One CTA per grid world: in a world that rebuilds, the cell size from the
+ * mean extent (as k_grid_stats) and the margin s/32; every world clears its
+ * large list and moved count. */
+__global__ void k_inc_stats(Dev d) {
+  __shared__ double s_sum[32];
+  __shared__ int s_cnt[32];
+  const int wld = blockIdx.x;
+  if (d.grid_T[wld] == 0) return;
+  if (d.inc_state[wld] != 0) {
+    if (threadIdx.x == 0) {
+      d.large_cnt[wld] = 0;
+      d.inc_moved[wld] = 0;
+    }
+    return;
+  }
+  const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+  double sum = 0.0;
+  int cnt = 0;
+  for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
+    const double w = d.box[4 * g + 1] - d.box[4 * g + 0];
+    const double h = d.box[4 * g + 3] - d.box[4 * g + 2];
+    const double e = w > h ? w : h;
+    if (small_mag(e)) {
+      sum += e;
+      ++cnt;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_sum[threadIdx.x >> 5] = sum;
+    s_cnt[threadIdx.x >> 5] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    int c = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      t += s_sum[k];
+      c += s_cnt[k];
+    }
+    const double sz = c > 0 ? 2.0 * t / c : 0.0;
+    const double inv = (sz > 0.0 && small_mag(sz) && small_mag(1.0 / sz)) ? 1.0 / sz : 0.0;
+    d.grid_inv_s[wld] = inv;
+    d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
+    d.inc_margin[wld] = inv > 0.0 ? 0.03125 / inv : 0.0;
+    d.large_cnt[wld] = 0;
+    d.inc_moved[wld] = 0;
+  }
+}
+
+/* One thread per body of a grid world: moved or not, and the large list. */
+__global__ void k_inc_mark(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0) continue;
+    const bool rebuild = d.inc_state[wld] == 0;
+    const bool was = !rebuild && d.row_mode[g];
+    double fb[4];
+    int cx, cy;
+    const bool fits = fat_box(d, g, wld, fb, &cx, &cy);
+    bool moved, now;
+    if (rebuild) {
+      moved = true;
+      now = fits;
+    } else if (was) {
+      const uint64_t* f = d.fatk + 4 * g;
+      const uint64_t* b = d.boxk + 4 * g;
+      const bool inside = !(d.flags[g] & kFlagBoxNaN) && f[0] <= b[0] && b[1] <= f[1] && f[2] <= b[2] && b[3] <= f[3];
+      moved = !inside;
+      now = inside || fits;
+    } else {
+      moved = fits;
+      now = fits;
+    }
+    d.moved[g] = (moved ? kMovedBit : 0) | (was ? kMovedWasGrid : 0) | (now ? kMovedNowGrid : 0);
+    if (moved && !rebuild) atomicAdd(&d.inc_moved[wld], 1);
+    if (!now) {
+      const int k = atomicAdd(&d.large_cnt[wld], 1);
+      d.large_ids[d.world_body_off[wld] + k] = g;
+    }
+  }
+}
+
+/* One thread per world: rebuild when the adjacency is new or more than a
+ * quarter of the world moved. */
+__global__ void k_inc_decide(Dev d) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < d.n_worlds; w += gridDim.x * blockDim.x) {
+    if (d.grid_T[w] == 0) continue;
+    const int n = d.world_body_off[w + 1] - d.world_body_off[w];
+    d.inc_rebuild[w] = (d.inc_state[w] == 0 || 4 * d.inc_moved[w] > n) ? 1 : 0;
+    d.inc_state[w] = 1;
+  }
+}
+
+/* One thread per moved body that was in the adjacency: its entry in each
+ * unmoved neighbour's list becomes -1 (every entry is removed by the thread
+ * of the body it names, so the stores never collide). */
+__global__ void k_inc_remove(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0 || d.inc_rebuild[wld]) continue;
+    const uint8_t mg = d.moved[g];
+    if (!(mg & kMovedBit) || !(mg & kMovedWasGrid)) continue;
+    const int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
+    const int n = min(d.nbr_cnt[g], d.nbr_cap);
+    for (int k = 0; k < n; ++k) {
+      const int j = lst[k];
+      if (j < 0 || (d.moved[j] & kMovedBit)) continue;
+      int32_t* lj = d.nbr + (size_t)j * d.nbr_cap;
+      const int nj = min(d.nbr_cnt[j], d.nbr_cap);
+      for (int t = 0; t < nj; ++t)
+        if (lj[t] == g) {
+          lj[t] = -1;
+          break;
+        }
+    }
+  }
+}
+
+/* One thread per body re-inserted this frame (all bodies of a rebuilding
+ * world): new fat box, cell and grid membership; counts grid bodies into the
+ * buckets of worlds that search this frame. */
+__global__ void k_inc_refat(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0) continue;
+    const bool rebuild = d.inc_rebuild[wld] != 0;
+    const uint8_t mg = d.moved[g];
+    const bool now = (mg & kMovedNowGrid) != 0;
+    if (mg & kMovedBit) { /* a moved body's grid membership is exactly fat_box's verdict */
+      d.row_mode[g] = now ? 1 : 0;
+      if (now) {
+        double fb[4];
+        int cx = 0, cy = 0;
+        fat_box(d, g, wld, fb, &cx, &cy);
+        for (int k = 0; k < 4; ++k) d.fatk[4 * g + k] = okey(fb[k]);
+        d.cell_x[g] = cx;
+        d.cell_y[g] = cy;
+      }
+    }
+    if (rebuild) d.nbr_cnt[g] = 0; /* unmoved bodies of a rebuilding world keep their fat boxes */
+    if (now && (rebuild || d.inc_moved[wld] > 0))
+      atomicAdd(&d.bucket_cnt[d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld])], 1);
+  }
+}
+
+__global__ void k_inc_scatter(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0 || !d.row_mode[g] || !(d.inc_rebuild[wld] || d.inc_moved[wld] > 0)) continue;
+    const int b = d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld]);
+    const int pos = atomicAdd(&d.bucket_off[b], 1);
+    d.grid_ids[pos] = g;
+  }
+}
+
+__device__ __forceinline__ bool fat_overlap(const uint64_t* a, const uint64_t* b) {
+  return !(b[0] > a[1] || b[1] < a[0]) && !(b[2] > a[3] || b[3] < a[2]);
+}
+
+/* One thread per re-inserted grid body: its new list from the 3x3 cells of
+ * the fat-box grid; in an incremental frame it is also appended to each
+ * unmoved neighbour's list. */
+__global__ void k_inc_query(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0 || !d.row_mode[g]) continue;
+    const bool rebuild = d.inc_rebuild[wld] != 0;
+    if (!rebuild && !(d.moved[g] & kMovedBit)) continue;
+    const int T = d.grid_T[wld], base = d.grid_base[wld];
+    const int cx = d.cell_x[g], cy = d.cell_y[g];
+    uint64_t fg[4];
+    for (int k = 0; k < 4; ++k) fg[k] = d.fatk[4 * g + k];
+    int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
+    int cnt = 0;
+    bool over = false;
+    for (int dy = -1; dy <= 1; ++dy) {
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int ncx = cx + dx, ncy = cy + dy;
+        const int b = base + cell_bucket(ncx, ncy, T);
+        const int k0 = b > 0 ? d.bucket_off[b - 1] : 0, k1 = d.bucket_off[b];
+        for (int k = k0; k < k1; ++k) {
+          const int j = d.grid_ids[k];
+          if (j == g || d.cell_x[j] != ncx || d.cell_y[j] != ncy) continue;
+          if (!fat_overlap(fg, d.fatk + 4 * j)) continue;
+          if (cnt < d.nbr_cap) lst[cnt] = j; else over = true;
+          ++cnt;
+          if (!rebuild && !(d.moved[j] & kMovedBit)) {
+            const int pos = atomicAdd(&d.nbr_cnt[j], 1);
+            if (pos < d.nbr_cap) d.nbr[(size_t)j * d.nbr_cap + pos] = g; else over = true;
+          }
+        }
+      }
+    }
+    d.nbr_cnt[g] = cnt;
+    if (over) atomicOr(&d.counters[kCntOverflow], 4ull);
+  }
+}
+
+/* One thread per grid row i: the entries j < i of its list whose current
+ * boxes overlap, then the world's large bodies j < i.  COUNT also compacts
+ * the list (drops removed entries). */
+template <bool COUNT>
+__global__ void k_inc_rows(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    const int wld = d.body_world[g];
+    if (d.grid_T[wld] == 0 || !d.row_mode[g]) continue;
+    const int off = d.world_body_off[wld];
+    const int n = d.world_body_off[wld + 1] - off;
+    const int q = off + (n - 1 - (g - off));
+    const uint8_t fi = d.flags[g];
+    uint64_t ki[4];
+    ki[0] = d.boxk[4 * g + 0];
+    ki[1] = d.boxk[4 * g + 1];
+    ki[2] = d.boxk[4 * g + 2];
+    ki[3] = d.boxk[4 * g + 3];
+    int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
+    int nl = min(d.nbr_cnt[g], d.nbr_cap);
+    if (COUNT) {
+      int w = 0;
+      for (int k = 0; k < nl; ++k) {
+        const int j = lst[k];
+        if (j >= 0) lst[w++] = j;
+      }
+      if (d.nbr_cnt[g] <= d.nbr_cap) d.nbr_cnt[g] = w;
+      nl = w;
+    }
+    int count = 0;
+    const int out = COUNT ? 0 : d.row_off[q];
+    for (int k = 0; k < nl; ++k) {
+      const int j = lst[k];
+      if (j >= 0 && j < g && pair_overlaps(d, g, j, fi, ki)) {
+        if (!COUNT && out + count < d.pair_cap) {
+          d.pair_a[out + count] = g;
+          d.pair_b[out + count] = j;
+        }
+        ++count;
+      }
+    }
+    const int nlarge = d.large_cnt[wld];
+    for (int k = 0; k < nlarge; ++k) {
+      const int j = d.large_ids[off + k];
+      if (j < g && pair_overlaps(d, g, j, fi, ki)) {
+        if (!COUNT && out + count < d.pair_cap) {
+          d.pair_a[out + count] = g;
+          d.pair_b[out + count] = j;
+        }
+        ++count;
+      }
+    }
+    if (COUNT) d.row_cnt[q] = count;
+  }
+}
+
 /* world_pair_off[w] = row_off[world_body_off[w]] (first row of the world in
  * mirrored order); also records the pair total and overflow. */
 __global__ void k_world_pair_offsets(Dev d) {
@@ -731,6 +1077,142 @@ __device__ __forceinline__ int manifold(const HullView& se, int e, const HullVie
   return 2;
 }
 
+/* ---- circles (Contact.hs:22-40, Contact/Circle.hs, CircleVsHull.hs, GJK.hs) */
+
+__device__ __forceinline__ double dot2(double ax, double ay, double bx, double by) { return ax * bx + ay * by; }
+
+/* crossV2V2 (Linear.hs:135-139): (a x b) x c. */
+__device__ __forceinline__ void cross3(double ax, double ay, double bx, double by, double cx, double cy,
+                                       double* x, double* y) {
+  const double abz = ax * by - ay * bx;
+  *x = -(abz * cy);
+  *y = abz * cx;
+}
+
+/* sameDirection (GJK.hs:137-138): a . b > 0, compared on the integer pipe. */
+__device__ __forceinline__ bool same_dir(double ax, double ay, double bx, double by) {
+  return f_lt(0.0, dot2(ax, ay, bx, by));
+}
+
+/* support (ConvexHull.hs:124-128): the first vertex of largest projection. */
+__device__ __forceinline__ int gjk_support(const HullView& h, double dx, double dy) {
+  int best = 0;
+  double bd = dot2(h.wx[0], h.wy[0], dx, dy);
+  for (int k = 1; k < h.nv; ++k) {
+    const double t = dot2(h.wx[k], h.wy[k], dx, dy);
+    if (f_lt(bd, t)) { bd = t; best = k; }
+  }
+  return best;
+}
+
+/* GJK.closestSimplex (GJK.hs:52-135) from vertex 0 toward (ox, oy): returns
+ * the simplex size (3 = encloses the point), s[0] the vertex added last.  The
+ * reference loop is unbounded; this one gives up after 4 nv + 8 extensions
+ * (a failed search), a bound an ordinary convex hull never reaches. */
+__device__ int gjk_closest(const HullView& h, double ox, double oy, int s[3]) {
+  int n = 1;
+  s[0] = 0;
+  double dx = ox - h.wx[0], dy = oy - h.wy[0];
+  for (int it = 0; it < 4 * h.nv + 8; ++it) {
+    const int a = gjk_support(h, dx, dy);
+    if (n == 1) {
+      if (a == s[0]) return 1;
+      s[1] = s[0];
+      s[0] = a;
+      n = 2;
+      const double abx = h.wx[s[1]] - h.wx[a], aby = h.wy[s[1]] - h.wy[a];
+      const double aox = ox - h.wx[a], aoy = oy - h.wy[a];
+      if (same_dir(abx, aby, aox, aoy)) {
+        cross3(abx, aby, aox, aoy, abx, aby, &dx, &dy);
+      } else {
+        n = 1;
+        dx = aox;
+        dy = aoy;
+      }
+      continue;
+    }
+    if (a == s[0] || a == s[1]) return 2;
+    const int b = s[0], c = s[1];
+    const double ax = h.wx[a], ay = h.wy[a];
+    const double abx = h.wx[b] - ax, aby = h.wy[b] - ay;
+    const double acx = h.wx[c] - ax, acy = h.wy[c] - ay;
+    const double aox = ox - ax, aoy = oy - ay;
+    const double abc = abx * acy - aby * acx;
+    const double abcacx = -(abc * acy), abcacy = abc * acx;
+    const double ababcx = aby * abc, ababcy = -(abx * abc);
+    int mode; /* 0 star, 1 (a, c), 2 enclosed */
+    if (same_dir(abcacx, abcacy, aox, aoy)) mode = same_dir(acx, acy, aox, aoy) ? 1 : 0;
+    else mode = same_dir(ababcx, ababcy, aox, aoy) ? 0 : 2;
+    if (mode == 2) {
+      s[0] = a; s[1] = b; s[2] = c;
+      return 3;
+    }
+    if (mode == 1) {
+      s[0] = a; s[1] = c; n = 2;
+      cross3(acx, acy, aox, aoy, acx, acy, &dx, &dy);
+    } else if (same_dir(abx, aby, aox, aoy)) {
+      s[0] = a; s[1] = b; n = 2;
+      cross3(abx, aby, aox, aoy, abx, aby, &dx, &dy);
+    } else {
+      s[0] = a; n = 1;
+      dx = aox; dy = aoy;
+    }
+  }
+  return n;
+}
+
+/* Circle.contact (Contact/Circle.hs:27-56): a is penetrated, b penetrates. */
+__device__ bool circle_circle(double ax, double ay, double ra, double bx, double by, double rb, double* v) {
+  const double abx = bx - ax, aby = by - ay;
+  const double rab = ra + rb;
+  const double ab_sq = abx * abx + aby * aby;
+  if (!f_le(ab_sq, rab * rab)) return false;
+  const double len = sqrt(ab_sq);
+  const double ux = abx / len, uy = aby / len;
+  const double a1x = ux * ra + ax, a1y = uy * ra + ay;
+  const double b1x = ux * (-rb) + bx, b1y = uy * (-rb) + by;
+  v[0] = ux;
+  v[1] = uy;
+  v[2] = (a1x + b1x) / 2.0;
+  v[3] = (a1y + b1y) / 2.0;
+  v[4] = ra + rb - len;
+  return true;
+}
+
+/* CircleVsHull.generateContacts (CircleVsHull.hs:18-69): the circle
+ * penetrates; one contact at the closest hull point, keyed by the vertex the
+ * simplex ended on; none for a 3-point simplex. */
+__device__ bool circle_hull(double ox, double oy, double r, const HullView& hull, int* feature, double* v) {
+  int s[3];
+  const int n = gjk_closest(hull, ox, oy, s);
+  if (n == 3) return false;
+  double qx, qy;
+  if (n == 1) {
+    qx = hull.wx[s[0]];
+    qy = hull.wy[s[0]];
+  } else { /* closestAlong (CircleVsHull.hs:61-69) */
+    const double ax = hull.wx[s[0]], ay = hull.wy[s[0]];
+    const double aox = ox - ax, aoy = oy - ay;
+    const double abx = hull.wx[s[1]] - ax, aby = hull.wy[s[1]] - ay;
+    const double l = sqrt(abx * abx + aby * aby);
+    const double ux = abx / l, uy = aby / l;
+    const double t = dot2(aox, aoy, ux, uy);
+    qx = ux * t + ax;
+    qy = uy * t + ay;
+  }
+  const double bx = ox - qx, by = oy - qy;
+  const double ab_sq = bx * bx + by * by;
+  if (f_lt(r * r, ab_sq)) return false; /* processSimplex_ (CircleVsHull.hs:44-59) */
+  const double len = sqrt(ab_sq);
+  *feature = s[0];
+  v[0] = -(bx / len);
+  v[1] = -(by / len);
+  v[2] = qx;
+  v[3] = qy;
+  v[4] = r - len;
+  return true;
+}
+
 /* Pairs are processed grouped by the vertex counts of their two hulls, so
  * that the lanes of a warp run SAT loops of the same trip counts (one thread
  * per pair, the warp pays for its longest loop).  The grouping is a
@@ -738,7 +1220,8 @@ __device__ __forceinline__ int manifold(const HullView& se, int e, const HullVie
  * slots, so the results do not depend on it. */
 __device__ __forceinline__ int np_class(const Dev& d, int p) {
   const int ga = d.pair_a[p], gb = d.pair_b[p];
-  const int na = min(d.vert_off[ga + 1] - d.vert_off[ga], 9), nb = min(d.vert_off[gb + 1] - d.vert_off[gb], 9);
+  const int na = max(3, min(d.vert_off[ga + 1] - d.vert_off[ga], 9));
+  const int nb = max(3, min(d.vert_off[gb + 1] - d.vert_off[gb], 9));
   return (na - 3) * 7 + (nb - 3);
 }
 
@@ -801,6 +1284,29 @@ __global__ void k_narrowphase(Dev d) {
     const int p = d.np_perm ? d.np_perm[i] : i;
     const int ga = d.pair_a[p], gb = d.pair_b[p];
     const HullView a = hull_view(d, ga), b = hull_view(d, gb);
+    const double ra = d.radius ? d.radius[ga] : 0.0, rb = d.radius ? d.radius[gb] : 0.0;
+    if (ra > 0.0 || rb > 0.0) { /* Contact.generateContacts (Contact.hs:22-40) */
+      double v[5];
+      int f = 0, fa = 0, fb = 0, flip = 0;
+      bool hit;
+      if (ra > 0.0 && rb > 0.0) {
+        hit = circle_circle(a.wx[0], a.wy[0], ra, b.wx[0], b.wy[0], rb, v);
+      } else if (ra > 0.0) {
+        hit = circle_hull(a.wx[0], a.wy[0], ra, b, &f, v);
+        fb = f;
+      } else {
+        hit = circle_hull(b.wx[0], b.wy[0], rb, a, &f, v);
+        fa = f;
+        flip = 1;
+      }
+      if (hit) {
+        d.slot_feat[2 * p] = fa | (fb << 12) | (flip << 24);
+        double* o = d.slot_val + 5 * (2 * (size_t)p);
+        for (int k = 0; k < 5; ++k) o[k] = v[k];
+      }
+      d.slot_cnt[p] = hit ? 1 : 0;
+      continue;
+    }
     int cnt = 0;
     int e_ab, pen_ab, e_ba, pen_ba;
     double dep_ab, dep_ba;
@@ -1394,53 +1900,94 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
 /* Per-world solver residual after the last sweep: one more improveContactSln
  * pass over the world's contacts that applies nothing (every contact sees the
  * final velocities), reporting sqrt(mean over contacts of the normal and
- * friction amounts it would apply, squared).  One warp per world, fixed
- * summation order. */
-__global__ void k_residual(Dev d) {
+ * friction amounts it would apply, squared).  The squared amounts of one
+ * contact: */
+__device__ __forceinline__ double residual_term(const Dev& d, int c) {
+  const int ga = d.c_ga[c], gb = d.c_gb[c];
+  const double2* cp = reinterpret_cast<const double2*>(d.con + c);
+  double j_n[6], j_f[6];
+  const double2 a0 = cp[0], a1 = cp[1], a2 = cp[2], a3 = cp[3], a4 = cp[4], a5 = cp[5];
+  j_n[0] = a0.x; j_n[1] = a0.y; j_n[2] = a1.x; j_n[3] = a1.y; j_n[4] = a2.x; j_n[5] = a2.y;
+  j_f[0] = a3.x; j_f[1] = a3.y; j_f[2] = a4.x; j_f[3] = a4.y; j_f[4] = a5.x; j_f[5] = a5.y;
+  const double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
+  const double2 b6 = cp[6], b7 = cp[7], b8 = cp[8], b9 = cp[9], b10 = cp[10], b11 = cp[11], b12 = cp[12];
+  const double2 cached = reinterpret_cast<const double2*>(d.lam)[c];
+  const double nwa = -v[2];
+  const double cvx = ((-v[0] + (-(nwa * b7.y))) + v[3]) + (-(v[5] * b8.y));
+  const double cvy = ((-v[1] + nwa * b7.x) + v[4]) + v[5] * b8.x;
+  const double tb = b11.y * (cvx * b9.x + cvy * b9.y);
+  const double bias = b6.x + (f_le(0.0, tb) ? 0.0 : tb);
+  const double ln_new = div_rn(-(dot6(j_n, v) + bias), b10.x, b12.x);
+  const double lf_new = div_rn(-plus_zero(dot6(j_f, v)), b10.y, b12.y);
+  const double ln_apply = f_le(ln_new, -cached.x) ? -cached.x : ln_new;
+  const double thr = (cached.x + ln_apply) * b11.x;
+  const double acc = cached.y + lf_new;
+  const double acc2 = f_lt(thr, acc) ? thr : (f_lt(acc, -thr) ? -thr : acc);
+  const double lf_apply = acc2 - cached.y;
+  return ln_apply * ln_apply + lf_apply * lf_apply;
+}
+
+/* One warp per world (fixed summation order); worlds of `split_from` bodies
+ * or more are left to k_residual_part / k_metric_final. */
+__global__ void k_residual(Dev d, int split_from) {
   const int lane = threadIdx.x & 31;
   const int wld = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (wld >= d.n_worlds) return;
+  if (d.world_body_off[wld + 1] - d.world_body_off[wld] >= split_from) return;
   const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
   double sum = 0.0;
-  for (int c = c0 + lane; c < c1; c += 32) {
-    const int ga = d.c_ga[c], gb = d.c_gb[c];
-    const double2* cp = reinterpret_cast<const double2*>(d.con + c);
-    double j_n[6], j_f[6];
-    const double2 a0 = cp[0], a1 = cp[1], a2 = cp[2], a3 = cp[3], a4 = cp[4], a5 = cp[5];
-    j_n[0] = a0.x; j_n[1] = a0.y; j_n[2] = a1.x; j_n[3] = a1.y; j_n[4] = a2.x; j_n[5] = a2.y;
-    j_f[0] = a3.x; j_f[1] = a3.y; j_f[2] = a4.x; j_f[3] = a4.y; j_f[4] = a5.x; j_f[5] = a5.y;
-    const double v[6] = {d.vx[ga], d.vy[ga], d.w[ga], d.vx[gb], d.vy[gb], d.w[gb]};
-    const double2 b6 = cp[6], b7 = cp[7], b8 = cp[8], b9 = cp[9], b10 = cp[10], b11 = cp[11], b12 = cp[12];
-    const double2 cached = reinterpret_cast<const double2*>(d.lam)[c];
-    const double nwa = -v[2];
-    const double cvx = ((-v[0] + (-(nwa * b7.y))) + v[3]) + (-(v[5] * b8.y));
-    const double cvy = ((-v[1] + nwa * b7.x) + v[4]) + v[5] * b8.x;
-    const double tb = b11.y * (cvx * b9.x + cvy * b9.y);
-    const double bias = b6.x + (f_le(0.0, tb) ? 0.0 : tb);
-    const double ln_new = div_rn(-(dot6(j_n, v) + bias), b10.x, b12.x);
-    const double lf_new = div_rn(-plus_zero(dot6(j_f, v)), b10.y, b12.y);
-    const double ln_apply = f_le(ln_new, -cached.x) ? -cached.x : ln_new;
-    const double thr = (cached.x + ln_apply) * b11.x;
-    const double acc = cached.y + lf_new;
-    const double acc2 = f_lt(thr, acc) ? thr : (f_lt(acc, -thr) ? -thr : acc);
-    const double lf_apply = acc2 - cached.y;
-    sum += ln_apply * ln_apply + lf_apply * lf_apply;
-  }
+  for (int c = c0 + lane; c < c1; c += 32) sum += residual_term(d, c);
   for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
   if (lane == 0) d.world_residual[wld] = c1 > c0 ? sqrt(sum / (2.0 * (c1 - c0))) : 0.0;
 }
 
 /* Per-world maximum penetration depth over the contacts of the last collide.
- * One warp per world. */
-__global__ void k_world_depth(Dev d) {
+ * One warp per world; worlds of `split_from` bodies or more are left to
+ * k_depth_part / k_metric_final. */
+__global__ void k_world_depth(Dev d, int split_from) {
   const int lane = threadIdx.x & 31;
   const int wld = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (wld >= d.n_worlds) return;
+  if (d.world_body_off[wld + 1] - d.world_body_off[wld] >= split_from) return;
   const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
   double m = 0.0;
   for (int c = c0 + lane; c < c1; c += 32) m = fmax(m, d.c_val[5 * (size_t)c + 4]);
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
   if (lane == 0) d.world_depth[wld] = m;
+}
+
+/* The same metrics for one large world over kMetricParts warps: warp k takes
+ * the k-th contiguous chunk of the world's contacts, and k_metric_final
+ * combines the parts in order (a fixed summation order for the residual). */
+constexpr int kMetricParts = 256;
+
+template <bool RESIDUAL>
+__global__ void k_metric_part(Dev d, int wld, double* part) {
+  const int lane = threadIdx.x & 31;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (k >= kMetricParts) return;
+  const int c0 = d.world_contact_off[wld], c1 = d.world_contact_off[wld + 1];
+  const int chunk = (c1 - c0 + kMetricParts - 1) / kMetricParts;
+  const int a = c0 + k * chunk, b = min(c1, a + chunk);
+  double acc = 0.0;
+  for (int c = a + lane; c < b; c += 32) acc = RESIDUAL ? acc + residual_term(d, c) : fmax(acc, d.c_val[5 * (size_t)c + 4]);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_xor_sync(0xffffffffu, acc, o);
+    acc = RESIDUAL ? acc + t : fmax(acc, t);
+  }
+  if (lane == 0) part[k] = acc;
+}
+
+template <bool RESIDUAL>
+__global__ void k_metric_final(Dev d, int wld, const double* part) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = 0.0;
+  for (int k = 0; k < kMetricParts; ++k) acc = RESIDUAL ? acc + part[k] : fmax(acc, part[k]);
+  const int n = d.world_contact_off[wld + 1] - d.world_contact_off[wld];
+  if (RESIDUAL)
+    d.world_residual[wld] = n > 0 ? sqrt(acc / (2.0 * n)) : 0.0;
+  else
+    d.world_depth[wld] = acc;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -56,6 +56,20 @@ class Hull:
     """A convex hull shape given by counter-clockwise local vertices."""
 
     vertices: np.ndarray
+    kind: int = _lib.SHAPE_HULL
+
+
+@dataclass(frozen=True)
+class Circle:
+    """A circle centred on its body's position; crosses the ABI as the one
+    local point (radius, 0)."""
+
+    radius: float
+    kind: int = _lib.SHAPE_CIRCLE
+
+    @property
+    def vertices(self) -> np.ndarray:
+        return np.array([[self.radius, 0.0]])
 
 
 @dataclass(frozen=True)
@@ -114,12 +128,12 @@ def make_rectangle_hull(w: float, h: float) -> Hull:
     return Hull(rectangle_vertices(float(w), float(h)))
 
 
-def make_circle(radius: float):
-    """makeCircle (Engine.hs:53-54): circles are not supported by the GPU step."""
-    raise _lib.ShapesError(_lib.SHAPES_E_UNSUPPORTED, "make_circle")
+def make_circle(radius: float) -> Circle:
+    """makeCircle (Engine.hs:53-54) = CircleShape . circleWithRadius."""
+    return Circle(float(radius))
 
 
-def make_world_obj(phys_obj: PhysicalObj, mu: float, bounce: float, shape: Hull, label=None) -> WorldObj:
+def make_world_obj(phys_obj: PhysicalObj, mu: float, bounce: float, shape: "Hull | Circle", label=None) -> WorldObj:
     """makeWorldObj (World.hs:142-149)."""
     return WorldObj(phys_obj, label, float(mu), float(bounce), shape)
 
@@ -137,7 +151,7 @@ def make_constant_accel(accel) -> ConstantAccel:
 def _upload(world: World) -> _lib.Batch:
     n = len(world.objs)
     bodies = {f: np.empty(n) for f in _lib.BODY_FIELDS}
-    verts, vo = [], [0]
+    verts, vo, kinds = [], [0], []
     for k, o in enumerate(world.objs):
         p = o.phys_obj
         vals = (p.vel[0], p.vel[1], p.rot_vel, p.pos[0], p.pos[1], p.rot, p.inv_mass[0], p.inv_mass[1],
@@ -146,8 +160,9 @@ def _upload(world: World) -> _lib.Batch:
             bodies[f][k] = v
         verts.append(o.shape.vertices)
         vo.append(vo[-1] + len(o.shape.vertices))
+        kinds.append(o.shape.kind)
     return _lib.Batch(np.array([0, n], dtype=np.int32), bodies, np.asarray(vo, dtype=np.int32),
-                      np.concatenate(verts, axis=0))
+                      np.concatenate(verts, axis=0), np.asarray(kinds, dtype=np.uint8))
 
 
 def init_engine(scene: Scene) -> EngineState:

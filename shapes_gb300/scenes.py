@@ -12,8 +12,11 @@ A scene is a dict with
   world_body_offsets  int32[W+1]
   bodies              dict of ten float64[N] arrays (shapes_bodies fields)
   vert_offsets        int32[N+1]
-  local_xy            float64[V, 2]  (counter-clockwise hull vertices)
+  local_xy            float64[V, 2]  (counter-clockwise hull vertices; a
+                      circle is one point (radius, 0))
   config              dict(dt, baumgarte, slop, accel, iterations, steps)
+  shape_kind          uint8[N] SHAPE_HULL / SHAPE_CIRCLE (only when the
+                      scene holds circles)
 """
 from __future__ import annotations
 
@@ -21,7 +24,7 @@ import math
 
 import numpy as np
 
-from ._lib import BODY_FIELDS
+from ._lib import BODY_FIELDS, SHAPE_CIRCLE, SHAPE_HULL
 
 DEFAULT_MU = 0.2
 DEFAULT_BOUNCE = 0.0
@@ -63,6 +66,7 @@ class SceneBuilder:
     def __init__(self):
         self.rows = {f: [] for f in BODY_FIELDS}
         self.verts: list[np.ndarray] = []
+        self.kinds: list[int] = []
         self.world_off = [0]
 
     def add(self, xy, pos, rot=0.0, vel=(0.0, 0.0), rot_vel=0.0, mass=None, inertia=None,
@@ -82,6 +86,23 @@ class SceneBuilder:
         for f in BODY_FIELDS:
             self.rows[f].append(float(vals[f]))
         self.verts.append(xy)
+        self.kinds.append(SHAPE_HULL)
+
+    def add_circle(self, radius, pos, rot=0.0, vel=(0.0, 0.0), rot_vel=0.0, mass=1.0, inertia=None,
+                   mu=DEFAULT_MU, bounce=DEFAULT_BOUNCE, static=False):
+        """A circle: one local point (radius, 0), the library's convention for
+        makeCircle (Engine.hs:53-54).  Inertia defaults to a uniform disc's."""
+        if static:
+            iml = imr = 0.0
+        else:
+            i = 0.5 * mass * radius * radius if inertia is None else inertia
+            iml, imr = to_inv_mass(mass), to_inv_mass(i)
+        vals = dict(vel_x=vel[0], vel_y=vel[1], rot_vel=rot_vel, pos_x=pos[0], pos_y=pos[1], rot=rot,
+                    inv_mass_lin=iml, inv_mass_rot=imr, mu=mu, bounce=bounce)
+        for f in BODY_FIELDS:
+            self.rows[f].append(float(vals[f]))
+        self.verts.append(np.array([[float(radius), 0.0]]))
+        self.kinds.append(SHAPE_CIRCLE)
 
     def end_world(self):
         self.world_off.append(len(self.verts))
@@ -91,13 +112,16 @@ class SceneBuilder:
             self.end_world()
         vo = np.zeros(len(self.verts) + 1, dtype=np.int32)
         vo[1:] = np.cumsum([len(v) for v in self.verts])
-        return dict(
+        scene = dict(
             world_body_offsets=np.asarray(self.world_off, dtype=np.int32),
             bodies={f: np.asarray(v, dtype=np.float64) for f, v in self.rows.items()},
             vert_offsets=vo,
             local_xy=np.concatenate(self.verts, axis=0),
             config=config,
         )
+        if SHAPE_CIRCLE in self.kinds:
+            scene["shape_kind"] = np.asarray(self.kinds, dtype=np.uint8)
+        return scene
 
 
 def box_grid_world(b: SceneBuilder, rng, cols=20, rows=20, spacing=1.05, bottom=0.55, jitter=0.05,
@@ -300,10 +324,11 @@ def batched_mixed(seed: int = 3, n_worlds: int = 1024, n_bodies: int = 256, step
 
 
 def container_world(seed: int = 4, n: int = 262144, width: float = 1024.0, rmin=0.3, rmax=1.0,
-                    steps: int = 2000) -> dict:
+                    steps: int = 2000, circle_fraction: float = 0.0) -> dict:
     """One world: a static U container `width` wide (floor + two walls) holding
     n mixed convex polygons (3-8 vertices, radius U[rmin,rmax]) dropped from a
-    jittered grid; dt = 1/120."""
+    jittered grid; dt = 1/120.  With circle_fraction > 0 that share of the
+    bodies are circles of radius U[rmin,rmax] instead (mass from area)."""
     rng = np.random.default_rng(seed)
     b = SceneBuilder()
     b.add(rectangle_vertices(width + 4.0, 2.0), (0.0, -1.0), static=True)
@@ -315,6 +340,11 @@ def container_world(seed: int = 4, n: int = 262144, width: float = 1024.0, rmin=
     left = -pitch * (cols - 1) / 2.0
     for k in range(n - 3):
         c, r = k % cols, k // cols
+        if circle_fraction > 0.0 and rng.random() < circle_fraction:
+            rad = float(rng.uniform(rmin, rmax))
+            b.add_circle(rad, (left + c * pitch + rng.uniform(-0.02, 0.02), pitch * (r + 0.5)),
+                         mass=math.pi * rad * rad)
+            continue
         xy = perturbed_polygon(rng, int(rng.integers(3, 9)), float(rng.uniform(rmin, rmax)))
         b.add(xy, (left + c * pitch + rng.uniform(-0.02, 0.02), pitch * (r + 0.5)), rng.uniform(0, 2 * np.pi))
     b.end_world()
@@ -343,6 +373,109 @@ def stacks_make_scene(dims=(30, 30), spacing=0.0) -> dict:
     return b.build(dt=0.01, baumgarte=0.01, slop=0.02, accel=(0.0, -2.0), iterations=2, steps=10)
 
 
+def balls_make_scene(dims=(10, 10), diameter=1.0, spacing=0.0) -> dict:
+    """Balls.makeScene (Scenes/Balls.hs:61-64): the 18x1 static floor at
+    (0,-6), then dims[0] columns from left to right alternating a stack of
+    dims[1] circles of the given diameter (friction 0.2, bounce 0.5) and a
+    stack of diameter-sized boxes (friction 0.2, bounce 0), every body mass 2
+    and inertia 1 (Stacks.box, Scenes/Stacks.hs:16-17), gravity (0,-2) and
+    contactBehavior (0.01, 0.02), run like Stacks at dt 0.01 with 2 sweeps."""
+    b = SceneBuilder()
+    b.add(rectangle_vertices(18.0, 1.0), (0.0, -6.0), static=True)
+    n_w, n_h = dims
+    left = 0.0 - (diameter * float(n_w - 1) / 2.0)
+    circles = True
+    for _ in range(n_w):
+        y = -4.5
+        for _ in range(n_h):
+            if circles:
+                b.add_circle(diameter / 2.0, (left, y), mass=2.0, inertia=1.0, mu=0.2, bounce=0.5)
+            else:
+                b.add(rectangle_vertices(diameter, diameter), (left, y), mass=2.0, inertia=1.0)
+            y = y + (diameter + spacing)
+        left = left + diameter
+        circles = not circles
+    b.end_world()
+    return b.build(dt=0.01, baumgarte=0.01, slop=0.02, accel=(0.0, -2.0), iterations=2, steps=10)
+
+
+def batched_balls(seed: int = 5, n_worlds: int = 256, n_bodies: int = 128, steps: int = 300,
+                  circle_fraction: float = 0.5) -> dict:
+    """Many worlds of circles and polygons dropped into a static U container.
+
+    Each world: a floor and two walls (static, friction 0.2), then
+    n_bodies - 3 bodies on a jittered grid above the floor, each a circle
+    (radius U[0.25,0.5], bounce U[0,0.5]) with probability circle_fraction,
+    else a perturbed 3-8 vertex polygon (radius U[0.3,0.5], vertex radii
+    +-10%, random rotation, bounce 0); density 1, friction U[0.2,0.6], small
+    random velocities and spins; dt 1/60, 8 sweeps, gravity (0,-9.8)."""
+    rng = np.random.default_rng(seed)
+    nb = n_bodies - 3
+    total = n_worlds * nb
+    cols = max(1, int(math.ceil(math.sqrt(nb))))
+    width = cols * 1.1 + 1.0
+    circ = rng.uniform(size=total) < circle_fraction
+    cr = rng.uniform(0.25, 0.5, size=total)
+    pr = rng.uniform(0.3, 0.5, size=total)
+    nv = np.where(circ, 1, rng.integers(3, 9, size=total))
+    start = np.zeros(total + 1, dtype=np.int64)
+    start[1:] = np.cumsum(nv)
+    owner = np.repeat(np.arange(total), nv)
+    k = np.arange(start[-1]) - start[owner]
+    ang = 2.0 * np.pi * k / nv[owner]
+    rad = pr[owner] * rng.uniform(0.9, 1.1, size=start[-1])
+    x = np.where(circ[owner], cr[owner], rad * np.cos(ang))
+    y = np.where(circ[owner], 0.0, rad * np.sin(ang))
+    nxt = np.arange(start[-1]) + 1
+    nxt[start[1:] - 1] = start[:-1]
+    x1, y1 = x[nxt], y[nxt]
+    crs = x * y1 - x1 * y
+    area = np.where(circ, math.pi * cr * cr, 0.5 * np.bincount(owner, crs, minlength=total))
+    inertia = np.where(circ, 0.5 * math.pi * cr ** 4,
+                       np.bincount(owner, crs * (x * x + x * x1 + x1 * x1 + y * y + y * y1 + y1 * y1),
+                                   minlength=total) / 12.0)
+    j = np.tile(np.arange(nb), n_worlds)
+    px = -(width / 2.0) + 1.0 + (j % cols) * 1.1 + rng.uniform(-0.05, 0.05, size=total)
+    py = 0.8 + (j // cols) * 1.1 + rng.uniform(-0.05, 0.05, size=total)
+    n = n_worlds * n_bodies
+    is_static = (np.arange(n) % n_bodies) < 3
+    body_pos = np.flatnonzero(~is_static)
+    f = {kk: np.zeros(n) for kk in BODY_FIELDS}
+    f["pos_x"][body_pos], f["pos_y"][body_pos] = px, py
+    f["rot"][body_pos] = np.where(circ, 0.0, rng.uniform(-math.pi, math.pi, size=total))
+    f["vel_x"][body_pos] = rng.uniform(-0.5, 0.5, size=total)
+    f["vel_y"][body_pos] = rng.uniform(-0.5, 0.5, size=total)
+    f["rot_vel"][body_pos] = rng.uniform(-1.0, 1.0, size=total)
+    f["inv_mass_lin"][body_pos] = 1.0 / area
+    f["inv_mass_rot"][body_pos] = 1.0 / inertia
+    f["mu"][body_pos] = rng.uniform(0.2, 0.6, size=total)
+    f["bounce"][body_pos] = np.where(circ, rng.uniform(0.0, 0.5, size=total), DEFAULT_BOUNCE)
+    base = np.arange(n_worlds) * n_bodies
+    f["pos_y"][base] = -0.5
+    f["pos_x"][base + 1] = -(width / 2.0) - 0.5
+    f["pos_x"][base + 2] = (width / 2.0) + 0.5
+    f["pos_y"][base + 1] = f["pos_y"][base + 2] = 20.0
+    for q in range(3):
+        f["mu"][base + q] = DEFAULT_MU
+    fnv = np.full(n, 4, dtype=np.int64)
+    fnv[body_pos] = nv
+    fvo = np.zeros(n + 1, dtype=np.int64)
+    fvo[1:] = np.cumsum(fnv)
+    verts = np.zeros((int(fvo[-1]), 2))
+    dst = fvo[body_pos][owner] + k
+    verts[dst, 0], verts[dst, 1] = x, y
+    for q, rect in enumerate((rectangle_vertices(width + 2.0, 1.0), rectangle_vertices(1.0, 40.0),
+                              rectangle_vertices(1.0, 40.0))):
+        for v in range(4):
+            verts[fvo[base + q] + v] = rect[v]
+    kinds = np.full(n, SHAPE_HULL, dtype=np.uint8)
+    kinds[body_pos[circ]] = SHAPE_CIRCLE
+    scene = assemble(np.full(n_worlds, n_bodies), f, verts, fnv, dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE,
+                     slop=DEFAULT_SLOP, accel=(0.0, -9.8), iterations=8, steps=steps)
+    scene["shape_kind"] = kinds
+    return scene
+
+
 def subset_worlds(scene: dict, worlds) -> dict:
     """A scene holding only the given worlds of `scene` (in the given order)."""
     off = scene["world_body_offsets"]
@@ -354,6 +487,9 @@ def subset_worlds(scene: dict, worlds) -> dict:
     new_vo = np.zeros(len(b_idx) + 1, dtype=np.int32)
     new_vo[1:] = np.cumsum(counts)
     xy = np.concatenate([scene["local_xy"][vo[b]:vo[b + 1]] for b in b_idx], axis=0)
-    return dict(world_body_offsets=new_off,
-                bodies={f: scene["bodies"][f][b_idx].copy() for f in BODY_FIELDS},
-                vert_offsets=new_vo, local_xy=xy, config=dict(scene["config"]))
+    out = dict(world_body_offsets=new_off,
+               bodies={f: scene["bodies"][f][b_idx].copy() for f in BODY_FIELDS},
+               vert_offsets=new_vo, local_xy=xy, config=dict(scene["config"]))
+    if "shape_kind" in scene:
+        out["shape_kind"] = scene["shape_kind"][b_idx].copy()
+    return out

@@ -32,7 +32,8 @@ def max_rel_err(a, b) -> float:
 
 
 def batch_from_scene(scene) -> _lib.Batch:
-    return _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"])
+    return _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"],
+                      scene.get("shape_kind"))
 
 
 def config_of(scene, iterations=None, warm_start=True, external=True) -> _lib.Config:

@@ -272,7 +272,7 @@ def test_invalid_inputs_are_rejected():
     kinds[2] = 1
     with pytest.raises(_lib.ShapesError) as e:
         _lib.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], sc["local_xy"], kinds)
-    assert e.value.status == _lib.SHAPES_E_UNSUPPORTED
+    assert e.value.status == _lib.SHAPES_E_INVALID_ARG  # a 4-vertex body marked as a circle
     b = batch_from_scene(bad)
     cfg = config_of(sc)
     cfg.iterations = -1

@@ -237,3 +237,72 @@ def test_world_mutation_slots(O):
     assert w.append(body, box) == n0  # none free: a new slot
     assert list(w.active()) == [1] * (n0 + 1)
     step(5)
+
+
+def _collide_two(O, first, second):
+    """A two-body world (body 0 = `first`, body 1 = `second`, each a tuple
+    ('circle', radius, centre) or ('box', (w, h), centre)); returns the
+    contacts of pair (1, 0)."""
+    b = scenes.SceneBuilder()
+    for kind, size, centre in (first, second):
+        if kind == "circle":
+            b.add_circle(size, centre)
+        else:
+            b.add(scenes.rectangle_vertices(*size), centre)
+    sc = b.build(dt=0.01, baumgarte=0.01, slop=0.02, accel=(0.0, 0.0), iterations=2, steps=1)
+    w = O.world_from_scene(sc)
+    w.collide()
+    return w.contacts()
+
+
+def test_circle_circle_contact(O):
+    """Circle.contact (Contact/Circle.hs:27-56) on pair (1, 0): body 1 is the
+    penetrated circle; key (0, 0), not flipped; normal from 1 toward 0, the
+    midpoint of the two rims, depth ra + rb - distance."""
+    keys, vals = _collide_two(O, ("circle", 1.0, (1.5, 0.0)), ("circle", 1.0, (0.0, 0.0)))
+    assert [list(k) for k in keys] == [[1, 0, 0, 0, 0]]
+    assert list(vals[0]) == [1.0, 0.0, 0.75, 0.0, 0.5]
+    # boxes overlap, circles do not: a pair without contacts
+    keys, _ = _collide_two(O, ("circle", 1.0, (1.5, 1.5)), ("circle", 1.0, (0.0, 0.0)))
+    assert len(keys) == 0
+
+
+def test_circle_hull_contacts_follow_gjk(O):
+    """CircleVsHull (CircleVsHull.hs:18-69) on the points of the reference's
+    GJK benchmark (bench/Physics/Contact/GJK/Benchmark.hs: a 1.9 box and the
+    points (1, 1), (0, 1), (0, 0.9)): a vertex simplex, an edge simplex, and an
+    enclosing simplex that gives no contact."""
+    box = ("box", (1.9, 1.9), (0.0, 0.0))
+    # (1, 1): closest to vertex 0 (0.95, 0.95) - a one-point simplex
+    keys, vals = _collide_two(O, box, ("circle", 0.1, (1.0, 1.0)))
+    assert [list(k) for k in keys] == [[1, 0, 0, 0, 0]]
+    nx, ny, px, py, depth = vals[0]
+    assert (px, py) == (0.95, 0.95)
+    assert nx == pytest.approx(-math.sqrt(0.5), abs=1e-12) and ny == pytest.approx(-math.sqrt(0.5), abs=1e-12)
+    assert depth == pytest.approx(0.1 - math.hypot(0.05, 0.05), abs=1e-12)
+    # (0, 1): the top edge, ending on vertex 1 (-0.95, 0.95)
+    keys, vals = _collide_two(O, box, ("circle", 0.1, (0.0, 1.0)))
+    assert [list(k) for k in keys] == [[1, 0, 0, 1, 0]]
+    nx, ny, px, py, depth = vals[0]
+    assert (nx, ny, px) == (0.0, -1.0, 0.0) and py == pytest.approx(0.95, abs=1e-15)
+    assert depth == pytest.approx(0.05, abs=1e-12)
+    # (0, 0.9): inside the box - the reference leaves deep overlap unhandled
+    keys, _ = _collide_two(O, box, ("circle", 0.1, (0.0, 0.9)))
+    assert len(keys) == 0
+    # hull first in the pair: the same contact, flipped, keyed (feature, 0)
+    keys, vals2 = _collide_two(O, ("circle", 0.1, (0.0, 1.0)), box)
+    assert [list(k) for k in keys] == [[1, 0, 1, 0, 1]]
+    assert list(vals2[0]) == list(vals[0])
+
+
+def test_balls_scene_settles(O):
+    """Balls.makeScene (Scenes/Balls.hs:61-64): alternating circle and box
+    stacks on the floor stay finite and come to rest on it."""
+    sc = scenes.balls_make_scene((4, 4), 1.0, 0.0)
+    w = O.world_from_scene(sc)
+    cfg = sc["config"]
+    w.step(cfg["dt"], cfg["baumgarte"], cfg["slop"], cfg["accel"], cfg["iterations"], nsteps=400)
+    b = w.bodies()
+    assert np.isfinite(b["pos_y"]).all()
+    assert (b["pos_y"][1:] > -5.6).all() and (b["pos_y"][1:] < 0.0).all()
+    assert len(w.contacts()[0]) >= 16
