@@ -725,23 +725,21 @@ __global__ void k_inc_mark(Dev d) {
     if (d.grid_T[wld] == 0) continue;
     const bool rebuild = d.inc_state[wld] == 0;
     const bool was = !rebuild && d.row_mode[g];
-    double fb[4];
-    int cx, cy;
-    const bool fits = fat_box(d, g, wld, fb, &cx, &cy);
-    bool moved, now;
-    if (rebuild) {
-      moved = true;
-      now = fits;
-    } else if (was) {
+    bool inside = false;
+    if (was) {
       const uint64_t* f = d.fatk + 4 * g;
-      const uint64_t* b = d.boxk + 4 * g;
-      const bool inside = !(d.flags[g] & kFlagBoxNaN) && f[0] <= b[0] && b[1] <= f[1] && f[2] <= b[2] && b[3] <= f[3];
-      moved = !inside;
-      now = inside || fits;
-    } else {
-      moved = fits;
-      now = fits;
+      const ulonglong2 b01 = *reinterpret_cast<const ulonglong2*>(d.boxk + 4 * g);
+      const ulonglong2 b23 = *reinterpret_cast<const ulonglong2*>(d.boxk + 4 * g + 2);
+      inside = !(d.flags[g] & kFlagBoxNaN) && f[0] <= b01.x && b01.y <= f[1] && f[2] <= b23.x && b23.y <= f[3];
     }
+    bool fits = false;
+    if (!inside) { /* only a body that is not staying needs the fat-box verdict */
+      double fb[4];
+      int cx, cy;
+      fits = fat_box(d, g, wld, fb, &cx, &cy);
+    }
+    const bool moved = rebuild || (!inside && (was || fits));
+    const bool now = inside || fits;
     d.moved[g] = (moved ? kMovedBit : 0) | (was ? kMovedWasGrid : 0) | (now ? kMovedNowGrid : 0);
     if (moved && !rebuild) atomicAdd(&d.inc_moved[wld], 1);
     if (!now) {
@@ -1654,6 +1652,8 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item, int ga, 
  * of the other warps on the SM. */
 constexpr int kMaxGroupWorlds = 32;
 
+constexpr int kScanBlock = 8;
+
 __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int external, double ax, double ay,
                                  double dt, int n_groups, int smem_last_per_warp) {
   extern __shared__ __align__(16) int32_t s_dyn[];
@@ -1694,9 +1694,7 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
   /* 2b. lane l scans world l */
   int my_depth = 0, my_items = 0, my_hits = 0;
   size_t my_region = 0;
-  int pass = iterations + 1, c = 0, c0 = 0, c1 = 0;
-  uint8_t info_n = 0;
-  int ga_n = 0, gb_n = 0;
+  int c0 = 0, c1 = 0;
   int32_t* last = d.last;
   if (lane < nw) {
     const int wld = d.group_worlds[o0 + lane];
@@ -1710,49 +1708,59 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
     c0 = d.world_contact_off[wld];
     c1 = d.world_contact_off[wld + 1];
     my_region = (size_t)stride * c0;
-    pass = warm_start ? 0 : 1;
-    c = c0;
-    if (c0 < c1) {
-      info_n = d.c_hit[c0];
-      ga_n = d.c_ga[c0];
-      gb_n = d.c_gb[c0];
-    } else {
-      pass = iterations + 1;
+  }
+  /* Sequential scan of this lane's world, pass by pass.  The only
+   * loop-carried dependency is through last[]; contacts are read in blocks of
+   * kScanBlock and the next block is loaded while the current one is
+   * processed, so the global-load latency hides behind kScanBlock updates of
+   * shared-memory work (loads past the world's end are clamped to its last
+   * contact and never used). */
+  if (lane < nw && c0 < c1) {
+    for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
+      uint8_t inf[kScanBlock];
+      int ia[kScanBlock], ib[kScanBlock];
+#pragma unroll
+      for (int k = 0; k < kScanBlock; ++k) {
+        const int cc = min(c0 + k, c1 - 1);
+        inf[k] = d.c_hit[cc];
+        ia[k] = d.c_ga[cc];
+        ib[k] = d.c_gb[cc];
+      }
+      for (int cb = c0; cb < c1; cb += kScanBlock) {
+        uint8_t inf2[kScanBlock];
+        int ia2[kScanBlock], ib2[kScanBlock];
+#pragma unroll
+        for (int k = 0; k < kScanBlock; ++k) {
+          const int cc = min(cb + kScanBlock + k, c1 - 1);
+          inf2[k] = d.c_hit[cc];
+          ia2[k] = d.c_ga[cc];
+          ib2[k] = d.c_gb[cc];
+        }
+#pragma unroll
+        for (int k = 0; k < kScanBlock; ++k) {
+          const int cur_c = cb + k;
+          const uint8_t info = inf[k];
+          if (cur_c < c1 && !(pass == 0 && !(info & kInfoHit))) {
+            const int ga = ia[k], gb = ib[k];
+            const bool da = info & kInfoDynA, db = info & kInfoDynB;
+            const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
+            const int lvl = (la > lb ? la : lb) + 1;
+            if (da) last[ga] = lvl;
+            if (db) last[gb] = lvl;
+            d.idesc[my_region + my_items] =
+                make_int4((int)((uint32_t)cur_c | (pass == 0 ? kWarmBit : 0u)), ga, gb, (int)info | (lane << 8));
+            d.ilevel[my_region + my_items] = lvl;
+            ++my_items;
+            my_depth = lvl > my_depth ? lvl : my_depth;
+            my_hits += pass == 0;
+          }
+          inf[k] = inf2[k];
+          ia[k] = ia2[k];
+          ib[k] = ib2[k];
+        }
+      }
     }
   }
-  /* Sequential scan of this lane's world while pass <= pass_end.  The only
-   * loop-carried dependency is through last[]; the next contact's info and
-   * bodies are loaded one iteration ahead so their latency hides behind the
-   * current update's shared-memory work. */
-  auto scan_until = [&](int pass_end) {
-    if (lane >= nw) return;
-    while (pass <= pass_end) {
-      const uint8_t info = info_n;
-      const int ga = ga_n, gb = gb_n, cur_c = c, cur_pass = pass;
-      if (++c == c1) {
-        c = c0;
-        ++pass;
-      }
-      if (pass <= iterations) {
-        info_n = d.c_hit[c];
-        ga_n = d.c_ga[c];
-        gb_n = d.c_gb[c];
-      }
-      if (cur_pass == 0 && !(info & kInfoHit)) continue;
-      const bool da = info & kInfoDynA, db = info & kInfoDynB;
-      const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
-      const int lvl = (la > lb ? la : lb) + 1;
-      if (da) last[ga] = lvl;
-      if (db) last[gb] = lvl;
-      d.idesc[my_region + my_items] =
-          make_int4((int)((uint32_t)cur_c | (cur_pass == 0 ? kWarmBit : 0u)), ga, gb, (int)info | (lane << 8));
-      d.ilevel[my_region + my_items] = lvl;
-      ++my_items;
-      my_depth = lvl > my_depth ? lvl : my_depth;
-      my_hits += cur_pass == 0;
-    }
-  };
-  scan_until(iterations);
   if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 1] = clock64();
   /* 3. the group's updates counting-sorted by level into a region of gdesc /
    *    ghist taken from a bump allocator, as packed descriptors, so that a
