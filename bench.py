@@ -545,12 +545,13 @@ def run_ours(args, rank, world, local):
     # ---- roofline of the dominant kernel (profiled pass) -------------------
     solve_ms, solve_launches = prof["solve"]
     items = st_prof["solver_items"]
-    solver_kernel = "k_schedule_solve"
+    solver_kernel = "k_schedule_solve" if not tuned or tuned[2] == 1 else f"k_group_solve<{tuned[2]}>"
+    if args.workload == "container":
+        solver_kernel = "k_lw_color_pass + k_lw_color_seq" if args.coloured else "k_lw_ordered"
     if items == 0 and st_prof["contacts"] > 0:
         # large-world solvers count no items: the last step's contacts x (sweeps + warm-start pass)
         # per profiled step; the stage holds every kernel of the solve (ordered: one launch a step)
         items = st_prof["contacts"] * (run_it + 1) * prof_steps
-        solver_kernel = "k_lw_color_pass + k_lw_color_seq" if args.coloured else "k_lw_ordered"
     peaks = measured_peaks()
     roof = None
     if solve_launches and solve_ms > 0:
@@ -595,7 +596,8 @@ def run_ours(args, rank, world, local):
                        "launch": "CUDA graph per step",
                        "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
                        else "grid, full 3x3 search every frame",
-                       "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1]} if tuned else "default"},
+                       "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
+                                          "warps_per_group": tuned[2]} if tuned else "default"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * n_bodies,
@@ -734,7 +736,7 @@ def main():
     ap.add_argument("--worlds", type=int, default=None, help="override the world count (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the solver-packing autotuner")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
-    ap.add_argument("--tune-steps", type=int, default=4, help="steps per autotuner trial")
+    ap.add_argument("--tune-steps", type=int, default=10, help="steps per autotuner trial")
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")

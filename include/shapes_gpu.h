@@ -214,10 +214,19 @@ int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, in
  * shapes_batch_autotune. */
 int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, int32_t threads);
 
+/* Cooperative groups: 2, 4 or 8 warps share each group (one group per CTA;
+ * the level's updates are spread over all of them, __syncthreads between
+ * levels); 1 (default) = one warp per group, `threads` / 32 groups per CTA.
+ * Results do not depend on it. */
+int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps);
+/* The packing in use (any pointer may be NULL). */
+int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps);
+
 /* Autotuner for the solver packing: from the current state, times
- * `steps_per_trial` steps for each candidate (worlds per warp group x warps
- * per CTA), restores the state exactly after every trial, and keeps the
- * fastest.  The world state and cache are left exactly as they were; results
+ * `steps_per_trial` steps for each candidate (worlds per group x warps per
+ * CTA, and worlds per group x warps per cooperative group) after one untimed
+ * step, restores the state exactly after every trial, and keeps the fastest (read it back with
+ * shapes_batch_get_launch).  The world state and cache are left exactly as they were; results
  * never depend on the packing.  Tune on a state that has contacts (e.g. after
  * the scene settles).  chosen_* may be NULL.  Allocates temporary device
  * memory for the saved state. */

@@ -124,6 +124,8 @@ SIGNATURES = [
     ("shapes_batch_get_world_metrics", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     ("shapes_batch_set_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_launch_groups", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    ("shapes_batch_set_group_warps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_get_launch", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _ip]),
     ("shapes_batch_set_stream", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("shapes_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Config), ctypes.c_int32, _ip, _ip]),
     ("shapes_batch_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
@@ -301,11 +303,21 @@ class Batch:
         check(lib().shapes_batch_get_stats(self._h, ctypes.byref(s)), "shapes_batch_get_stats")
         return {f[0]: getattr(s, f[0]) for f in Stats._fields_}
 
-    def autotune(self, cfg: Config, steps_per_trial: int = 5) -> tuple[int, int]:
-        wpg, thr = ctypes.c_int32(), ctypes.c_int32()
-        check(lib().shapes_batch_autotune(self._h, ctypes.byref(cfg), steps_per_trial, ctypes.byref(wpg),
-                                          ctypes.byref(thr)), "shapes_batch_autotune")
-        return wpg.value, thr.value
+    def autotune(self, cfg: Config, steps_per_trial: int = 5) -> tuple[int, int, int]:
+        """Returns the chosen (worlds per group, threads per CTA, warps per group)."""
+        check(lib().shapes_batch_autotune(self._h, ctypes.byref(cfg), steps_per_trial, None, None),
+              "shapes_batch_autotune")
+        return self.get_launch()
+
+    def get_launch(self) -> tuple[int, int, int]:
+        wpg, thr, gw = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(lib().shapes_batch_get_launch(self._h, ctypes.byref(wpg), ctypes.byref(thr), ctypes.byref(gw)),
+              "shapes_batch_get_launch")
+        return wpg.value, thr.value, gw.value
+
+    def set_group_warps(self, warps: int) -> None:
+        """Warps cooperating on each solver group (1, 2, 4 or 8)."""
+        check(lib().shapes_batch_set_group_warps(self._h, warps), "shapes_batch_set_group_warps")
 
     def set_stream(self, cuda_stream: int | None) -> None:
         check(lib().shapes_batch_set_stream(self._h, ctypes.c_void_p(cuda_stream or None)), "shapes_batch_set_stream")
@@ -319,10 +331,13 @@ class Batch:
         check(lib().shapes_batch_get_profile(self._h, _ptr(ms, _dp), _ptr(n, _lp)), "shapes_batch_get_profile")
         return {name: (float(ms[k]), int(n[k])) for k, name in enumerate(STAGE_NAMES)}
 
-    def set_launch_groups(self, worlds_per_group: int, threads: int) -> None:
-        """Fixed worlds per warp group (what the autotuner chooses)."""
+    def set_launch_groups(self, worlds_per_group: int, threads: int, group_warps: int | None = None) -> None:
+        """Fixed worlds per group (what the autotuner chooses); group_warps > 1
+        makes that many warps share each group."""
         check(lib().shapes_batch_set_launch_groups(self._h, worlds_per_group, threads),
               "shapes_batch_set_launch_groups")
+        if group_warps is not None:
+            self.set_group_warps(group_warps)
 
     def group_clocks(self) -> np.ndarray:
         """Per solver group of the last profiled step: [start, after scan, after sort, end,

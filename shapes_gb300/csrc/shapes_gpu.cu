@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -128,6 +129,7 @@ struct shapes_batch {
   int32_t* inc_state = nullptr;
   int32_t* inc_rebuild = nullptr;
   int32_t* inc_moved = nullptr;
+  int32_t* inc_frames = nullptr;
   double* inc_margin = nullptr;
   int32_t* pair_a = nullptr;
   int32_t* pair_b = nullptr;
@@ -195,6 +197,7 @@ struct shapes_batch {
   int32_t worlds_per_group_override = 0;
   int32_t target_group_bodies = 0;
   int32_t solve_threads = 32;
+  int32_t group_warps = 1; /* > 1: that many warps cooperate on each group (k_group_solve) */
   /* scans */
   int32_t* tile_sums = nullptr;
   int32_t tile_cap = 0;
@@ -393,6 +396,7 @@ struct shapes_batch {
       d.inc_state = inc_state;
       d.inc_rebuild = inc_rebuild;
       d.inc_moved = inc_moved;
+      d.inc_frames = inc_frames;
       d.inc_margin = inc_margin;
       d.nbr_cap = nbr_cap;
     }
@@ -755,12 +759,12 @@ struct shapes_batch {
 
   void free_incremental() {
     dfree(fatk); dfree(nbr); dfree(nbr_cnt); dfree(moved); dfree(inc_state); dfree(inc_rebuild); dfree(inc_moved);
-    dfree(inc_margin);
+    dfree(inc_frames); dfree(inc_margin);
     fatk = nullptr;
     nbr = nullptr;
     nbr_cnt = nullptr;
     moved = nullptr;
-    inc_state = inc_rebuild = inc_moved = nullptr;
+    inc_state = inc_rebuild = inc_moved = inc_frames = nullptr;
     inc_margin = nullptr;
   }
 
@@ -775,6 +779,7 @@ struct shapes_batch {
     inc_state = dalloc<int32_t>(W, "cudaMalloc grid");
     inc_rebuild = dalloc<int32_t>(W, "cudaMalloc grid");
     inc_moved = dalloc<int32_t>(W, "cudaMalloc grid");
+    inc_frames = dalloc<int32_t>(W, "cudaMalloc grid");
     inc_margin = dalloc<double>(W, "cudaMalloc grid");
     reset_incremental();
   }
@@ -933,12 +938,28 @@ struct shapes_batch {
     const int wpc = solve_threads / 32;
     /* each warp's slice of last levels: 40 KB of dynamic shared memory in all (static use is ~1 KB) */
     const int per_warp = std::min<int>(smem_last_cap, (40 * 1024 / (int)sizeof(int32_t)) / wpc) & ~1;
-    if (G > 0)
+    if (G > 0 && group_warps > 1) {
+      /* one group per CTA of group_warps warps, the group's slice up to 40 KB */
+      const int ints = std::min<int>(smem_last_cap, 40 * 1024 / (int)sizeof(int32_t)) & ~1;
+      const size_t bytes = (size_t)ints * sizeof(int32_t);
+      stage(4, 1, [&]() {
+        if (group_warps == 2)
+          shapes::k_group_solve<2><<<G, 64, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
+                                                             cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
+        else if (group_warps == 4)
+          shapes::k_group_solve<4><<<G, 128, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
+                                                              cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
+        else
+          shapes::k_group_solve<8><<<G, 256, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
+                                                              cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
+      });
+    } else if (G > 0) {
       stage(4, 1, [&]() {
         shapes::k_schedule_solve<<<(G + wpc - 1) / wpc, solve_threads, (size_t)wpc * per_warp * sizeof(int32_t),
                                    stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, cfg.accel_x,
                                              cfg.accel_y, cfg.dt, G, per_warp);
       });
+    }
     for (size_t k = 0; k < large_worlds.size(); ++k) solve_large_world(d, k, cfg);
     if ((cfg.flags & SHAPES_FLAG_RESIDUAL) || (learn && judge_set))
       stage(4, 1 + 2 * (int)large_worlds.size(), [&]() { world_metric_kernels(d, true); });
@@ -1685,6 +1706,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     void* slam = keep(b->lam[cache_buf0], sizeof(double) * 2 * n_cache);
     void* scwo = keep(b->cwo[cache_buf0], sizeof(int32_t) * (W + 1));
     const int32_t wpg0 = b->worlds_per_group_override, thr0 = b->solve_threads, tgt0 = b->target_group_bodies;
+    const int32_t gw0 = b->group_warps;
     const bool prof0 = b->profiling;
     b->profiling = false;
     auto restore_state = [&]() {
@@ -1698,24 +1720,32 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->pose(0, 0.0);
     };
     const int base = std::max(1, std::min(shapes::kMaxGroupWorlds, 32 / (cfg->iterations + 1)));
-    std::vector<std::pair<int, int>> cands;
+    /* (worlds per group, threads per CTA, warps per group) */
+    std::vector<std::array<int, 3>> cands;
+    auto add = [&](int wpg, int thr, int gw) {
+      const std::array<int, 3> c{wpg, thr, gw};
+      if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds && std::find(cands.begin(), cands.end(), c) == cands.end())
+        cands.push_back(c);
+    };
     for (int wpg : {1, base / 2, base, base + 1, 2 * base})
-      for (int thr : {32, 64, 128})
-        if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds &&
-            std::find(cands.begin(), cands.end(), std::make_pair(wpg, thr)) == cands.end())
-          cands.emplace_back(wpg, thr);
+      for (int thr : {32, 64, 128}) add(wpg, thr, 1);
+    for (int wpg : {1, base, 2 * base, 3 * base, 4 * base})
+      for (int gw : {2, 4, 8}) add(wpg, 32 * gw, gw);
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     float best = 1e30f;
-    std::pair<int, int> best_c = {wpg0, thr0};
+    std::array<int, 3> best_c{wpg0, thr0, gw0};
     int rc = SHAPES_OK;
     for (const auto& c : cands) {
       restore_state();
-      b->worlds_per_group_override = c.first;
+      b->worlds_per_group_override = c[0];
       b->target_group_bodies = 0;
-      b->solve_threads = c.second;
+      b->solve_threads = c[1];
+      b->group_warps = c[2];
       b->make_groups(cfg->iterations);
+      rc = b->run(*cfg, 1, true); /* untimed: captures this packing's step graphs */
+      if (rc != SHAPES_OK) break;
       ck(cudaEventRecord(e0, b->stream), "event");
       rc = b->run(*cfg, steps_per_trial, true);
       if (rc != SHAPES_OK) break;
@@ -1732,13 +1762,15 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     cudaEventDestroy(e1);
     restore_state();
     if (rc == SHAPES_OK) {
-      b->worlds_per_group_override = best_c.first;
+      b->worlds_per_group_override = best_c[0];
       b->target_group_bodies = 0;
-      b->solve_threads = best_c.second;
+      b->solve_threads = best_c[1];
+      b->group_warps = best_c[2];
     } else {
       b->worlds_per_group_override = wpg0;
       b->target_group_bodies = tgt0;
       b->solve_threads = thr0;
+      b->group_warps = gw0;
     }
     b->make_groups(cfg->iterations);
     ck(cudaStreamSynchronize(b->stream), "sync");
@@ -2265,6 +2297,24 @@ int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, in
     b->make_groups(b->grouped_iterations >= 0 ? b->grouped_iterations : 2);
     return SHAPES_OK;
   });
+}
+
+int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps) {
+  if (!b || (warps != 1 && warps != 2 && warps != 4 && warps != 8)) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->group_warps = warps;
+    b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  if (worlds_per_group) *worlds_per_group = b->worlds_per_group_override;
+  if (threads) *threads = b->solve_threads;
+  if (group_warps) *group_warps = b->group_warps;
+  return SHAPES_OK;
 }
 
 int shapes_batch_set_launch(shapes_batch* b, int32_t target_bodies_per_group, int32_t threads) {

@@ -97,6 +97,7 @@ struct Dev {
   int32_t* inc_state;    /* [W] 0 = rebuild the adjacency next frame, 1 = valid */
   int32_t* inc_rebuild;  /* [W] this frame rebuilds the world's adjacency */
   int32_t* inc_moved;    /* [W] bodies re-inserted this frame */
+  int32_t* inc_frames;   /* [W] consecutive quiet frames of a FULL world */
   double* inc_margin;    /* [W] fat-box margin */
   int32_t nbr_cap;
   int32_t* row_cnt; /* [N] mirrored per-row pair counts */
@@ -632,14 +633,21 @@ __global__ void k_grid_sort_rows(Dev d) {
  * whose box left its fat box (or that changed between grid and large) is
  * "moved": it is removed from its old neighbours' lists, gets a new fat box,
  * searches the 3x3 cells of the fat-box grid (binned only in worlds with
- * moved bodies) and is appended to each unmoved neighbour's list.  A world
- * with more than a quarter of its bodies moved, a new world, and every world
- * after a retry rebuild the whole adjacency.  Large bodies (fat box not
- * small, or a non-finite box) stay on the per-world large list as before.
+ * moved bodies) and is appended to each unmoved neighbour's list.
+ * Each world picks one of three modes per frame: LIST (the above), BUILD
+ * (every grid body searches and the lists are written afresh: a new world,
+ * every world after a retry, and a world coming back from FULL) and FULL
+ * (more than a quarter of the world moved: no lists; the rows search the
+ * 3x3 cells of the fat-box grid directly, like the plain grid rows).  A FULL
+ * world keeps counting the bodies that leave their fat boxes and returns
+ * through BUILD once that share stays below an eighth for four frames.  Large bodies (fat box not small, or a non-finite
+ * box) stay on the per-world large list as before.
  * Rows come out unordered and are sorted like grid rows, so the pair list is
  * exactly the brute-force rows' list.  A list that would exceed nbr_cap sets
  * overflow bit 4 and the host retries with a larger capacity. */
 
+constexpr int kIncList = 0, kIncBuild = 1, kIncFull = 2; /* per-world mode of a frame */
+constexpr int kIncStateNew = 0, kIncStateList = 1, kIncStateFull = 2;
 constexpr uint8_t kMovedBit = 1;     /* re-inserted this frame */
 constexpr uint8_t kMovedWasGrid = 2; /* was in the adjacency before this frame */
 constexpr uint8_t kMovedNowGrid = 4; /* is in the adjacency after this frame */
@@ -735,8 +743,13 @@ __global__ void k_inc_mark(Dev d) {
     bool fits = false;
     if (!inside) { /* only a body that is not staying needs the fat-box verdict */
       double fb[4];
-      int cx, cy;
+      int cx = 0, cy = 0;
       fits = fat_box(d, g, wld, fb, &cx, &cy);
+      if (fits) { /* its new fat box (read by nothing before k_inc_scatter) */
+        for (int k = 0; k < 4; ++k) d.fatk[4 * g + k] = okey(fb[k]);
+        d.cell_x[g] = cx;
+        d.cell_y[g] = cy;
+      }
     }
     const bool moved = rebuild || (!inside && (was || fits));
     const bool now = inside || fits;
@@ -749,14 +762,26 @@ __global__ void k_inc_mark(Dev d) {
   }
 }
 
-/* One thread per world: rebuild when the adjacency is new or more than a
- * quarter of the world moved. */
+/* One thread per world: this frame's mode (inc_rebuild) and the next
+ * frame's state (inc_state). */
 __global__ void k_inc_decide(Dev d) {
   for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < d.n_worlds; w += gridDim.x * blockDim.x) {
     if (d.grid_T[w] == 0) continue;
     const int n = d.world_body_off[w + 1] - d.world_body_off[w];
-    d.inc_rebuild[w] = (d.inc_state[w] == 0 || 4 * d.inc_moved[w] > n) ? 1 : 0;
-    d.inc_state[w] = 1;
+    const int st = d.inc_state[w], moved = d.inc_moved[w];
+    int mode;
+    if (st == kIncStateNew) {
+      mode = kIncBuild;
+    } else if (st == kIncStateList) {
+      mode = 4 * moved > n ? kIncFull : kIncList;
+    } else { /* FULL: back through BUILD after 4 quiet-enough frames */
+      const int quiet = 8 * moved < n ? d.inc_frames[w] + 1 : 0;
+      d.inc_frames[w] = quiet;
+      mode = quiet >= 4 ? kIncBuild : kIncFull;
+    }
+    if (mode == kIncFull && st != kIncStateFull) d.inc_frames[w] = 0;
+    d.inc_rebuild[w] = mode;
+    d.inc_state[w] = mode == kIncFull ? kIncStateFull : kIncStateList;
   }
 }
 
@@ -766,7 +791,7 @@ __global__ void k_inc_decide(Dev d) {
 __global__ void k_inc_remove(Dev d) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
     const int wld = d.body_world[g];
-    if (d.grid_T[wld] == 0 || d.inc_rebuild[wld]) continue;
+    if (d.grid_T[wld] == 0 || d.inc_rebuild[wld] != kIncList) continue;
     const uint8_t mg = d.moved[g];
     if (!(mg & kMovedBit) || !(mg & kMovedWasGrid)) continue;
     const int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
@@ -785,29 +810,20 @@ __global__ void k_inc_remove(Dev d) {
   }
 }
 
-/* One thread per body re-inserted this frame (all bodies of a rebuilding
- * world): new fat box, cell and grid membership; counts grid bodies into the
- * buckets of worlds that search this frame. */
+/* One thread per body: a moved body's grid membership (its fat box and cell
+ * were written by k_inc_mark; a staying body keeps the ones it has, which
+ * still contain its box); counts grid bodies into the buckets of worlds that
+ * search this frame. */
 __global__ void k_inc_refat(Dev d) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
     const int wld = d.body_world[g];
     if (d.grid_T[wld] == 0) continue;
-    const bool rebuild = d.inc_rebuild[wld] != 0;
+    const int mode = d.inc_rebuild[wld];
     const uint8_t mg = d.moved[g];
     const bool now = (mg & kMovedNowGrid) != 0;
-    if (mg & kMovedBit) { /* a moved body's grid membership is exactly fat_box's verdict */
-      d.row_mode[g] = now ? 1 : 0;
-      if (now) {
-        double fb[4];
-        int cx = 0, cy = 0;
-        fat_box(d, g, wld, fb, &cx, &cy);
-        for (int k = 0; k < 4; ++k) d.fatk[4 * g + k] = okey(fb[k]);
-        d.cell_x[g] = cx;
-        d.cell_y[g] = cy;
-      }
-    }
-    if (rebuild) d.nbr_cnt[g] = 0; /* unmoved bodies of a rebuilding world keep their fat boxes */
-    if (now && (rebuild || d.inc_moved[wld] > 0))
+    if (mg & kMovedBit) d.row_mode[g] = now ? 1 : 0;
+    if (mode == kIncBuild) d.nbr_cnt[g] = 0;
+    if (now && (mode != kIncList || d.inc_moved[wld] > 0))
       atomicAdd(&d.bucket_cnt[d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld])], 1);
   }
 }
@@ -815,7 +831,7 @@ __global__ void k_inc_refat(Dev d) {
 __global__ void k_inc_scatter(Dev d) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
     const int wld = d.body_world[g];
-    if (d.grid_T[wld] == 0 || !d.row_mode[g] || !(d.inc_rebuild[wld] || d.inc_moved[wld] > 0)) continue;
+    if (d.grid_T[wld] == 0 || !d.row_mode[g] || !(d.inc_rebuild[wld] != kIncList || d.inc_moved[wld] > 0)) continue;
     const int b = d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld]);
     const int pos = atomicAdd(&d.bucket_off[b], 1);
     d.grid_ids[pos] = g;
@@ -833,8 +849,9 @@ __global__ void k_inc_query(Dev d) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
     const int wld = d.body_world[g];
     if (d.grid_T[wld] == 0 || !d.row_mode[g]) continue;
-    const bool rebuild = d.inc_rebuild[wld] != 0;
-    if (!rebuild && !(d.moved[g] & kMovedBit)) continue;
+    const int mode = d.inc_rebuild[wld];
+    const bool rebuild = mode == kIncBuild;
+    if (mode == kIncFull || (!rebuild && !(d.moved[g] & kMovedBit))) continue;
     const int T = d.grid_T[wld], base = d.grid_base[wld];
     const int cx = d.cell_x[g], cy = d.cell_y[g];
     uint64_t fg[4];
@@ -882,27 +899,50 @@ __global__ void k_inc_rows(Dev d) {
     ki[1] = d.boxk[4 * g + 1];
     ki[2] = d.boxk[4 * g + 2];
     ki[3] = d.boxk[4 * g + 3];
-    int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
-    int nl = min(d.nbr_cnt[g], d.nbr_cap);
-    if (COUNT) {
-      int w = 0;
-      for (int k = 0; k < nl; ++k) {
-        const int j = lst[k];
-        if (j >= 0) lst[w++] = j;
-      }
-      if (d.nbr_cnt[g] <= d.nbr_cap) d.nbr_cnt[g] = w;
-      nl = w;
-    }
     int count = 0;
     const int out = COUNT ? 0 : d.row_off[q];
-    for (int k = 0; k < nl; ++k) {
-      const int j = lst[k];
-      if (j >= 0 && j < g && pair_overlaps(d, g, j, fi, ki)) {
-        if (!COUNT && out + count < d.pair_cap) {
-          d.pair_a[out + count] = g;
-          d.pair_b[out + count] = j;
+    if (d.inc_rebuild[wld] == kIncFull) { /* no lists: the 3x3 cells of the fat-box grid */
+      const int T = d.grid_T[wld], base = d.grid_base[wld];
+      const int cx = d.cell_x[g], cy = d.cell_y[g];
+      for (int dy = -1; dy <= 1; ++dy) {
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int ncx = cx + dx, ncy = cy + dy;
+          const int b = base + cell_bucket(ncx, ncy, T);
+          const int k0 = b > 0 ? d.bucket_off[b - 1] : 0, k1 = d.bucket_off[b];
+          for (int k = k0; k < k1; ++k) {
+            const int j = d.grid_ids[k];
+            if (j >= g || d.cell_x[j] != ncx || d.cell_y[j] != ncy) continue;
+            if (pair_overlaps(d, g, j, fi, ki)) {
+              if (!COUNT && out + count < d.pair_cap) {
+                d.pair_a[out + count] = g;
+                d.pair_b[out + count] = j;
+              }
+              ++count;
+            }
+          }
         }
-        ++count;
+      }
+    } else {
+      int32_t* lst = d.nbr + (size_t)g * d.nbr_cap;
+      int nl = min(d.nbr_cnt[g], d.nbr_cap);
+      if (COUNT) {
+        int w = 0;
+        for (int k = 0; k < nl; ++k) {
+          const int j = lst[k];
+          if (j >= 0) lst[w++] = j;
+        }
+        if (d.nbr_cnt[g] <= d.nbr_cap) d.nbr_cnt[g] = w;
+        nl = w;
+      }
+      for (int k = 0; k < nl; ++k) {
+        const int j = lst[k];
+        if (j >= 0 && j < g && pair_overlaps(d, g, j, fi, ki)) {
+          if (!COUNT && out + count < d.pair_cap) {
+            d.pair_a[out + count] = g;
+            d.pair_b[out + count] = j;
+          }
+          ++count;
+        }
       }
     }
     const int nlarge = d.large_cnt[wld];
@@ -1897,6 +1937,258 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
     }
   }
   if (d.phase_clock && lane == 0) {
+    d.phase_clock[8 * grp + 3] = clock64();
+    d.phase_clock[8 * grp + 4] = max_depth;
+    d.phase_clock[8 * grp + 5] = tot_items;
+    d.phase_clock[8 * grp + 6] = group_bodies;
+    d.phase_clock[8 * grp + 7] = nw;
+  }
+}
+
+/* The same schedule and solve with P warps per group (one group per CTA of
+ * 32 P threads).  A group's worlds are scanned by P warps at once (world k by
+ * lane k / P of warp k % P), the counting sort and the level loop use all
+ * 32 P threads, and __syncthreads separates the levels.  Updates of one level
+ * touch disjoint dynamic bodies, so splitting a level over more threads
+ * changes nothing in the results; it lets the host pack more worlds into a
+ * group (fuller FP64 instructions: one warp instruction serves 32 updates)
+ * without lengthening each warp's share of a level. */
+template <int P>
+__global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, int warm_start, int external,
+                                                        double ax, double ay, double dt, int n_groups,
+                                                        int smem_ints) {
+  constexpr int NT = 32 * P;
+  extern __shared__ __align__(16) int32_t s_dyn[];
+  __shared__ int32_t s_delta[kMaxGroupWorlds];
+  __shared__ int32_t s_nitems[kMaxGroupWorlds];
+  __shared__ unsigned long long s_region[kMaxGroupWorlds];
+  __shared__ int32_t s_red[3][P];
+  __shared__ int32_t s_gbase;
+  if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
+  const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+  const int grp = blockIdx.x;
+  if (grp >= n_groups) return;
+  const int o0 = d.group_world_off[grp], o1 = d.group_world_off[grp + 1];
+  const int nw = o1 - o0;
+  const int stride = iterations + 1;
+  int32_t* s_last = s_dyn;
+  if (d.phase_clock && tid == 0) d.phase_clock[8 * grp + 0] = clock64();
+  /* 1. gravity, 2a. reset last levels */
+  int group_bodies = 0;
+  for (int k = 0; k < nw; ++k) {
+    const int wld = d.group_worlds[o0 + k];
+    group_bodies += d.world_body_off[wld + 1] - d.world_body_off[wld];
+  }
+  const bool smem_last = group_bodies <= smem_ints;
+  {
+    int base = 0;
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + tid; g < b1; g += NT) {
+        if (external && !(0.0 == d.iml[g]) && !(d.flags[g] & kFlagInactive)) {
+          d.vx[g] = d.vx[g] + ax * dt;
+          d.vy[g] = d.vy[g] + ay * dt;
+        }
+        if (smem_last) s_last[base + g - b0] = 0;
+        else d.last[g] = 0;
+      }
+      if (tid == 0) s_delta[k] = base - b0;
+      base += b1 - b0;
+    }
+  }
+  __syncthreads();
+  /* 2b. world k is scanned by lane k / P of warp k % P */
+  const int my_k = lane * P + wib;
+  int my_depth = 0, my_items = 0, my_hits = 0;
+  size_t my_region = 0;
+  int c0 = 0, c1 = 0;
+  int32_t* last = d.last;
+  if (my_k < nw) {
+    const int wld = d.group_worlds[o0 + my_k];
+    last = smem_last ? s_last + s_delta[my_k] : d.last;
+    c0 = d.world_contact_off[wld];
+    c1 = d.world_contact_off[wld + 1];
+    my_region = (size_t)stride * c0;
+  }
+  if (my_k < nw && c0 < c1) {
+    for (int pass = warm_start ? 0 : 1; pass <= iterations; ++pass) {
+      uint8_t inf[kScanBlock];
+      int ia[kScanBlock], ib[kScanBlock];
+#pragma unroll
+      for (int k = 0; k < kScanBlock; ++k) {
+        const int cc = min(c0 + k, c1 - 1);
+        inf[k] = d.c_hit[cc];
+        ia[k] = d.c_ga[cc];
+        ib[k] = d.c_gb[cc];
+      }
+      for (int cb = c0; cb < c1; cb += kScanBlock) {
+        uint8_t inf2[kScanBlock];
+        int ia2[kScanBlock], ib2[kScanBlock];
+#pragma unroll
+        for (int k = 0; k < kScanBlock; ++k) {
+          const int cc = min(cb + kScanBlock + k, c1 - 1);
+          inf2[k] = d.c_hit[cc];
+          ia2[k] = d.c_ga[cc];
+          ib2[k] = d.c_gb[cc];
+        }
+#pragma unroll
+        for (int k = 0; k < kScanBlock; ++k) {
+          const int cur_c = cb + k;
+          const uint8_t info = inf[k];
+          if (cur_c < c1 && !(pass == 0 && !(info & kInfoHit))) {
+            const int ga = ia[k], gb = ib[k];
+            const bool da = info & kInfoDynA, db = info & kInfoDynB;
+            const int la = da ? last[ga] : 0, lb = db ? last[gb] : 0;
+            const int lvl = (la > lb ? la : lb) + 1;
+            if (da) last[ga] = lvl;
+            if (db) last[gb] = lvl;
+            d.idesc[my_region + my_items] =
+                make_int4((int)((uint32_t)cur_c | (pass == 0 ? kWarmBit : 0u)), ga, gb, (int)info | (my_k << 8));
+            d.ilevel[my_region + my_items] = lvl;
+            ++my_items;
+            my_depth = lvl > my_depth ? lvl : my_depth;
+            my_hits += pass == 0;
+          }
+          inf[k] = inf2[k];
+          ia[k] = ia2[k];
+          ib[k] = ib2[k];
+        }
+      }
+    }
+  }
+  if (my_k < nw) {
+    s_nitems[my_k] = my_items;
+    s_region[my_k] = (unsigned long long)my_region;
+  }
+  if (d.phase_clock && tid == 0) d.phase_clock[8 * grp + 1] = clock64();
+  /* 3. counting sort by level into a region of gdesc / ghist */
+  int max_depth = my_depth, tot_items = my_items, tot_hits = my_hits;
+  for (int o = 16; o > 0; o >>= 1) {
+    max_depth = max(max_depth, __shfl_xor_sync(0xffffffffu, max_depth, o));
+    tot_items += __shfl_xor_sync(0xffffffffu, tot_items, o);
+    tot_hits += __shfl_xor_sync(0xffffffffu, tot_hits, o);
+  }
+  if (lane == 0) {
+    s_red[0][wib] = max_depth;
+    s_red[1][wib] = tot_items;
+    s_red[2][wib] = tot_hits;
+  }
+  __syncthreads();
+  max_depth = 0;
+  tot_items = 0;
+  tot_hits = 0;
+#pragma unroll
+  for (int w = 0; w < P; ++w) {
+    max_depth = max(max_depth, s_red[0][w]);
+    tot_items += s_red[1][w];
+    tot_hits += s_red[2][w];
+  }
+  if (tid == 0) {
+    atomicAdd(&d.counters[kCntLevels], (unsigned long long)max_depth);
+    atomicAdd(&d.counters[kCntHits], (unsigned long long)tot_hits);
+    atomicAdd(&d.counters[kCntItems], (unsigned long long)tot_items);
+    s_gbase = (int)atomicAdd(&d.counters[kCntGroupAlloc], (unsigned long long)(tot_items + 1));
+  }
+  __syncthreads();
+  const int gbase = s_gbase;
+  int32_t* gh = d.ghist + gbase;
+  int4* gdesc = d.gdesc + gbase;
+  int32_t* hist = max_depth <= smem_ints ? s_last : gh; /* the last levels are dead by now */
+  for (int t = tid; t < max_depth; t += NT) hist[t] = 0;
+  __syncthreads();
+  for (int k = 0; k < nw; ++k) {
+    const int n_items = s_nitems[k];
+    const size_t region = (size_t)s_region[k];
+#pragma unroll 4
+    for (int t = tid; t < n_items; t += NT) atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
+  }
+  __syncthreads();
+  if (wib == 0) { /* exclusive scan of the level counts by warp 0 */
+    int carry = 0;
+    for (int t0 = 0; t0 < max_depth; t0 += 32) {
+      const int t = t0 + lane;
+      const int x = t < max_depth ? hist[t] : 0;
+      int incl = x;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (t < max_depth) hist[t] = carry + incl - x;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < nw; ++k) {
+    const int n_items = s_nitems[k];
+    const size_t region = (size_t)s_region[k];
+#pragma unroll 4
+    for (int t = tid; t < n_items; t += NT) {
+      const int4 u = d.idesc[region + t];
+      gdesc[atomicAdd(&hist[d.ilevel[region + t] - 1], 1)] = u;
+    }
+  }
+  __syncthreads();
+  if (hist != gh)
+    for (int t = tid; t < max_depth; t += NT) gh[t] = hist[t];
+  __syncthreads();
+  if (d.phase_clock && tid == 0) d.phase_clock[8 * grp + 2] = clock64();
+  /* 4. levels, velocities in shared memory when they fit */
+  const bool smem_vel = 6 * group_bodies <= smem_ints;
+  VelStore vs;
+  vs.d = &d;
+  vs.s = smem_vel ? reinterpret_cast<double*>(s_last) : nullptr;
+  if (smem_vel) {
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + tid; g < b1; g += NT) {
+        double* p = vs.s + 3 * (g + s_delta[k]);
+        p[0] = d.vx[g];
+        p[1] = d.vy[g];
+        p[2] = d.w[g];
+      }
+    }
+  }
+  __syncthreads();
+  const int4 none = make_int4(0, 0, 0, 0);
+  int e_prev = 0;
+  int e_cur = max_depth > 0 ? gh[0] : 0;
+  int e_next = max_depth > 1 ? gh[1] : e_cur;
+  int4 cur = tid < e_cur ? gdesc[tid] : none;
+  int4 nxt = e_cur + tid < e_next ? gdesc[e_cur + tid] : none;
+  if (tid < e_cur) prefetch_con(d.con + (cur.x & ~kWarmBit));
+  for (int L = 0; L < max_depth; ++L) {
+    const int e_next2 = L + 2 < max_depth ? gh[L + 2] : e_next;
+    const int4 nxt2 = e_next + tid < tot_items ? gdesc[e_next + tid] : none;
+    if (e_cur + tid < e_next) prefetch_con(d.con + (nxt.x & ~kWarmBit));
+    const int count = e_cur - e_prev;
+    if (tid < count)
+      solve_item(d, (uint32_t)cur.x, cur.y, cur.z, (uint8_t)(cur.w & 0xff), vs, s_delta[cur.w >> 8]);
+    for (int t = tid + NT; t < count; t += NT) { /* levels wider than the CTA */
+      const int4 u = gdesc[e_prev + t];
+      solve_item(d, (uint32_t)u.x, u.y, u.z, (uint8_t)(u.w & 0xff), vs, s_delta[u.w >> 8]);
+    }
+    __syncthreads();
+    cur = nxt;
+    nxt = nxt2;
+    e_prev = e_cur;
+    e_cur = e_next;
+    e_next = e_next2;
+  }
+  if (smem_vel) {
+    for (int k = 0; k < nw; ++k) {
+      const int wld = d.group_worlds[o0 + k];
+      const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+      for (int g = b0 + tid; g < b1; g += NT) {
+        const double* p = vs.s + 3 * (g + s_delta[k]);
+        d.vx[g] = p[0];
+        d.vy[g] = p[1];
+        d.w[g] = p[2];
+      }
+    }
+  }
+  if (d.phase_clock && tid == 0) {
     d.phase_clock[8 * grp + 3] = clock64();
     d.phase_clock[8 * grp + 4] = max_depth;
     d.phase_clock[8 * grp + 5] = tot_items;

@@ -130,6 +130,21 @@ def test_mixed_polygon_worlds():
     b.close()
 
 
+@pytest.mark.parametrize("wpg,warps", [(1, 2), (3, 4), (8, 8), (32, 4)])
+def test_cooperative_groups_do_not_change_results(wpg, warps):
+    """Several warps sharing a solver group (levels split across them)."""
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
+    b = batch_from_scene(sc)
+    b.set_launch_groups(wpg, 32 * warps, warps)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 40)
+    step_oracles(ow, sc, 40)
+    compare_bodies(b, ow, sc, f"cooperative {wpg}/{warps}")
+    compare_collision(b, ow, f"cooperative {wpg}/{warps}")
+    b.close()
+
+
 @pytest.mark.parametrize("target,threads", [(1, 32), (64, 64), (100000, 256), (0, 128)])
 def test_solver_packing_does_not_change_results(target, threads):
     sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
@@ -350,8 +365,8 @@ def test_autotune_keeps_state_and_results():
     step_oracles(ow, sc, 90)
     before = b.get_bodies()
     k0, l0, _ = b.get_cache()
-    wpg, thr = b.autotune(cfg, 3)
-    assert 1 <= wpg <= 32 and thr in (32, 64, 128)
+    wpg, thr, gw = b.autotune(cfg, 3)
+    assert 1 <= wpg <= 32 and gw in (1, 2, 4, 8) and (thr in (32, 64, 128) if gw == 1 else thr == 32 * gw)
     after = b.get_bodies()
     k1, l1, _ = b.get_cache()
     for f in STATE_FIELDS:
