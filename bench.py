@@ -310,7 +310,8 @@ def new_batch(_lib, scene, stream, tuned=None):
     if not INCREMENTAL_PAIRS:
         b.set_incremental(False)
     if tuned:
-        b.set_launch_groups(*tuned)
+        b.set_launch_groups(*tuned[:3])
+        b.set_world_order(tuned[3])
     return b
 
 
@@ -427,7 +428,7 @@ def run_ours(args, rank, world, local):
     if not args.no_tune and int(len(scene["world_body_offsets"]) - 1) > 1:
         t = new_batch(_lib, scene, stream)
         t.step(cfg_for(plain_it, False), args.tune_after)
-        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps)
+        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(),)
         t.close()
 
     def timed(it, use_net):
@@ -597,7 +598,11 @@ def run_ours(args, rank, world, local):
                        "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
                        else "grid, full 3x3 search every frame",
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
-                                          "warps_per_group": tuned[2]} if tuned else "default"},
+                                          "warps_per_group": tuned[2],
+                                          "world_order": "by size" if np.array_equal(
+                                              tuned[3], np.argsort(-np.diff(scene["world_body_offsets"]),
+                                                                   kind="stable")) else "by dependency levels"}
+                       if tuned else "default"},
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * n_bodies,

@@ -221,6 +221,14 @@ int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, in
 int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps);
 /* The packing in use (any pointer may be NULL). */
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps);
+/* The order in which worlds are packed into groups: a permutation of
+ * 0..n_worlds-1 (NULL = by body count, largest first, the default).  The
+ * autotuner may choose an order by dependency levels; get_world_order reads
+ * the one in use so that another handle of the same scene can reuse it. */
+int shapes_batch_set_world_order(shapes_batch* b, const int32_t* order);
+int shapes_batch_get_world_order(shapes_batch* b, int32_t* order);
+/* Dependency levels of each world's last solve (0 for large worlds). */
+int shapes_batch_get_world_levels(shapes_batch* b, int32_t* levels);
 
 /* Autotuner for the solver packing: from the current state, times
  * `steps_per_trial` steps for each candidate (worlds per group x warps per

@@ -126,6 +126,9 @@ SIGNATURES = [
     ("shapes_batch_set_launch_groups", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_group_warps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_get_launch", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _ip]),
+    ("shapes_batch_set_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
+    ("shapes_batch_get_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
+    ("shapes_batch_get_world_levels", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_batch_set_stream", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     ("shapes_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Config), ctypes.c_int32, _ip, _ip]),
     ("shapes_batch_set_profiling", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
@@ -314,6 +317,22 @@ class Batch:
         check(lib().shapes_batch_get_launch(self._h, ctypes.byref(wpg), ctypes.byref(thr), ctypes.byref(gw)),
               "shapes_batch_get_launch")
         return wpg.value, thr.value, gw.value
+
+    def world_order(self) -> np.ndarray:
+        out = np.empty(self.n_worlds, dtype=np.int32)
+        check(lib().shapes_batch_get_world_order(self._h, _ptr(out, _ip)), "shapes_batch_get_world_order")
+        return out
+
+    def set_world_order(self, order) -> None:
+        """Packing order of the worlds (None = by size)."""
+        o = None if order is None else np.ascontiguousarray(order, dtype=np.int32)
+        check(lib().shapes_batch_set_world_order(self._h, None if o is None else _ptr(o, _ip)),
+              "shapes_batch_set_world_order")
+
+    def world_levels(self) -> np.ndarray:
+        out = np.empty(self.n_worlds, dtype=np.int32)
+        check(lib().shapes_batch_get_world_levels(self._h, _ptr(out, _ip)), "shapes_batch_get_world_levels")
+        return out
 
     def set_group_warps(self, warps: int) -> None:
         """Warps cooperating on each solver group (1, 2, 4 or 8)."""

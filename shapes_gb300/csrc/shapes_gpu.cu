@@ -165,7 +165,7 @@ struct shapes_batch {
   int32_t* ghist = nullptr;
   long long* phase_clock = nullptr; /* [8 * G], allocated while profiling */
   int32_t phase_clock_groups = 0;
-  int32_t* world_items = nullptr;
+  int32_t* world_levels = nullptr;
   int32_t* group_depth = nullptr;
   int32_t* group_world_off = nullptr;
   int32_t* group_worlds = nullptr;
@@ -198,6 +198,7 @@ struct shapes_batch {
   int32_t target_group_bodies = 0;
   int32_t solve_threads = 32;
   int32_t group_warps = 1; /* > 1: that many warps cooperate on each group (k_group_solve) */
+  std::vector<int32_t> world_order; /* packing order of the worlds; empty = by body count */
   /* scans */
   int32_t* tile_sums = nullptr;
   int32_t tile_cap = 0;
@@ -432,7 +433,7 @@ struct shapes_batch {
     d.idesc = idesc;
     d.phase_clock = profiling ? phase_clock : nullptr;
     d.ghist = ghist;
-    d.world_items = world_items;
+    d.world_levels = world_levels;
     d.group_depth = group_depth;
     d.group_world_off = group_world_off;
     d.group_worlds = group_worlds;
@@ -599,12 +600,16 @@ struct shapes_batch {
     if (stream) ck(cudaStreamSynchronize(stream), "sync"); /* no kernel may still read the old groups */
     invalidate_graphs();
     std::vector<int32_t> order;
-    for (int w = 0; w < W; ++w)
+    const bool given = (int)world_order.size() == W;
+    for (int k = 0; k < W; ++k) {
+      const int w = given ? world_order[k] : k;
       if (h_world_body_off[w + 1] - h_world_body_off[w] < large_world_bodies) order.push_back(w);
+    }
     const int n_small = (int)order.size();
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      return (h_world_body_off[a + 1] - h_world_body_off[a]) > (h_world_body_off[b + 1] - h_world_body_off[b]);
-    });
+    if (!given)
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (h_world_body_off[a + 1] - h_world_body_off[a]) > (h_world_body_off[b + 1] - h_world_body_off[b]);
+      });
     int per_group = std::max(1, std::min(shapes::kMaxGroupWorlds, 32 / (iterations + 1)));
     if (worlds_per_group_override > 0) per_group = std::min(shapes::kMaxGroupWorlds, worlds_per_group_override);
     h_group_world_off.assign(1, 0);
@@ -1114,7 +1119,7 @@ struct shapes_batch {
       dfree(body_stage[k]);
     }
     dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
-    dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(world_items);
+    dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(world_levels);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(active);
     active = nullptr;
@@ -1149,7 +1154,8 @@ struct shapes_batch {
     if (!cwo[0])
       for (int k = 0; k < 2; ++k) cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
     last = dalloc<int32_t>(N, "cudaMalloc");
-    world_items = dalloc<int32_t>(n_worlds, "cudaMalloc");
+    world_levels = dalloc<int32_t>(n_worlds, "cudaMalloc");
+    ck(cudaMemset(world_levels, 0, sizeof(int32_t) * n_worlds), "memset");
     if (!counters) counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
     if (!np_cls) np_cls = dalloc<int32_t>(2 * shapes::kNpClasses + 1, "cudaMalloc");
     if (!world_residual) world_residual = dalloc<double>(n_worlds, "cudaMalloc");
@@ -1239,7 +1245,7 @@ struct shapes_batch {
     dfree(radius);
     dfree(metric_part);
     for (int k = 0; k < 2; ++k) dfree(cwo[k]);
-    dfree(last); dfree(world_items); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
+    dfree(last); dfree(world_levels); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
     dfree(phase_clock);
     dfree(counters);
     dfree(np_cls);
@@ -1707,6 +1713,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     void* scwo = keep(b->cwo[cache_buf0], sizeof(int32_t) * (W + 1));
     const int32_t wpg0 = b->worlds_per_group_override, thr0 = b->solve_threads, tgt0 = b->target_group_bodies;
     const int32_t gw0 = b->group_warps;
+    const std::vector<int32_t> order0 = b->world_order;
     const bool prof0 = b->profiling;
     b->profiling = false;
     auto restore_state = [&]() {
@@ -1720,29 +1727,48 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->pose(0, 0.0);
     };
     const int base = std::max(1, std::min(shapes::kMaxGroupWorlds, 32 / (cfg->iterations + 1)));
-    /* (worlds per group, threads per CTA, warps per group) */
-    std::vector<std::array<int, 3>> cands;
-    auto add = [&](int wpg, int thr, int gw) {
-      const std::array<int, 3> c{wpg, thr, gw};
+    /* The level-ordered packing: worlds sorted by the dependency levels of
+     * one step from the saved state (deepest first, then by size), so that a
+     * group's worlds end their levels together. */
+    restore_state();
+    b->world_order.clear();
+    b->make_groups(cfg->iterations);
+    const int rc0 = b->run(*cfg, 1, true);
+    std::vector<int32_t> lv(W, 0), by_levels(W);
+    if (rc0 == SHAPES_OK)
+      ck(cudaMemcpy(lv.data(), b->world_levels, sizeof(int32_t) * W, cudaMemcpyDeviceToHost), "download");
+    for (int w = 0; w < W; ++w) by_levels[w] = w;
+    std::stable_sort(by_levels.begin(), by_levels.end(), [&](int a, int c) {
+      if (lv[a] != lv[c]) return lv[a] > lv[c];
+      return (b->h_world_body_off[a + 1] - b->h_world_body_off[a]) > (b->h_world_body_off[c + 1] - b->h_world_body_off[c]);
+    });
+    /* (worlds per group, threads per CTA, warps per group, level order) */
+    std::vector<std::array<int, 4>> cands;
+    auto add = [&](int wpg, int thr, int gw, int lo) {
+      const std::array<int, 4> c{wpg, thr, gw, lo};
       if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds && std::find(cands.begin(), cands.end(), c) == cands.end())
         cands.push_back(c);
     };
-    for (int wpg : {1, base / 2, base, base + 1, 2 * base})
-      for (int thr : {32, 64, 128}) add(wpg, thr, 1);
-    for (int wpg : {1, base, 2 * base, 3 * base, 4 * base})
-      for (int gw : {2, 4, 8}) add(wpg, 32 * gw, gw);
+    for (int lo : {0, 1}) {
+      for (int wpg : {1, base / 2, base, base + 1, 2 * base})
+        for (int thr : {32, 64, 128}) add(wpg, thr, 1, lo);
+      for (int wpg : {1, base, 2 * base, 3 * base, 4 * base})
+        for (int gw : {2, 4, 8}) add(wpg, 32 * gw, gw, lo);
+    }
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     float best = 1e30f;
-    std::array<int, 3> best_c{wpg0, thr0, gw0};
-    int rc = SHAPES_OK;
+    std::array<int, 4> best_c{wpg0, thr0, gw0, -1};
+    int rc = rc0;
+    if (rc0 != SHAPES_OK) cands.clear();
     for (const auto& c : cands) {
       restore_state();
       b->worlds_per_group_override = c[0];
       b->target_group_bodies = 0;
       b->solve_threads = c[1];
       b->group_warps = c[2];
+      if (c[3]) b->world_order = by_levels; else b->world_order.clear();
       b->make_groups(cfg->iterations);
       rc = b->run(*cfg, 1, true); /* untimed: captures this packing's step graphs */
       if (rc != SHAPES_OK) break;
@@ -1761,16 +1787,18 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     restore_state();
-    if (rc == SHAPES_OK) {
+    if (rc == SHAPES_OK && best_c[3] >= 0) {
       b->worlds_per_group_override = best_c[0];
       b->target_group_bodies = 0;
       b->solve_threads = best_c[1];
       b->group_warps = best_c[2];
+      if (best_c[3]) b->world_order = by_levels; else b->world_order.clear();
     } else {
       b->worlds_per_group_override = wpg0;
       b->target_group_bodies = tgt0;
       b->solve_threads = thr0;
       b->group_warps = gw0;
+      b->world_order = order0;
     }
     b->make_groups(cfg->iterations);
     ck(cudaStreamSynchronize(b->stream), "sync");
@@ -2305,6 +2333,47 @@ int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps) {
     ck(cudaStreamSynchronize(b->stream), "sync");
     b->group_warps = warps;
     b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_world_order(shapes_batch* b, const int32_t* order) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  if (order) {
+    std::vector<char> seen(b->W, 0);
+    for (int32_t k = 0; k < b->W; ++k) {
+      if (order[k] < 0 || order[k] >= b->W || seen[order[k]]) return SHAPES_E_INVALID_ARG;
+      seen[order[k]] = 1;
+    }
+  }
+  return guarded([&]() -> int {
+    if (order)
+      b->world_order.assign(order, order + b->W);
+    else
+      b->world_order.clear();
+    b->make_groups(b->grouped_iterations >= 0 ? b->grouped_iterations : 2);
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_world_order(shapes_batch* b, int32_t* order) {
+  if (!b || !order) return SHAPES_E_INVALID_ARG;
+  if ((int)b->world_order.size() == b->W) {
+    std::copy(b->world_order.begin(), b->world_order.end(), order);
+  } else {
+    for (int32_t k = 0; k < b->W; ++k) order[k] = k;
+    std::stable_sort(order, order + b->W, [&](int a, int c) {
+      return (b->h_world_body_off[a + 1] - b->h_world_body_off[a]) > (b->h_world_body_off[c + 1] - b->h_world_body_off[c]);
+    });
+  }
+  return SHAPES_OK;
+}
+
+int shapes_batch_get_world_levels(shapes_batch* b, int32_t* levels) {
+  if (!b || !levels) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaMemcpyAsync(levels, b->world_levels, sizeof(int32_t) * b->W, cudaMemcpyDeviceToHost, b->stream), "download");
+    ck(cudaStreamSynchronize(b->stream), "download");
     return SHAPES_OK;
   });
 }

@@ -132,7 +132,7 @@ struct Dev {
   int4* idesc;                /* [item_cap] the same descriptors in sequential order, per world region */
   long long* phase_clock;     /* [G * 8] per-group phase clocks when profiling, else null */
   int32_t* ghist;             /* [item_cap + W + 1] per-group level ends */
-  int32_t* world_items;       /* [W] */
+  int32_t* world_levels;      /* [W] dependency levels of each small world's last solve */
   int32_t* group_depth;       /* [G] */
   const int32_t* group_world_off; /* [G+1] offsets into group_worlds */
   const int32_t* group_worlds;    /* [W] world ids, grouped */
@@ -1801,6 +1801,7 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
       }
     }
   }
+  if (lane < nw) d.world_levels[d.group_worlds[o0 + lane]] = my_depth;
   if (d.phase_clock && lane == 0) d.phase_clock[8 * grp + 1] = clock64();
   /* 3. the group's updates counting-sorted by level into a region of gdesc /
    *    ghist taken from a bump allocator, as packed descriptors, so that a
@@ -2060,6 +2061,7 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
   if (my_k < nw) {
     s_nitems[my_k] = my_items;
     s_region[my_k] = (unsigned long long)my_region;
+    d.world_levels[d.group_worlds[o0 + my_k]] = my_depth;
   }
   if (d.phase_clock && tid == 0) d.phase_clock[8 * grp + 1] = clock64();
   /* 3. counting sort by level into a region of gdesc / ghist */

@@ -145,6 +145,29 @@ def test_cooperative_groups_do_not_change_results(wpg, warps):
     b.close()
 
 
+def test_world_order_does_not_change_results():
+    """Groups packed in a shuffled world order (and by dependency levels)."""
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 20)
+    step_oracles(ow, sc, 20)
+    levels = b.world_levels()
+    assert levels.max() > 0
+    b.set_world_order(np.random.default_rng(1).permutation(24))
+    b.set_launch_groups(3, 128, 4)
+    b.step(cfg, 20)
+    step_oracles(ow, sc, 20)
+    b.set_world_order(np.argsort(-levels, kind="stable"))
+    b.step(cfg, 20)
+    step_oracles(ow, sc, 20)
+    compare_bodies(b, ow, sc, "world orders")
+    with pytest.raises(_lib.ShapesError):
+        b.set_world_order(np.zeros(24, dtype=np.int32))  # not a permutation
+    b.close()
+
+
 @pytest.mark.parametrize("target,threads", [(1, 32), (64, 64), (100000, 256), (0, 128)])
 def test_solver_packing_does_not_change_results(target, threads):
     sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
