@@ -1752,7 +1752,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     for (int lo : {0, 1}) {
       for (int wpg : {1, base / 2, base, base + 1, 2 * base})
         for (int thr : {32, 64, 128}) add(wpg, thr, 1, lo);
-      for (int wpg : {1, base, 2 * base, 3 * base, 4 * base})
+      for (int wpg : {1, 2, base, base + 1, 2 * base, 3 * base, 4 * base})
         for (int gw : {2, 4, 8}) add(wpg, 32 * gw, gw, lo);
     }
     cudaEvent_t e0, e1;
