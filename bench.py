@@ -566,8 +566,12 @@ def run_ours(args, rank, world, local):
         achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
         roof = {"kernel": solver_kernel, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": items / solve_launches * SOLVER_DRAM_BYTES_PER_ITEM,
-                "traffic_source": "ncu dram bytes per update (512-world capture) x updates per launch",
+                "traffic": items / solve_launches * (GROUP_SOLVE_DRAM_BYTES_PER_ITEM if "group" in solver_kernel
+                                                     else SOLVER_DRAM_BYTES_PER_ITEM),
+                "traffic_source": ("ncu dram bytes per update of k_group_solve<4> (mixed, 256 worlds)"
+                                   if "group" in solver_kernel else
+                                   "ncu dram bytes per update of k_schedule_solve (batched, 512 worlds)")
+                                  + " x updates per launch",
                 "bytes_per_item": SOLVER_BYTES_PER_ITEM,
                 "items_per_launch": items / solve_launches, "avg_launch_ms": avg_ms}
         fp64_peak = measure_fp64_peak()
@@ -733,6 +737,9 @@ SOLVER_FP64_OPS_PER_ITEM = 72.5
 # dram__bytes_write.sum = 12.70 MB over 370,978 updates): the working set is
 # L2-resident, so traffic is far below the algorithmic bytes.
 SOLVER_DRAM_BYTES_PER_ITEM = 34.2
+# the same for k_group_solve<4> (one ncu capture, mixed scene, 256 worlds,
+# settled frame): 25.78 MB over 865,243 updates.
+GROUP_SOLVE_DRAM_BYTES_PER_ITEM = 29.8
 
 
 def main():
