@@ -97,6 +97,7 @@ struct shapes_batch {
   double* box = nullptr;
   uint64_t* boxk = nullptr;
   uint8_t* flags = nullptr;
+  uint8_t* body_changed = nullptr; /* [N] scratch of set_bodies: pose inputs changed */
   /* broadphase / narrowphase */
   int32_t pair_cap = 0, contact_cap = 0;
   int64_t item_cap = 0;
@@ -1118,7 +1119,7 @@ struct shapes_batch {
       dfree(body[k]);
       dfree(body_stage[k]);
     }
-    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
+    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags); dfree(body_changed);
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(world_levels);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(active);
@@ -1148,6 +1149,7 @@ struct shapes_batch {
     box = dalloc<double>(4 * (size_t)N, "cudaMalloc");
     boxk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc");
     flags = dalloc<uint8_t>(N, "cudaMalloc");
+    body_changed = dalloc<uint8_t>(N, "cudaMalloc");
     row_cnt = dalloc<int32_t>(N, "cudaMalloc");
     row_off = dalloc<int32_t>((size_t)N + 1, "cudaMalloc");
     world_pair_off = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
@@ -1237,7 +1239,7 @@ struct shapes_batch {
       dfree(body[k]);
       dfree(body_stage[k]);
     }
-    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags);
+    dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags); dfree(body_changed);
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
@@ -1431,13 +1433,42 @@ int shapes_batch_collide(shapes_batch* b) {
   });
 }
 
+/* Device addresses of ten caller arrays when every one is pinned host memory
+ * mapped into the device address space (then one copy kernel moves them);
+ * false for pageable memory, which goes through cudaMemcpyAsync. */
+static bool mapped_host10(double* const host[10], double* dev[10]) {
+  for (int k = 0; k < 10; ++k) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host[k]) != cudaSuccess) {
+      cudaGetLastError(); /* clear: an unknown pointer is simply not mapped */
+      return false;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return false;
+    dev[k] = static_cast<double*>(a.devicePointer);
+  }
+  return true;
+}
+
+static dim3 copy10_grid(int n) { return dim3((unsigned)std::min<int64_t>((n + 255) / 256, 1024), 10); }
+
 int shapes_batch_get_bodies(shapes_batch* b, shapes_bodies* out) {
   if (!b || !body_arrays_ok(out)) return SHAPES_E_INVALID_ARG;
   return guarded([&]() -> int {
     double* bp[10];
     body_ptrs(out, bp);
-    for (int k = 0; k < 10; ++k)
-      ck(cudaMemcpyAsync(bp[k], b->body[k], sizeof(double) * b->N, cudaMemcpyDeviceToHost, b->stream), "download");
+    double* dp[10];
+    if (b->N > 0 && mapped_host10(bp, dp)) {
+      shapes::Ptr10 p{};
+      for (int k = 0; k < 10; ++k) {
+        p.src[k] = b->body[k];
+        p.dst[k] = dp[k];
+      }
+      shapes::k_copy10<<<copy10_grid(b->N), 256, 0, b->stream>>>(p, b->N, nullptr);
+      ck(cudaGetLastError(), "launch");
+    } else {
+      for (int k = 0; k < 10; ++k)
+        ck(cudaMemcpyAsync(bp[k], b->body[k], sizeof(double) * b->N, cudaMemcpyDeviceToHost, b->stream), "download");
+    }
     ck(cudaStreamSynchronize(b->stream), "download");
     return SHAPES_OK;
   });
@@ -1448,23 +1479,44 @@ int shapes_batch_set_bodies(shapes_batch* b, const shapes_bodies* in) {
   double* bp[10];
   body_ptrs(in, bp);
   return guarded([&]() -> int {
-    for (int k = 0; k < 10; ++k)
-      ck(cudaMemcpyAsync(b->body_stage[k], bp[k], sizeof(double) * b->N, cudaMemcpyHostToDevice, b->stream), "upload");
     ck(cudaMemsetAsync(b->counters + shapes::kCntBadInput, 0, sizeof(unsigned long long), b->stream), "memset");
-    shapes::k_check_finite<<<grid_for(10LL * b->N, 256), 256, 0, b->stream>>>(
-        b->body_stage[0], b->body_stage[1], b->body_stage[2], b->body_stage[3], b->body_stage[4],
-        b->body_stage[5], b->body_stage[6], b->body_stage[7], b->body_stage[8], b->body_stage[9], b->N,
-        b->counters + shapes::kCntBadInput);
+    double* dp[10];
+    if (mapped_host10(bp, dp)) { /* copy and check in one pass over NVLink-C2C / PCIe */
+      shapes::Ptr10 p{};
+      for (int k = 0; k < 10; ++k) {
+        p.src[k] = dp[k];
+        p.dst[k] = b->body_stage[k];
+      }
+      shapes::k_copy10<<<copy10_grid(b->N), 256, 0, b->stream>>>(p, b->N, b->counters + shapes::kCntBadInput);
+    } else {
+      for (int k = 0; k < 10; ++k)
+        ck(cudaMemcpyAsync(b->body_stage[k], bp[k], sizeof(double) * b->N, cudaMemcpyHostToDevice, b->stream),
+           "upload");
+      shapes::k_check_finite<<<grid_for(10LL * b->N, 256), 256, 0, b->stream>>>(
+          b->body_stage[0], b->body_stage[1], b->body_stage[2], b->body_stage[3], b->body_stage[4],
+          b->body_stage[5], b->body_stage[6], b->body_stage[7], b->body_stage[8], b->body_stage[9], b->N,
+          b->counters + shapes::kCntBadInput);
+    }
+    ck(cudaGetLastError(), "launch");
     unsigned long long bad = 0;
     ck(cudaMemcpyAsync(&bad, b->counters + shapes::kCntBadInput, sizeof(bad), cudaMemcpyDeviceToHost, b->stream), "download");
     ck(cudaStreamSynchronize(b->stream), "validate");
     if (bad) return SHAPES_E_NAN; /* live state untouched */
     /* copied, not swapped: the live arrays keep their addresses, which the
      * captured step graphs hold */
-    for (int k = 0; k < 10; ++k)
-      ck(cudaMemcpyAsync(b->body[k], b->body_stage[k], sizeof(double) * b->N, cudaMemcpyDeviceToDevice, b->stream),
-         "upload");
-    b->pose(0, 0.0);
+    shapes::Ptr10 p{};
+    for (int k = 0; k < 10; ++k) {
+      p.src[k] = b->body_stage[k];
+      p.dst[k] = b->body[k];
+    }
+    /* only bodies whose position, rotation or inverse masses changed get a
+     * new pose: every other body's pose is already that of the state written
+     * back (the live pose always follows the live state) */
+    shapes::k_commit_bodies<<<grid_for(b->N, 256), 256, 0, b->stream>>>(p, b->N, b->body_changed);
+    {
+      Dev d = b->view(0);
+      shapes::k_integrate_pose<<<grid_for(b->N, 128), 128, 0, b->stream>>>(d, 0.0, 0, b->body_changed);
+    }
     ck(cudaGetLastError(), "launch");
     ck(cudaStreamSynchronize(b->stream), "upload");
     b->have_results = false;

@@ -185,6 +185,44 @@ __global__ void k_check_finite(const double* a0, const double* a1, const double*
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
 }
 
+/* Ten arrays of n doubles copied in one launch (blockIdx.y = array), with an
+ * optional finiteness check of what passes through.  Either side may be
+ * pinned host memory mapped into the device address space: on a Grace host
+ * the loads and stores then cross NVLink-C2C from every SM at once instead of
+ * through the copy engines. */
+struct Ptr10 {
+  const double* src[10];
+  double* dst[10];
+};
+
+__global__ void k_copy10(Ptr10 p, int n, unsigned long long* bad_flag) {
+  const double* __restrict__ src = p.src[blockIdx.y];
+  double* __restrict__ dst = p.dst[blockIdx.y];
+  bool bad = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = src[i];
+    bad |= !isfinite(v);
+    dst[i] = v;
+  }
+  if (bad_flag && __any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(bad_flag, 1ull);
+}
+
+/* Staged body state -> live arrays, one thread per body; changed[g] = 1 when
+ * a field the pose depends on (position, rotation, inverse masses, which set
+ * the static flag) differs bit for bit from the live value. */
+__global__ void k_commit_bodies(Ptr10 p, int n, uint8_t* changed) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    bool c = false;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+      const double v = p.src[k][g];
+      if (k >= 3 && k <= 7) c |= __double_as_longlong(v) != __double_as_longlong(p.dst[k][g]);
+      p.dst[k][g] = v;
+    }
+    changed[g] = c ? 1 : 0;
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* helpers                                                                    */
 /* ------------------------------------------------------------------------ */
@@ -241,8 +279,9 @@ __global__ void k_init_extents(Dev d) {
  * (Linear.hs:217-220) per vertex, unitEdgeNormal (ConvexHull.hs:218-226) per
  * edge, then hullToAabb (Aabb.hs:81-84, 106-110) and its ordered keys.
  * One thread per body. */
-__global__ void k_integrate_pose(Dev d, double dt, int advance) {
+__global__ void k_integrate_pose(Dev d, double dt, int advance, const uint8_t* only = nullptr) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (only && !only[g]) continue; /* re-pose: this body's pose inputs did not change */
     if (d.active && !d.active[g]) { /* empty slot: left as it was, out of the broadphase */
       d.flags[g] = kFlagInactive;
       continue;
@@ -1550,11 +1589,20 @@ __device__ int block_exclusive_scan(int32_t* a, int n, int32_t* smem /* >= 32 */
   return carry;
 }
 
-/* applyLagrangian2 (Constraint.hs:197-204): v += (J * lambda) * invMass. */
+/* applyLagrangian2 (Constraint.hs:197-204): v += (J * lambda) * invMass.
+ * Every contact Jacobian built by k_build has J[0] = -J[3] and J[1] = -J[4]
+ * (the normal and the tangent enter the two bodies with opposite signs, and
+ * a Flip only swaps the halves), and (-x) * l is exactly -(x * l) in IEEE
+ * arithmetic, so those two products are computed once. */
 __device__ __forceinline__ void apply_impulse(const double j[6], double l, double v[6],
                                               const double m[6]) {
-#pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = v[k] + (j[k] * l) * m[k];
+  const double p3 = j[3] * l, p4 = j[4] * l;
+  v[0] = v[0] + (-p3) * m[0];
+  v[1] = v[1] + (-p4) * m[1];
+  v[2] = v[2] + (j[2] * l) * m[2];
+  v[3] = v[3] + p3 * m[3];
+  v[4] = v[4] + p4 * m[4];
+  v[5] = v[5] + (j[5] * l) * m[5];
 }
 
 /* J . v as a left fold (Shapes/Linear/Template.hs:108-110). */

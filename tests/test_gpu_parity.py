@@ -422,3 +422,39 @@ def test_world_metrics_residual_and_depth():
         assert depth[w] == want_d
     compare_bodies(b, ow, sc, "after metrics")
     b.close()
+
+
+def test_pinned_host_buffers_round_trip():
+    """Body state through pinned host buffers (copied by a kernel over the
+    mapped host memory) equals the pageable path, and a non-finite value in
+    a pinned buffer is still refused with the live state untouched."""
+    import ctypes
+
+    import torch
+
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=24), list(range(24)))
+    cfg = config_of(sc)
+    a, b = batch_from_scene(sc), batch_from_scene(sc)
+    a.step(cfg, 25)
+    b.step(cfg, 25)
+    n = b.n_bodies
+    pin = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
+    desc = _lib.Bodies(*[ctypes.cast(pin[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS])
+    L = _lib.lib()
+    _lib.check(L.shapes_batch_get_bodies(b.handle, ctypes.byref(desc)), "get_bodies pinned")
+    want = a.get_bodies()
+    for f in _lib.BODY_FIELDS:
+        assert_bits_equal(pin[f].numpy(), want[f], f"pinned get {f}")
+    _lib.check(L.shapes_batch_set_bodies(b.handle, ctypes.byref(desc)), "set_bodies pinned")
+    a.step(cfg, 10)
+    b.step(cfg, 10)
+    ga, gb = a.get_bodies(), b.get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(ga[f], gb[f], f"pinned round trip {f}")
+    pin["vel_x"][5] = float("nan")
+    assert L.shapes_batch_set_bodies(b.handle, ctypes.byref(desc)) == _lib.SHAPES_E_NAN
+    gc = b.get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(gc[f], gb[f], f"refused pinned input {f}")
+    a.close()
+    b.close()
