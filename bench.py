@@ -639,7 +639,25 @@ def run_contacts(args, rank, world, local, scene, stream):
     from shapes_gb300 import _lib
 
     n_bodies = int(scene["world_body_offsets"][-1])
+    # The bodies never move here, so incremental pair lists would skip the grid
+    # search after the first collide: the value is measured with the full
+    # search every step, the incremental figure is reported beside it.
+    inc_value = None
+    if INCREMENTAL_PAIRS:
+        bi = new_batch(_lib, scene, stream)
+        for _ in range(args.warmup):
+            bi.collide()
+        i0, i1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        i0.record(stream)
+        for _ in range(args.steps):
+            bi.collide()
+        i1.record(stream)
+        torch.cuda.synchronize()
+        inc_value = n_bodies * args.steps / (i0.elapsed_time(i1) * 1e-3)
+        bi.close()
     b = new_batch(_lib, scene, stream)
+    b.set_incremental(False)
     for _ in range(args.warmup):
         b.collide()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -710,7 +728,10 @@ def run_contacts(args, rank, world, local, scene, stream):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": "contacts", "description": WORKLOADS["contacts"], "bodies_per_gpu": n_bodies,
-                       "step": "one collide", "l2": "inputs larger than L2 are not needed: 65,536 hulls (~30 MB)"},
+                       "step": "one collide", "l2": "inputs larger than L2 are not needed: 65,536 hulls (~30 MB)",
+                       "broadphase": "grid, full 3x3 search every collide (incremental pair lists off: the "
+                                     "bodies never move in this workload)",
+                       "incremental_pairs_value": inc_value},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": total * args.steps / (e_ms * 1e-3), "unit": UNIT,
                     "h2d_bytes_per_step": 10 * 8 * n_bodies, "d2h_bytes_per_step": st["contacts"] * 60},
