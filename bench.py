@@ -315,6 +315,63 @@ def new_batch(_lib, scene, stream, tuned=None):
     return b
 
 
+class Lanes:
+    """The worlds of a scene sharded over `k` handles, each on its own CUDA
+    stream, stepped together by shapes_batches_step (the solver of one
+    handle's worlds overlaps the other stages of another's).  Worlds are dealt
+    round-robin in the packing order, so every handle gets the same mix."""
+
+    def __init__(self, _lib, scene, k, tuned, torch):
+        from shapes_gb300 import scenes
+
+        self._lib = _lib
+        W = len(scene["world_body_offsets"]) - 1
+        order = (np.asarray(tuned[3]) if tuned else
+                 np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable")).astype(np.int64)
+        self.worlds = [order[j::k] for j in range(k) if len(order[j::k])]
+        self.streams = [torch.cuda.Stream() for _ in self.worlds]
+        self.scenes = [scenes.subset_worlds(scene, w.tolist()) for w in self.worlds]
+        self.handles = []
+        for sc, st in zip(self.scenes, self.streams):
+            b = _lib.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], sc["local_xy"],
+                           sc.get("shape_kind"))
+            b.set_stream(st.cuda_stream)
+            if not INCREMENTAL_PAIRS:
+                b.set_incremental(False)
+            if tuned:
+                b.set_launch_groups(*tuned[:3])
+            b.set_world_order(np.arange(len(sc["world_body_offsets"]) - 1, dtype=np.int32))
+            self.handles.append(b)
+        assert sum(len(w) for w in self.worlds) == W
+
+    def set_mlp(self, net, wres, wdep):
+        for b, w in zip(self.handles, self.worlds):
+            b.set_mlp(net)
+            b.set_judge(np.asarray(wres)[w], np.asarray(wdep)[w])
+
+    def step(self, cfg, n):
+        self._lib.step_many(self.handles, cfg, n)
+
+    def timed_step(self, cfg, n, stream, torch):
+        """n steps of every handle between CUDA events on `stream` (the lane
+        streams wait for the start event; `stream` waits for their ends)."""
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for st in self.streams:
+            st.wait_event(t0)
+        self.step(cfg, n)
+        for st in self.streams:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            stream.wait_event(ev)
+        t1.record(stream)
+        return t0, t1
+
+    def close(self):
+        for b in self.handles:
+            b.close()
+
+
 def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10, coloured=False):
     """Steps a fresh copy with the residual flag: (mean over steps of the
     world-mean residual, mean over sampled steps of the world-mean largest
@@ -434,13 +491,35 @@ def run_ours(args, rank, world, local):
         tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(),)
         t.close()
 
+    n_worlds = len(scene["world_body_offsets"]) - 1
+    lanes = args.lanes if args.lanes > 0 else (8 if n_worlds >= 256 else 4 if n_worlds >= 64 else 1)
+
     def timed(it, use_net):
         """K steps after W warm-up from a fresh copy; returns (ms, batch)."""
+        cfg = cfg_for(it, use_net)
+        if lanes > 1:
+            ln = Lanes(_lib, scene, lanes, tuned, torch)
+            if use_net:
+                ln.set_mlp(net, p_wres, p_wdep)
+            ln.step(cfg, args.warmup)
+            barrier(world)
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("timed")
+            t0, t1 = ln.timed_step(cfg, args.steps, stream, torch)
+            torch.cuda.nvtx.range_pop()
+            torch.cuda.synchronize()
+            barrier(world)
+            ln.close()
+            b = new_batch(_lib, scene, stream, tuned)  # the single handle for stats and the profiled pass
+            if use_net:
+                b.set_mlp(net)
+                b.set_judge(p_wres, p_wdep)
+            b.step(cfg, args.warmup + args.steps)
+            return t0.elapsed_time(t1), b, cfg
         b = new_batch(_lib, scene, stream, tuned)
         if use_net:
             b.set_mlp(net)
             b.set_judge(p_wres, p_wdep)
-        cfg = cfg_for(it, use_net)
         b.step(cfg, args.warmup)
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier(world)
@@ -516,37 +595,72 @@ def run_ours(args, rank, world, local):
         lnet.close()
 
     # ---- e2e: host buffers through the C ABI every step --------------------
-    b = new_batch(_lib, scene, stream, tuned)
-    if run_learned:
-        b.set_mlp(net)
-        b.set_judge(p_wres, p_wdep)
-    b.step(cfg, args.warmup)
-    host_in = {f: torch.empty(n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
-    host_out = {f: torch.empty(n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
-    st0 = b.get_bodies()
-    for f in _lib.BODY_FIELDS:
-        host_in[f].copy_(torch.from_numpy(st0[f]))
-    bin_ = _lib.Bodies(*[ctypes.cast(host_in[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS])
-    bout = _lib.Bodies(*[ctypes.cast(host_out[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS])
+    if lanes > 1:
+        ln = Lanes(_lib, scene, lanes, tuned, torch)
+        if run_learned:
+            ln.set_mlp(net, p_wres, p_wdep)
+        handles = ln.handles
+    else:
+        ln = None
+        b = new_batch(_lib, scene, stream, tuned)
+        if run_learned:
+            b.set_mlp(net)
+            b.set_judge(p_wres, p_wdep)
+        handles = [b]
+    if ln:
+        ln.step(cfg, args.warmup)
+    else:
+        b.step(cfg, args.warmup)
+    bufs = []  # per handle: (input Bodies, output Bodies, keep-alive tensors)
+    for h in handles:
+        hin = {f: torch.empty(h.n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
+        hout = {f: torch.empty(h.n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
+        st0 = h.get_bodies()
+        for f in _lib.BODY_FIELDS:
+            hin[f].copy_(torch.from_numpy(st0[f]))
+        bufs.append([_lib.Bodies(*[ctypes.cast(hin[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]),
+                     _lib.Bodies(*[ctypes.cast(hout[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]),
+                     (hin, hout)])
     L = _lib.lib()
     e_steps = args.steps
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(e_steps):
-        _lib.check(L.shapes_batch_set_bodies(b.handle, ctypes.byref(bin_)), "set_bodies")
-        _lib.check(L.shapes_batch_step(b.handle, ctypes.byref(cfg), 1), "step")
-        _lib.check(L.shapes_batch_get_bodies(b.handle, ctypes.byref(bout)), "get_bodies")
-        for f in _lib.BODY_FIELDS:  # next step's input is this step's result
-            host_in[f], host_out[f] = host_out[f], host_in[f]
-        bin_, bout = bout, bin_
+    if ln:
+        for st_ in ln.streams:
+            st_.wait_event(e0)
+
+    def e2e_loop(h, bf):
+        # body state in from pinned host memory, one step, state back out, each step
+        # (shapes_batches_step_io on this handle: one wait per step)
+        for _ in range(e_steps):
+            _lib.check(_lib.step_many_io([h], cfg, [bf[0]], [bf[1]]), "shapes_batches_step_io")
+            bf[0], bf[1] = bf[1], bf[0]  # next step's input is this step's result
+
+    if len(handles) > 1:  # one host thread per handle: each handle's copies overlap the others' steps
+        import threading
+
+        ths = [threading.Thread(target=e2e_loop, args=(h, bf)) for h, bf in zip(handles, bufs)]
+        for t_ in ths:
+            t_.start()
+        for t_ in ths:
+            t_.join()
+        for st_ in ln.streams:
+            ev = torch.cuda.Event()
+            ev.record(st_)
+            stream.wait_event(ev)
+    else:
+        e2e_loop(handles[0], bufs[0])
     e1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
     e_ms = max_over_ranks(e0.elapsed_time(e1), world)
     e2e_value = total_bodies * e_steps / (e_ms * 1e-3)
-    b.close()
+    if ln:
+        ln.close()
+    else:
+        b.close()
 
     # ---- roofline of the dominant kernel (profiled pass) -------------------
     solve_ms, solve_launches = prof["solve"]
@@ -601,7 +715,10 @@ def run_ours(args, rank, world, local):
                        "iterations": run_it, "start": "learned" if run_learned else "plain (previous-frame cache)",
                        "large_world_solver": ("coloured" if args.coloured else "ordered")
                        if args.workload == "container" else None,
-                       "parallelism": f"worlds sharded, {world} rank(s)",
+                       "parallelism": f"worlds sharded, {world} rank(s)" + (
+                           f"; on each GPU over {lanes} handles, one CUDA stream each, stepped together "
+                           "(shapes_batches_step)" if lanes > 1 else ""),
+                       "lanes": lanes,
                        "l2": "inputs larger than L2 (state + contacts + constraints of all worlds)",
                        "launch": "CUDA graph per step",
                        "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
@@ -616,7 +733,7 @@ def run_ours(args, rank, world, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * n_bodies,
                     "d2h_bytes_per_step": 10 * 8 * n_bodies},
-            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "gpu_launches": int(round(launches_per_step * args.steps * lanes)),
             "clocks": clocks.summary(),
             "stages_ms_per_step": {k: v[0] / prof_steps for k, v in prof.items()},
             "last_step": {"pairs": st["pairs"], "contacts": st["contacts"]},
@@ -780,6 +897,9 @@ def main():
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="handles (one CUDA stream each) the worlds are sharded over and stepped together "
+                         "(0 = 8 for scenes of 256 worlds or more, 4 from 64, else 1)")
     ap.add_argument("--no-incremental", action="store_true",
                     help="grid worlds search every body's 3x3 cells every frame (no fat-box pair lists)")
     ap.add_argument("--large-quality", action="store_true",

@@ -143,6 +143,25 @@ int shapes_batch_create(int32_t n_worlds, const int32_t* world_body_offsets,
  * Replaces: updateWorld (Engine/Main.hs:71-84) and stepWorld (Engine/Main.hs:88-89). */
 int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps);
 
+/* Steps n handles (each on its own stream, see shapes_batch_set_stream) by
+ * `nsteps` steps each, with all of them in flight at once: the solver of one
+ * handle's worlds overlaps the other stages of another's.  Each handle ends
+ * exactly as shapes_batch_step would leave it; the first failing status is
+ * returned.  Two handles sharing a stream are SHAPES_E_INVALID_ARG.
+ * No counterpart in the reference (a way to shard worlds on one GPU). */
+int shapes_batches_step(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, int32_t nsteps);
+
+/* One step of n handles with the body state in and out of caller buffers,
+ * everything asynchronous until one wait per handle: for each handle, in[k]
+ * is uploaded and checked (as shapes_batch_set_bodies), the step runs and the
+ * result is written to out[k] (as shapes_batch_get_bodies), with all handles'
+ * copies and steps in flight at once.  A handle whose input holds a
+ * non-finite value returns SHAPES_E_NAN with its state as before the call
+ * (its out[k] is then unspecified).  Pinned host buffers are copied by a
+ * kernel over the host link. */
+int shapes_batches_step_io(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, const shapes_bodies* in,
+                           shapes_bodies* out);
+
 /* Broadphase + contact generation on the current poses only (no forces, no
  * solve); results readable with the pair/contact getters.
  * Replaces: G.culledKeys . G.toGrid (Engine/Main.hs:75) followed by

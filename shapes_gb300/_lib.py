@@ -125,6 +125,11 @@ SIGNATURES = [
     ("shapes_batch_set_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_launch_groups", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_group_warps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batches_step", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.POINTER(Config),
+                                           ctypes.c_int32]),
+    ("shapes_batches_step_io", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                              ctypes.POINTER(Config), ctypes.POINTER(Bodies),
+                                              ctypes.POINTER(Bodies)]),
     ("shapes_batch_get_launch", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _ip]),
     ("shapes_batch_set_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_batch_get_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
@@ -200,6 +205,25 @@ def make_bodies(arrays: dict) -> tuple[Bodies, list]:
     keep = [np.ascontiguousarray(arrays[f], dtype=np.float64) for f in BODY_FIELDS]
     b = Bodies(*[_ptr(a, _dp) for a in keep])
     return b, keep
+
+
+def step_many(batches, cfg: "Config", nsteps: int = 1) -> None:
+    """Steps several handles (each on its own stream) with all their steps in
+    flight at once (shapes_batches_step)."""
+    arr = (ctypes.c_void_p * len(batches))(*[b.handle for b in batches])
+    check(lib().shapes_batches_step(arr, len(batches), ctypes.byref(cfg), nsteps), "shapes_batches_step")
+
+
+def step_many_io(batches, cfg: "Config", inputs, outputs) -> int:
+    """One step of several handles with the body state read from `inputs` and
+    the result written to `outputs` (sequences of Bodies structs, one per
+    handle; shapes_batches_step_io).  Returns the status (0 or the first
+    error, e.g. SHAPES_E_NAN for refused input)."""
+    n = len(batches)
+    arr = (ctypes.c_void_p * n)(*[b.handle for b in batches])
+    ins = (Bodies * n)(*inputs)
+    outs = (Bodies * n)(*outputs)
+    return int(lib().shapes_batches_step_io(arr, n, ctypes.byref(cfg), ins, outs))
 
 
 class Batch:

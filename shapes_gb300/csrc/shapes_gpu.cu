@@ -1006,84 +1006,131 @@ struct shapes_batch {
          "restore");
   }
 
-  /* Runs `nsteps` steps (or one collide when !solve) with overflow retries. */
-  int run(const shapes_config& cfg, int32_t nsteps, bool solve) {
+  /* Asynchronous body-state upload for shapes_batches_step_io: caller arrays
+   * into the staging arrays with the finiteness check into the bad-input
+   * counter, then the staged state into the live arrays unless the check
+   * failed, and a re-pose of the bodies whose pose inputs changed. */
+  void io_upload(const shapes_bodies* in);
+  void io_commit() {
+    shapes::Ptr10 p{};
+    for (int k = 0; k < 10; ++k) {
+      p.src[k] = body_stage[k];
+      p.dst[k] = body[k];
+    }
+    shapes::k_commit_bodies<<<grid_for(N, 256), 256, 0, stream>>>(p, N, body_changed,
+                                                                  counters + shapes::kCntBadInput);
+    Dev d = view(0);
+    shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, 0.0, 0, body_changed);
+    ck(cudaGetLastError(), "launch");
+  }
+  void io_download(shapes_bodies* out);
+
+  /* One call of `nsteps` steps (or one collide when !solve) in three parts,
+   * so that several handles can have their steps in flight at once
+   * (shapes_batches_step): prepare() sizes buffers and groups, enqueue()
+   * snapshots the state for a retry and launches the steps and the read-back
+   * of the counters without waiting, finish() (after the stream is drained)
+   * checks them: kRunRetry means the buffers were too small, the state was
+   * restored and grown, and the call must be enqueued again. */
+  static constexpr int kRunRetry = 1;
+  int run_retries = 0, run_saved_cache_buf = 0, run_saved_cap = 0;
+  unsigned long long run_counters[shapes::kCntSlots] = {0};
+
+  void prepare(const shapes_config& cfg, bool solve) {
     ensure_items(solve ? cfg.iterations : 0);
     /* (re)build the solver groups before any device view of this call is
      * taken: make_groups reallocates the group arrays */
     if (solve && grouped_iterations != cfg.iterations) make_groups(cfg.iterations);
     if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
-    int retries = 0;
-    for (;;) {
-      ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntSlots, stream), "memset");
-      const int saved_cache_buf = cache_buf;
-      const int saved_cap = contact_cap;
-      if (solve) snapshot();
-      unsigned long long agg[shapes::kCntSlots] = {0};
-      unsigned long long h[shapes::kCntSlots];
-      for (int s = 0; s < (solve ? nsteps : 1); ++s) {
-        const int wb = 1 - cache_buf;
-        if (solve)
-          launch_step(cfg, wb);
-        else
-          enqueue_step(cfg, false, wb);
-        if (solve) cache_buf = wb;
-        results_buf = wb;
-        if (solve && nsteps > 1) {
-          /* accumulate per-step counters on the host only for the last step */
+  }
+
+  void enqueue_begin(bool solve) {
+    ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntSlots, stream), "memset");
+    run_saved_cache_buf = cache_buf;
+    run_saved_cap = contact_cap;
+    if (solve) snapshot();
+  }
+  void enqueue_one(const shapes_config& cfg, bool solve) {
+    const int wb = 1 - cache_buf;
+    if (solve)
+      launch_step(cfg, wb);
+    else
+      enqueue_step(cfg, false, wb);
+    if (solve) cache_buf = wb;
+    results_buf = wb;
+  }
+  void enqueue_end() {
+    ck(cudaMemcpyAsync(run_counters, counters, sizeof(run_counters), cudaMemcpyDeviceToHost, stream), "read counters");
+  }
+  void enqueue(const shapes_config& cfg, int32_t nsteps, bool solve) {
+    enqueue_begin(solve);
+    for (int s = 0; s < (solve ? nsteps : 1); ++s) enqueue_one(cfg, solve);
+    enqueue_end();
+  }
+
+  int finish(const shapes_config& cfg, bool solve) {
+    ck(cudaStreamSynchronize(stream), "step");
+    ck(cudaGetLastError(), "launch");
+    if (profiling) collect_profile();
+    const unsigned long long* agg = run_counters;
+    if (agg[shapes::kCntMlpErr]) {
+      g_last_error = "learned warm start: a bounded tensor-core wait gave up";
+      return SHAPES_E_TIMEOUT;
+    }
+    if (!agg[shapes::kCntOverflow] && solve && !large_worlds.empty()) {
+      std::vector<unsigned long long> ctl(8 * large_worlds.size());
+      ck(cudaMemcpy(ctl.data(), lw_ctl, sizeof(unsigned long long) * ctl.size(), cudaMemcpyDeviceToHost), "ctl");
+      for (size_t k = 0; k < large_worlds.size(); ++k)
+        if (ctl[8 * k + 1]) {
+          g_last_error = "large-world solver: a bounded wait gave up";
+          return SHAPES_E_TIMEOUT;
         }
-      }
-      ck(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, stream), "read counters");
-      ck(cudaStreamSynchronize(stream), "step");
-      ck(cudaGetLastError(), "launch");
-      if (profiling) collect_profile();
-      for (int k = 0; k < shapes::kCntSlots; ++k) agg[k] = h[k];
-      if (agg[shapes::kCntMlpErr]) {
-        g_last_error = "learned warm start: a bounded tensor-core wait gave up";
-        return SHAPES_E_TIMEOUT;
-      }
-      if (!agg[shapes::kCntOverflow] && solve && !large_worlds.empty()) {
-        std::vector<unsigned long long> ctl(8 * large_worlds.size());
-        ck(cudaMemcpy(ctl.data(), lw_ctl, sizeof(unsigned long long) * ctl.size(), cudaMemcpyDeviceToHost), "ctl");
-        for (size_t k = 0; k < large_worlds.size(); ++k)
-          if (ctl[8 * k + 1]) {
-            g_last_error = "large-world solver: a bounded wait gave up";
-            return SHAPES_E_TIMEOUT;
-          }
-      }
-      if (!agg[shapes::kCntOverflow]) {
-        stats.pairs = (int64_t)agg[shapes::kCntPairs];
-        stats.contacts = (int64_t)agg[shapes::kCntContacts];
-        stats.cache_hits = (int64_t)agg[shapes::kCntHits] - (int64_t)agg[shapes::kCntPredicted];
-        stats.predicted = (int64_t)agg[shapes::kCntPredicted];
-        stats.reverted = (int64_t)agg[shapes::kCntReverted];
-        stats.solver_items = (int64_t)agg[shapes::kCntItems];
-        stats.solver_levels = (int64_t)agg[shapes::kCntLevels];
-        stats.retries = retries;
-        have_results = true;
-        return SHAPES_OK;
-      }
-      if (++retries > 6) return SHAPES_E_CAPACITY;
-      /* undo, grow, redo */
-      cache_buf = saved_cache_buf;
-      if (solve) restore(saved_cap);
-      ck(cudaStreamSynchronize(stream), "restore");
-      if (agg[shapes::kCntOverflow] & 4ull) { /* an adjacency list was full */
-        if (nbr_cap > (1 << 14)) return SHAPES_E_CAPACITY;
-        nbr_cap *= 2;
-        invalidate_graphs();
-        setup_incremental();
-      }
-      reset_incremental(); /* the lists follow the undone steps' poses */
-      if (agg[shapes::kCntOverflow] & ~4ull) {
-        const int64_t np = (int64_t)pair_cap * ((agg[shapes::kCntOverflow] & 1ull) ? 2 : 1);
-        const int64_t nc = (int64_t)contact_cap * 2;
-        if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
-        alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
-      }
-      ensure_items(solve ? cfg.iterations : 0);
-      if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
-      if (solve) pose(0, 0.0);
+    }
+    if (!agg[shapes::kCntOverflow]) {
+      stats.pairs = (int64_t)agg[shapes::kCntPairs];
+      stats.contacts = (int64_t)agg[shapes::kCntContacts];
+      stats.cache_hits = (int64_t)agg[shapes::kCntHits] - (int64_t)agg[shapes::kCntPredicted];
+      stats.predicted = (int64_t)agg[shapes::kCntPredicted];
+      stats.reverted = (int64_t)agg[shapes::kCntReverted];
+      stats.solver_items = (int64_t)agg[shapes::kCntItems];
+      stats.solver_levels = (int64_t)agg[shapes::kCntLevels];
+      stats.retries = run_retries;
+      have_results = true;
+      return SHAPES_OK;
+    }
+    if (++run_retries > 6) return SHAPES_E_CAPACITY;
+    /* undo, grow, redo */
+    const unsigned long long overflow = agg[shapes::kCntOverflow];
+    cache_buf = run_saved_cache_buf;
+    if (solve) restore(run_saved_cap);
+    ck(cudaStreamSynchronize(stream), "restore");
+    if (overflow & 4ull) { /* an adjacency list was full */
+      if (nbr_cap > (1 << 14)) return SHAPES_E_CAPACITY;
+      nbr_cap *= 2;
+      invalidate_graphs();
+      setup_incremental();
+    }
+    reset_incremental(); /* the lists follow the undone steps' poses */
+    if (overflow & ~4ull) {
+      const int64_t np = (int64_t)pair_cap * ((overflow & 1ull) ? 2 : 1);
+      const int64_t nc = (int64_t)contact_cap * 2;
+      if (np > INT32_MAX / 2 || nc > INT32_MAX / 2) return SHAPES_E_CAPACITY;
+      alloc_step_buffers((int32_t)np, (int32_t)std::max<int64_t>(nc, 2 * np), solve ? cfg.iterations : 0);
+    }
+    ensure_items(solve ? cfg.iterations : 0);
+    if (solve && (learned_on(cfg) || collect_on(cfg))) ensure_row_buffers();
+    if (solve) pose(0, 0.0);
+    return kRunRetry;
+  }
+
+  /* Runs `nsteps` steps (or one collide when !solve) with overflow retries. */
+  int run(const shapes_config& cfg, int32_t nsteps, bool solve) {
+    prepare(cfg, solve);
+    run_retries = 0;
+    for (;;) {
+      enqueue(cfg, nsteps, solve);
+      const int rc = finish(cfg, solve);
+      if (rc != kRunRetry) return rc;
     }
   }
 
@@ -1423,6 +1470,100 @@ int shapes_batch_step(shapes_batch* b, const shapes_config* cfg, int32_t nsteps)
   });
 }
 
+int shapes_batches_step(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, int32_t nsteps) {
+  if (!bs || n < 1 || nsteps < 0) return SHAPES_E_INVALID_ARG;
+  for (int32_t k = 0; k < n; ++k) {
+    if (!bs[k]) return SHAPES_E_INVALID_ARG;
+    for (int32_t j = 0; j < k; ++j)
+      if (bs[j] == bs[k] || bs[j]->stream == bs[k]->stream) return SHAPES_E_INVALID_ARG;
+  }
+  const int rc0 = check_cfg(cfg);
+  if (rc0 != SHAPES_OK) return rc0;
+  if (nsteps == 0) return SHAPES_OK;
+  return guarded([&]() -> int {
+    /* every handle's steps in flight on its own stream, launched step by
+     * step in turn (a stream's launch queue is finite: launching all of one
+     * handle's steps first would block until most of them had run), then
+     * each finished */
+    for (int32_t k = 0; k < n; ++k) {
+      ck(cudaSetDevice(bs[k]->device), "cudaSetDevice");
+      bs[k]->prepare(*cfg, true);
+      bs[k]->run_retries = 0;
+      bs[k]->enqueue_begin(true);
+    }
+    for (int32_t s = 0; s < nsteps; ++s)
+      for (int32_t k = 0; k < n; ++k) bs[k]->enqueue_one(*cfg, true);
+    for (int32_t k = 0; k < n; ++k) bs[k]->enqueue_end();
+    int rc = SHAPES_OK;
+    for (int32_t k = 0; k < n; ++k) {
+      shapes_batch* b = bs[k];
+      int r = b->finish(*cfg, true);
+      while (r == shapes_batch::kRunRetry) { /* this handle alone, as shapes_batch_step would */
+        b->enqueue(*cfg, nsteps, true);
+        r = b->finish(*cfg, true);
+      }
+      b->residual_valid = r == SHAPES_OK && ((cfg->flags & SHAPES_FLAG_RESIDUAL) || b->learned_on(*cfg));
+      if (r != SHAPES_OK && rc == SHAPES_OK) rc = r;
+    }
+    return rc;
+  });
+}
+
+int shapes_batches_step_io(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, const shapes_bodies* in,
+                           shapes_bodies* out) {
+  if (!bs || n < 1 || !in || !out) return SHAPES_E_INVALID_ARG;
+  for (int32_t k = 0; k < n; ++k) {
+    if (!bs[k] || !body_arrays_ok(&in[k]) || !body_arrays_ok(&out[k])) return SHAPES_E_INVALID_ARG;
+    for (int32_t j = 0; j < k; ++j)
+      if (bs[j] == bs[k] || bs[j]->stream == bs[k]->stream) return SHAPES_E_INVALID_ARG;
+  }
+  const int rc0 = check_cfg(cfg);
+  if (rc0 != SHAPES_OK) return rc0;
+  return guarded([&]() -> int {
+    for (int32_t k = 0; k < n; ++k) {
+      shapes_batch* b = bs[k];
+      ck(cudaSetDevice(b->device), "cudaSetDevice");
+      b->prepare(*cfg, true);
+      b->run_retries = 0;
+      b->enqueue_begin(true); /* zeroes the counters and keeps the state a refusal returns to */
+      b->io_upload(&in[k]);
+      b->io_commit();
+    }
+    for (int32_t k = 0; k < n; ++k) bs[k]->enqueue_one(*cfg, true);
+    for (int32_t k = 0; k < n; ++k) {
+      bs[k]->io_download(&out[k]);
+      bs[k]->enqueue_end();
+    }
+    int rc = SHAPES_OK;
+    for (int32_t k = 0; k < n; ++k) {
+      shapes_batch* b = bs[k];
+      ck(cudaStreamSynchronize(b->stream), "step");
+      int r;
+      if (b->run_counters[shapes::kCntBadInput]) { /* refused: undo the step taken on the old state */
+        b->cache_buf = b->run_saved_cache_buf;
+        b->restore(b->run_saved_cap);
+        b->pose(0, 0.0);
+        ck(cudaStreamSynchronize(b->stream), "restore");
+        b->have_results = false;
+        r = SHAPES_E_NAN;
+      } else {
+        r = b->finish(*cfg, true);
+        while (r == shapes_batch::kRunRetry) { /* grown and restored: the staged input again, alone */
+          b->enqueue_begin(true);
+          b->io_commit();
+          b->enqueue_one(*cfg, true);
+          b->io_download(&out[k]);
+          b->enqueue_end();
+          r = b->finish(*cfg, true);
+        }
+        b->residual_valid = r == SHAPES_OK && ((cfg->flags & SHAPES_FLAG_RESIDUAL) || b->learned_on(*cfg));
+      }
+      if (r != SHAPES_OK && rc == SHAPES_OK) rc = r;
+    }
+    return rc;
+  });
+}
+
 int shapes_batch_collide(shapes_batch* b) {
   if (!b) return SHAPES_E_INVALID_ARG;
   shapes_config cfg{};
@@ -1450,6 +1591,45 @@ static bool mapped_host10(double* const host[10], double* dev[10]) {
 }
 
 static dim3 copy10_grid(int n) { return dim3((unsigned)std::min<int64_t>((n + 255) / 256, 1024), 10); }
+
+void shapes_batch::io_upload(const shapes_bodies* in) {
+  double* bp[10];
+  body_ptrs(in, bp);
+  double* dp[10];
+  if (mapped_host10(bp, dp)) {
+    shapes::Ptr10 p{};
+    for (int k = 0; k < 10; ++k) {
+      p.src[k] = dp[k];
+      p.dst[k] = body_stage[k];
+    }
+    shapes::k_copy10<<<copy10_grid(N), 256, 0, stream>>>(p, N, counters + shapes::kCntBadInput);
+  } else {
+    for (int k = 0; k < 10; ++k)
+      ck(cudaMemcpyAsync(body_stage[k], bp[k], sizeof(double) * N, cudaMemcpyHostToDevice, stream), "upload");
+    shapes::k_check_finite<<<grid_for(10LL * N, 256), 256, 0, stream>>>(
+        body_stage[0], body_stage[1], body_stage[2], body_stage[3], body_stage[4], body_stage[5], body_stage[6],
+        body_stage[7], body_stage[8], body_stage[9], N, counters + shapes::kCntBadInput);
+  }
+  ck(cudaGetLastError(), "launch");
+}
+
+void shapes_batch::io_download(shapes_bodies* out) {
+  double* bp[10];
+  body_ptrs(out, bp);
+  double* dp[10];
+  if (mapped_host10(bp, dp)) {
+    shapes::Ptr10 p{};
+    for (int k = 0; k < 10; ++k) {
+      p.src[k] = body[k];
+      p.dst[k] = dp[k];
+    }
+    shapes::k_copy10<<<copy10_grid(N), 256, 0, stream>>>(p, N, nullptr);
+    ck(cudaGetLastError(), "launch");
+  } else {
+    for (int k = 0; k < 10; ++k)
+      ck(cudaMemcpyAsync(bp[k], body[k], sizeof(double) * N, cudaMemcpyDeviceToHost, stream), "download");
+  }
+}
 
 int shapes_batch_get_bodies(shapes_batch* b, shapes_bodies* out) {
   if (!b || !body_arrays_ok(out)) return SHAPES_E_INVALID_ARG;

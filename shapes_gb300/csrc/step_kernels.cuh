@@ -210,8 +210,13 @@ __global__ void k_copy10(Ptr10 p, int n, unsigned long long* bad_flag) {
 /* Staged body state -> live arrays, one thread per body; changed[g] = 1 when
  * a field the pose depends on (position, rotation, inverse masses, which set
  * the static flag) differs bit for bit from the live value. */
-__global__ void k_commit_bodies(Ptr10 p, int n, uint8_t* changed) {
+__global__ void k_commit_bodies(Ptr10 p, int n, uint8_t* changed, const unsigned long long* bad = nullptr) {
+  const bool skip = bad && *bad != 0; /* refused input: the live state stays */
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
+    if (skip) {
+      changed[g] = 0;
+      continue;
+    }
     bool c = false;
 #pragma unroll
     for (int k = 0; k < 10; ++k) {

@@ -458,3 +458,92 @@ def test_pinned_host_buffers_round_trip():
         assert_bits_equal(gc[f], gb[f], f"refused pinned input {f}")
     a.close()
     b.close()
+
+
+def test_batches_step_concurrent_handles():
+    """Worlds sharded over three handles on three streams, stepped together:
+    each handle matches the oracle, including one whose adjacency lists
+    overflow (it retries alone); two handles on one stream are refused."""
+    import torch
+
+    big = scenes.subset_worlds(scenes.batched_columns(n_worlds=48), list(range(36)))
+    parts = [scenes.subset_worlds(big, list(range(k, 36, 2))) for k in range(2)]
+    pile = scenes.SceneBuilder()
+    pile.add(scenes.rectangle_vertices(60.0, 1.0), (0.0, -0.5), static=True)
+    for k in range(40):
+        pile.add(scenes.rectangle_vertices(1.0, 1.0), (0.01 * k, 5.0 + 0.02 * k))
+    for k in range(40):
+        pile.add(scenes.rectangle_vertices(1.0, 1.0), (-20.0 + k, 0.6))
+    parts.append(pile.build(dt=1.0 / 60.0, baumgarte=0.01, slop=0.02, accel=(0.0, -9.8), iterations=8, steps=1))
+    streams = [torch.cuda.Stream() for _ in parts]
+    hs = []
+    for sc_, st in zip(parts, streams):
+        h = batch_from_scene(sc_)
+        h.set_stream(st.cuda_stream)
+        hs.append(h)
+    hs[1].set_launch_groups(2, 128, 4)
+    cfg = config_of(parts[0])
+    _lib.step_many(hs, cfg, 25)
+    for h, sc_ in zip(hs, parts):
+        ow = oracle_worlds(sc_)
+        step_oracles(ow, sc_, 25, iterations=cfg.iterations)
+        compare_bodies(h, ow, sc_, "step_many")
+    assert hs[2].stats()["retries"] >= 1
+    hs[1].set_stream(streams[0].cuda_stream)
+    with pytest.raises(_lib.ShapesError):
+        _lib.step_many(hs, cfg, 1)
+    for h in hs:
+        h.close()
+
+
+def test_batches_step_io_matches_separate_calls():
+    """One asynchronous step of three handles with state in and out of pinned
+    buffers equals set_bodies + step + get_bodies on each; a non-finite input
+    is refused with that handle's state unchanged, the others still step."""
+    import ctypes
+
+    import torch
+
+    big = scenes.subset_worlds(scenes.batched_columns(n_worlds=48), list(range(30)))
+    parts = [scenes.subset_worlds(big, list(range(k, 30, 3))) for k in range(3)]
+    cfg = config_of(parts[0])
+    streams = [torch.cuda.Stream() for _ in parts]
+    hs, refs, ins, outs, keep = [], [], [], [], []
+    for sc_, st in zip(parts, streams):
+        h, r = batch_from_scene(sc_), batch_from_scene(sc_)
+        h.set_stream(st.cuda_stream)
+        h.step(cfg, 20)
+        r.step(cfg, 20)
+        n = h.n_bodies
+        pin_in = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
+        pin_out = {f: torch.empty(n, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
+        cur = h.get_bodies()
+        for f in _lib.BODY_FIELDS:
+            pin_in[f].copy_(torch.from_numpy(cur[f]))
+        ins.append(_lib.Bodies(*[ctypes.cast(pin_in[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]))
+        outs.append(_lib.Bodies(*[ctypes.cast(pin_out[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]))
+        keep.append((pin_in, pin_out))
+        hs.append(h)
+        refs.append(r)
+    for it in range(3):
+        assert _lib.step_many_io(hs, cfg, ins, outs) == 0
+        for r in refs:
+            r.step(cfg, 1)
+        for (pin_in, pin_out), r in zip(keep, refs):
+            want = r.get_bodies()
+            for f in STATE_FIELDS:
+                assert_bits_equal(pin_out[f].numpy(), want[f], f"step_io out {f} step {it}")
+            for f in _lib.BODY_FIELDS:
+                pin_in[f].copy_(pin_out[f])
+    before = hs[1].get_bodies()
+    keep[1][0]["pos_y"][3] = float("nan")
+    assert _lib.step_many_io(hs, cfg, ins, outs) == _lib.SHAPES_E_NAN
+    after = hs[1].get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(after[f], before[f], f"refused handle {f}")
+    refs[0].step(cfg, 1)
+    want0 = refs[0].get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(keep[0][1][f].numpy(), want0[f], f"other handle still stepped {f}")
+    for h in hs + refs:
+        h.close()
