@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -502,30 +503,32 @@ __global__ void k_mlp_update(float* params, float* m, float* v, const float* slo
 /* Launch helpers                                                             */
 /* ------------------------------------------------------------------------ */
 
-int num_sms() {
-  static int sms = 0;
-  if (!sms) {
+int num_sms() { /* handles may be used from several host threads: atomics */
+  static std::atomic<int> sms{0};
+  int v = sms.load(std::memory_order_relaxed);
+  if (!v) {
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 148;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 148;
+    sms.store(v, std::memory_order_relaxed);
   }
-  return sms;
+  return v;
 }
 
 /* Shared-memory limits of the two tensor-core kernels, set once per device
  * (outside any stream capture: prepare_device() runs before a step is
  * captured). */
 cudaError_t set_smem_attrs() {
-  static unsigned long long done = 0; /* bit per device */
+  static std::atomic<unsigned long long> done{0}; /* bit per device */
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 64 && ((done >> dev) & 1ull)) return cudaSuccess;
+  if (dev < 64 && ((done.load() >> dev) & 1ull)) return cudaSuccess;
   e = cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, kPredSmem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem);
-  if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
+  if (e == cudaSuccess && dev < 64) done.fetch_or(1ull << dev);
   return e;
 }
 
