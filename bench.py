@@ -312,6 +312,7 @@ def new_batch(_lib, scene, stream, tuned=None):
     if tuned:
         b.set_launch_groups(*tuned[:3])
         b.set_world_order(tuned[3])
+        b.set_parallel_levels(tuned[4])
     return b
 
 
@@ -340,6 +341,7 @@ class Lanes:
                 b.set_incremental(False)
             if tuned:
                 b.set_launch_groups(*tuned[:3])
+                b.set_parallel_levels(tuned[4])
             b.set_world_order(np.arange(len(sc["world_body_offsets"]) - 1, dtype=np.int32))
             self.handles.append(b)
         assert sum(len(w) for w in self.worlds) == W
@@ -483,12 +485,14 @@ def run_ours(args, rank, world, local):
     # ---- autotune the solver packing on a settled copy (setup, untimed) ------
     tuned = None
     if args.packing:
-        wpg, thr, gw = (int(x) for x in args.packing.split(","))
-        tuned = (wpg, thr, gw, np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable").astype(np.int32))
-    elif not args.no_tune and int(len(scene["world_body_offsets"]) - 1) > 1:
+        vals = [int(x) for x in args.packing.split(",")]
+        wpg, thr, gw = vals[:3]
+        par = bool(vals[3]) if len(vals) > 3 else True
+        tuned = (wpg, thr, gw, np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable").astype(np.int32), par)
+    elif not args.no_tune:
         t = new_batch(_lib, scene, stream)
         t.step(cfg_for(plain_it, False), args.tune_after)
-        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(),)
+        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(), t.parallel_levels())
         t.close()
 
     n_worlds = len(scene["world_body_offsets"]) - 1
@@ -724,7 +728,7 @@ def run_ours(args, rank, world, local):
                        "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
                        else "grid, full 3x3 search every frame",
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
-                                          "warps_per_group": tuned[2],
+                                          "warps_per_group": tuned[2], "parallel_levels": bool(tuned[4]),
                                           "world_order": "by size" if np.array_equal(
                                               tuned[3], np.argsort(-np.diff(scene["world_body_offsets"]),
                                                                    kind="stable")) else "by dependency levels"}
@@ -890,8 +894,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--worlds", type=int, default=None, help="override the world count (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the solver-packing autotuner")
-    ap.add_argument("--packing", default="", help="fixed solver packing 'worlds_per_group,threads,warps_per_group' "
-                    "(size order) instead of the autotuner")
+    ap.add_argument("--packing", default="", help="fixed solver packing 'worlds_per_group,threads,warps_per_group"
+                    "[,parallel_levels]' (size order) instead of the autotuner")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
     ap.add_argument("--tune-steps", type=int, default=30, help="steps per autotuner trial")
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")

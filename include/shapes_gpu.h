@@ -238,6 +238,13 @@ int shapes_batch_set_launch_groups(shapes_batch* b, int32_t worlds_per_group, in
  * levels); 1 (default) = one warp per group, `threads` / 32 groups per CTA.
  * Results do not depend on it. */
 int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps);
+/* Cooperative groups compute the dependency levels of the updates in
+ * parallel (default 1): one walk over each world's contacts records every
+ * update's predecessors, then the passes are levelled chunk by chunk to a
+ * fixed point; 0 walks over every update in order, one thread per world.
+ * Both give every update the same level. */
+int shapes_batch_set_parallel_levels(shapes_batch* b, int32_t enabled);
+int shapes_batch_get_parallel_levels(shapes_batch* b, int32_t* enabled);
 /* The packing in use (any pointer may be NULL). */
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps);
 /* The order in which worlds are packed into groups: a permutation of
@@ -251,7 +258,8 @@ int shapes_batch_get_world_levels(shapes_batch* b, int32_t* levels);
 
 /* Autotuner for the solver packing: from the current state, times
  * `steps_per_trial` steps for each candidate (worlds per group x warps per
- * CTA, and worlds per group x warps per cooperative group) after one untimed
+ * CTA, and worlds per group x warps per cooperative group x parallel or
+ * walked dependency levels, each in size and in level order) after one untimed
  * step, restores the state exactly after every trial, and keeps the fastest (read it back with
  * shapes_batch_get_launch).  The world state and cache are left exactly as they were; results
  * never depend on the packing.  Tune on a state that has contacts (e.g. after

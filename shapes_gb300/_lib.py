@@ -125,6 +125,8 @@ SIGNATURES = [
     ("shapes_batch_set_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_launch_groups", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     ("shapes_batch_set_group_warps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_set_parallel_levels", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_get_parallel_levels", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_batches_step", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.POINTER(Config),
                                            ctypes.c_int32]),
     ("shapes_batches_step_io", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
@@ -342,6 +344,11 @@ class Batch:
               "shapes_batch_get_launch")
         return wpg.value, thr.value, gw.value
 
+    def parallel_levels(self) -> bool:
+        v = ctypes.c_int32()
+        check(lib().shapes_batch_get_parallel_levels(self._h, ctypes.byref(v)), "shapes_batch_get_parallel_levels")
+        return bool(v.value)
+
     def world_order(self) -> np.ndarray:
         out = np.empty(self.n_worlds, dtype=np.int32)
         check(lib().shapes_batch_get_world_order(self._h, _ptr(out, _ip)), "shapes_batch_get_world_order")
@@ -357,6 +364,10 @@ class Batch:
         out = np.empty(self.n_worlds, dtype=np.int32)
         check(lib().shapes_batch_get_world_levels(self._h, _ptr(out, _ip)), "shapes_batch_get_world_levels")
         return out
+
+    def set_parallel_levels(self, enabled: bool) -> None:
+        """Cooperative groups: dependency levels in parallel (default) or by a walk over the updates."""
+        check(lib().shapes_batch_set_parallel_levels(self._h, int(bool(enabled))), "shapes_batch_set_parallel_levels")
 
     def set_group_warps(self, warps: int) -> None:
         """Warps cooperating on each solver group (1, 2, 4 or 8)."""

@@ -157,6 +157,9 @@ struct shapes_batch {
   Con* con = nullptr;
   /* scheduler */
   int32_t* last = nullptr;
+  int32_t* last_hit = nullptr; /* [N] scheduler scratch: last cache-hit contact of a body */
+  int4* c_pred = nullptr;      /* [contact_cap] previous contacts of each side (any / hit) */
+  int32_t* c_lvl = nullptr;    /* [2 * contact_cap] dependency levels of two consecutive passes */
   uint32_t* items = nullptr;
   int32_t* ilevel = nullptr;
   uint32_t* isorted = nullptr;
@@ -199,6 +202,7 @@ struct shapes_batch {
   int32_t target_group_bodies = 0;
   int32_t solve_threads = 32;
   int32_t group_warps = 1; /* > 1: that many warps cooperate on each group (k_group_solve) */
+  bool parallel_levels = true; /* cooperative groups: dependency levels by chunked fixed point */
   std::vector<int32_t> world_order; /* packing order of the worlds; empty = by body count */
   /* scans */
   int32_t* tile_sums = nullptr;
@@ -426,6 +430,9 @@ struct shapes_batch {
     d.world_pair_off = world_pair_off;
     d.world_contact_off = cwo[write_buf];
     d.last = last;
+    d.last_hit = last_hit;
+    d.c_pred = c_pred;
+    d.c_lvl = c_lvl;
     d.items = items;
     d.ilevel = ilevel;
     d.isorted = isorted;
@@ -478,6 +485,9 @@ struct shapes_batch {
     np_perm = nullptr;
     for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
     dfree(c_ga); dfree(c_gb); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
+    dfree(c_pred); dfree(c_lvl);
+    c_pred = nullptr;
+    c_lvl = nullptr;
     dfree(items); dfree(ilevel); dfree(isorted); dfree(ihist); dfree(gdesc); dfree(ghist); dfree(idesc);
     idesc = nullptr;
     dfree(tile_sums);
@@ -540,6 +550,8 @@ struct shapes_batch {
     c_hit = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
     c_val = dalloc<double>(5 * (size_t)contact_cap, "cudaMalloc contacts");
     con = dalloc<Con>(contact_cap, "cudaMalloc constraints");
+    c_pred = dalloc<int4>(contact_cap, "cudaMalloc constraints");
+    c_lvl = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc constraints");
     items = dalloc<uint32_t>(1, "cudaMalloc items");
     ilevel = dalloc<int32_t>(item_cap, "cudaMalloc items");
     isorted = dalloc<uint32_t>(1, "cudaMalloc items");
@@ -949,15 +961,19 @@ struct shapes_batch {
       const int ints = std::min<int>(smem_last_cap, 40 * 1024 / (int)sizeof(int32_t)) & ~1;
       const size_t bytes = (size_t)ints * sizeof(int32_t);
       stage(4, 1, [&]() {
-        if (group_warps == 2)
-          shapes::k_group_solve<2><<<G, 64, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
-                                                             cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
-        else if (group_warps == 4)
-          shapes::k_group_solve<4><<<G, 128, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
-                                                              cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
-        else
-          shapes::k_group_solve<8><<<G, 256, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external,
-                                                              cfg.accel_x, cfg.accel_y, cfg.dt, G, ints);
+#define SHAPES_GROUP_SOLVE(PW, PL)                                                                              \
+  shapes::k_group_solve<PW, PL><<<G, 32 * PW, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, \
+                                                               cfg.accel_x, cfg.accel_y, cfg.dt, G, ints)
+        if (parallel_levels) {
+          if (group_warps == 2) SHAPES_GROUP_SOLVE(2, true);
+          else if (group_warps == 4) SHAPES_GROUP_SOLVE(4, true);
+          else SHAPES_GROUP_SOLVE(8, true);
+        } else {
+          if (group_warps == 2) SHAPES_GROUP_SOLVE(2, false);
+          else if (group_warps == 4) SHAPES_GROUP_SOLVE(4, false);
+          else SHAPES_GROUP_SOLVE(8, false);
+        }
+#undef SHAPES_GROUP_SOLVE
       });
     } else if (G > 0) {
       stage(4, 1, [&]() {
@@ -1167,7 +1183,7 @@ struct shapes_batch {
       dfree(body_stage[k]);
     }
     dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags); dfree(body_changed);
-    dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(world_levels);
+    dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(last_hit); dfree(world_levels);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(active);
     active = nullptr;
@@ -1203,6 +1219,7 @@ struct shapes_batch {
     if (!cwo[0])
       for (int k = 0; k < 2; ++k) cwo[k] = dalloc<int32_t>(n_worlds + 1, "cudaMalloc");
     last = dalloc<int32_t>(N, "cudaMalloc");
+    last_hit = dalloc<int32_t>(N, "cudaMalloc");
     world_levels = dalloc<int32_t>(n_worlds, "cudaMalloc");
     ck(cudaMemset(world_levels, 0, sizeof(int32_t) * n_worlds), "memset");
     if (!counters) counters = dalloc<unsigned long long>(shapes::kCntSlots, "cudaMalloc");
@@ -1294,7 +1311,7 @@ struct shapes_batch {
     dfree(radius);
     dfree(metric_part);
     for (int k = 0; k < 2; ++k) dfree(cwo[k]);
-    dfree(last); dfree(world_levels); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
+    dfree(last); dfree(last_hit); dfree(world_levels); dfree(group_depth); dfree(group_world_off); dfree(group_worlds);
     dfree(phase_clock);
     dfree(counters);
     dfree(np_cls);
@@ -1974,24 +1991,27 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       if (lv[a] != lv[c]) return lv[a] > lv[c];
       return (b->h_world_body_off[a + 1] - b->h_world_body_off[a]) > (b->h_world_body_off[c + 1] - b->h_world_body_off[c]);
     });
-    /* (worlds per group, threads per CTA, warps per group, level order) */
-    std::vector<std::array<int, 4>> cands;
-    auto add = [&](int wpg, int thr, int gw, int lo) {
-      const std::array<int, 4> c{wpg, thr, gw, lo};
+    /* (worlds per group, threads per CTA, warps per group, level order,
+     * parallel levels) */
+    std::vector<std::array<int, 5>> cands;
+    auto add = [&](int wpg, int thr, int gw, int lo, int par) {
+      const std::array<int, 5> c{wpg, thr, gw, lo, par};
       if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds && std::find(cands.begin(), cands.end(), c) == cands.end())
         cands.push_back(c);
     };
     for (int lo : {0, 1}) {
       for (int wpg : {1, base / 2, base, base + 1, 2 * base})
-        for (int thr : {32, 64, 128}) add(wpg, thr, 1, lo);
+        for (int thr : {32, 64, 128}) add(std::min(wpg, W), thr, 1, lo, 0);
       for (int wpg : {1, 2, base, base + 1, 2 * base, 3 * base, 4 * base})
-        for (int gw : {2, 4, 8}) add(wpg, 32 * gw, gw, lo);
+        for (int gw : {2, 4, 8})
+          for (int par : {0, 1}) add(std::min(wpg, W), 32 * gw, gw, lo, par);
     }
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     float best = 1e30f;
-    std::array<int, 4> best_c{wpg0, thr0, gw0, -1};
+    const bool par0 = b->parallel_levels;
+    std::array<int, 5> best_c{wpg0, thr0, gw0, -1, par0 ? 1 : 0};
     int rc = rc0;
     if (rc0 != SHAPES_OK) cands.clear();
     for (const auto& c : cands) {
@@ -2000,6 +2020,8 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->target_group_bodies = 0;
       b->solve_threads = c[1];
       b->group_warps = c[2];
+      b->parallel_levels = c[4] != 0;
+      b->invalidate_graphs();
       if (c[3]) b->world_order = by_levels; else b->world_order.clear();
       b->make_groups(cfg->iterations);
       rc = b->run(*cfg, 1, true); /* untimed: captures this packing's step graphs */
@@ -2024,14 +2046,17 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->target_group_bodies = 0;
       b->solve_threads = best_c[1];
       b->group_warps = best_c[2];
+      b->parallel_levels = best_c[4] != 0;
       if (best_c[3]) b->world_order = by_levels; else b->world_order.clear();
     } else {
       b->worlds_per_group_override = wpg0;
       b->target_group_bodies = tgt0;
       b->solve_threads = thr0;
       b->group_warps = gw0;
+      b->parallel_levels = par0;
       b->world_order = order0;
     }
+    b->invalidate_graphs();
     b->make_groups(cfg->iterations);
     ck(cudaStreamSynchronize(b->stream), "sync");
     for (void* p : saved) cudaFree(p);
@@ -2610,11 +2635,27 @@ int shapes_batch_get_world_levels(shapes_batch* b, int32_t* levels) {
   });
 }
 
+int shapes_batch_set_parallel_levels(shapes_batch* b, int32_t enabled) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->parallel_levels = enabled != 0;
+    b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps) {
   if (!b) return SHAPES_E_INVALID_ARG;
   if (worlds_per_group) *worlds_per_group = b->worlds_per_group_override;
   if (threads) *threads = b->solve_threads;
   if (group_warps) *group_warps = b->group_warps;
+  return SHAPES_OK;
+}
+
+int shapes_batch_get_parallel_levels(shapes_batch* b, int32_t* enabled) {
+  if (!b || !enabled) return SHAPES_E_INVALID_ARG;
+  *enabled = b->parallel_levels ? 1 : 0;
   return SHAPES_OK;
 }
 

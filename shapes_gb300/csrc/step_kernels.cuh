@@ -124,6 +124,9 @@ struct Dev {
   int32_t* world_pair_off;    /* [W+1] */
   int32_t* world_contact_off; /* [W+1] */
   int32_t* last;              /* [N] scheduler scratch */
+  int32_t* last_hit;          /* [N] scheduler scratch: last cache-hit contact of each body */
+  int4* c_pred;               /* [contact_cap] per contact: previous contact touching side a, side b; previous hit contact of a, b (-1: none) */
+  int32_t* c_lvl;             /* [2 * contact_cap] levels of the current and the previous pass */
   uint32_t* items;            /* [item_cap] */
   int32_t* ilevel;            /* [item_cap] */
   uint32_t* isorted;          /* [item_cap] */
@@ -2007,13 +2010,16 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
  * changes nothing in the results; it lets the host pack more worlds into a
  * group (fuller FP64 instructions: one warp instruction serves 32 updates)
  * without lengthening each warp's share of a level. */
-template <int P>
+template <int P, bool PAR>
 __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, int warm_start, int external,
                                                         double ax, double ay, double dt, int n_groups,
                                                         int smem_ints) {
   constexpr int NT = 32 * P;
   extern __shared__ __align__(16) int32_t s_dyn[];
   __shared__ int32_t s_delta[kMaxGroupWorlds];
+  __shared__ int32_t s_coff[kMaxGroupWorlds + 1]; /* PAR: prefix of the worlds' contact counts */
+  __shared__ int32_t s_c0[kMaxGroupWorlds];       /* PAR: first contact of each world */
+  __shared__ int32_t s_wdepth[kMaxGroupWorlds];   /* PAR: levels of each world */
   __shared__ int32_t s_nitems[kMaxGroupWorlds];
   __shared__ unsigned long long s_region[kMaxGroupWorlds];
   __shared__ int32_t s_red[3][P];
@@ -2033,7 +2039,8 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
     const int wld = d.group_worlds[o0 + k];
     group_bodies += d.world_body_off[wld + 1] - d.world_body_off[wld];
   }
-  const bool smem_last = group_bodies <= smem_ints;
+  /* PAR keeps two per-body entries (last contact, last cache-hit contact) */
+  const bool smem_last = (PAR ? 2 : 1) * group_bodies <= smem_ints;
   {
     int base = 0;
     for (int k = 0; k < nw; ++k) {
@@ -2044,17 +2051,42 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
           d.vx[g] = d.vx[g] + ax * dt;
           d.vy[g] = d.vy[g] + ay * dt;
         }
-        if (smem_last) s_last[base + g - b0] = 0;
-        else d.last[g] = 0;
+        if (PAR) {
+          if (smem_last) {
+            s_last[base + g - b0] = -1;
+            s_last[group_bodies + base + g - b0] = -1;
+          } else {
+            d.last[g] = -1;
+            d.last_hit[g] = -1;
+          }
+        } else {
+          if (smem_last) s_last[base + g - b0] = 0;
+          else d.last[g] = 0;
+        }
       }
       if (tid == 0) s_delta[k] = base - b0;
       base += b1 - b0;
     }
   }
   __syncthreads();
+  if constexpr (PAR) {
+    if (tid == 0) {
+      int acc = 0;
+      for (int k = 0; k < nw; ++k) {
+        const int wld = d.group_worlds[o0 + k];
+        s_coff[k] = acc;
+        s_c0[k] = d.world_contact_off[wld];
+        s_wdepth[k] = 0;
+        acc += d.world_contact_off[wld + 1] - d.world_contact_off[wld];
+      }
+      s_coff[nw] = acc;
+    }
+    __syncthreads();
+  }
+  int my_depth = 0, my_items = 0, my_hits = 0;
+  if constexpr (!PAR) {
   /* 2b. world k is scanned by lane k / P of warp k % P */
   const int my_k = lane * P + wib;
-  int my_depth = 0, my_items = 0, my_hits = 0;
   size_t my_region = 0;
   int c0 = 0, c1 = 0;
   int32_t* last = d.last;
@@ -2116,6 +2148,152 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
     s_region[my_k] = (unsigned long long)my_region;
     d.world_levels[d.group_worlds[o0 + my_k]] = my_depth;
   }
+  } else {
+    /* 2b. Dependency levels without a walk over every update.  Phase A: the
+     * lane of world k walks the world's contacts once and records, for each
+     * dynamic side, the previous contact of the world on that body and the
+     * previous cache-hit contact (c_pred); the per-body arrays end holding
+     * each body's last contact and last hit contact. */
+    int32_t* lastc = smem_last ? s_last : d.last;
+    int32_t* lasth = smem_last ? s_last + group_bodies : d.last_hit;
+    const int my_k = lane * P + wib;
+    if (my_k < nw) {
+      const int dl = smem_last ? s_delta[my_k] : 0;
+      const int c0 = s_c0[my_k], c1 = c0 + (s_coff[my_k + 1] - s_coff[my_k]);
+      if (c0 < c1) {
+        uint8_t inf[kScanBlock];
+        int ia[kScanBlock], ib[kScanBlock];
+#pragma unroll
+        for (int k = 0; k < kScanBlock; ++k) {
+          const int cc = min(c0 + k, c1 - 1);
+          inf[k] = d.c_hit[cc];
+          ia[k] = d.c_ga[cc];
+          ib[k] = d.c_gb[cc];
+        }
+        for (int cb = c0; cb < c1; cb += kScanBlock) {
+          uint8_t inf2[kScanBlock];
+          int ia2[kScanBlock], ib2[kScanBlock];
+#pragma unroll
+          for (int k = 0; k < kScanBlock; ++k) {
+            const int cc = min(cb + kScanBlock + k, c1 - 1);
+            inf2[k] = d.c_hit[cc];
+            ia2[k] = d.c_ga[cc];
+            ib2[k] = d.c_gb[cc];
+          }
+#pragma unroll
+          for (int k = 0; k < kScanBlock; ++k) {
+            const int c = cb + k;
+            if (c < c1) {
+              const uint8_t info = inf[k];
+              const bool hit = info & kInfoHit;
+              int4 pr = make_int4(-1, -1, -1, -1);
+              if (info & kInfoDynA) {
+                const int sa = ia[k] + dl;
+                pr.x = lastc[sa];
+                pr.z = lasth[sa];
+                lastc[sa] = c;
+                if (hit) lasth[sa] = c;
+              }
+              if (info & kInfoDynB) {
+                const int sb = ib[k] + dl;
+                pr.y = lastc[sb];
+                pr.w = lasth[sb];
+                lastc[sb] = c;
+                if (hit) lasth[sb] = c;
+              }
+              d.c_pred[c] = pr;
+            }
+            inf[k] = inf2[k];
+            ia[k] = ia2[k];
+            ib[k] = ib2[k];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    /* Phase B: the passes in order over the group's contacts in chunks of the
+     * CTA's threads.  An update's level is one more than its predecessors'
+     * on each dynamic body: the previous contact of the same pass touching
+     * it, else the body's last contact of the previous pass (only cache hits
+     * are updates of the warm-start pass).  Within a chunk the levels are
+     * raised to a fixed point (they only grow and stay at or below the final
+     * values), which gives every update the level a walk over the updates in
+     * order gives it.  Update (pass p, contact c) of world k takes slot
+     * (p - p0) n_k + (c - c0_k) of the world's region; a slot without an
+     * update (the warm-start pass of a contact without a cache hit) keeps
+     * level 0. */
+    const int NC = s_coff[nw];
+    const int p0 = warm_start ? 0 : 1;
+    for (int p = p0; p <= iterations; ++p) {
+      int32_t* Lc = d.c_lvl + (size_t)(p & 1) * d.contact_cap;
+      const int32_t* Lp = d.c_lvl + (size_t)((p + 1) & 1) * d.contact_cap;
+      for (int s0 = 0; s0 < NC; s0 += NT) {
+        const int gc = s0 + tid;
+        int k = 0, c = -1, ga = 0, gb = 0;
+        uint8_t info = 0;
+        int4 pr = make_int4(-1, -1, -1, -1);
+        if (gc < NC) {
+          while (k + 1 < nw && s_coff[k + 1] <= gc) ++k;
+          c = s_c0[k] + (gc - s_coff[k]);
+          info = d.c_hit[c];
+          ga = d.c_ga[c];
+          gb = d.c_gb[c];
+          pr = d.c_pred[c];
+        }
+        const bool live = c >= 0 && !(p == 0 && !(info & kInfoHit));
+        const int dl = smem_last ? s_delta[k] : 0;
+        int a_same = -1, b_same = -1, base = 0;
+        if (live && (info & kInfoDynA)) {
+          a_same = p == 0 ? pr.z : pr.x;
+          if (a_same < 0 && p > p0) {
+            const int q = p - 1 == 0 ? lasth[ga + dl] : lastc[ga + dl];
+            if (q >= 0) base = max(base, Lp[q]);
+          }
+        }
+        if (live && (info & kInfoDynB)) {
+          b_same = p == 0 ? pr.w : pr.y;
+          if (b_same < 0 && p > p0) {
+            const int q = p - 1 == 0 ? lasth[gb + dl] : lastc[gb + dl];
+            if (q >= 0) base = max(base, Lp[q]);
+          }
+        }
+        if (live) Lc[c] = 0;
+        __syncthreads();
+        int L = 0;
+        for (;;) {
+          int v = base;
+          if (a_same >= 0) v = max(v, Lc[a_same]);
+          if (b_same >= 0) v = max(v, Lc[b_same]);
+          const int nl = live ? v + 1 : 0;
+          const bool changed = nl != L;
+          L = nl;
+          __syncthreads(); /* every read of this round before any write */
+          if (changed) Lc[c] = L;
+          if (!__syncthreads_or(changed)) break;
+        }
+        if (c >= 0) {
+          const size_t slot = (size_t)stride * s_c0[k] + (size_t)(p - p0) * (s_coff[k + 1] - s_coff[k]) +
+                              (size_t)(gc - s_coff[k]);
+          if (live) {
+            d.idesc[slot] = make_int4((int)((uint32_t)c | (p == 0 ? kWarmBit : 0u)), ga, gb, (int)info | (k << 8));
+            ++my_items;
+            my_depth = L > my_depth ? L : my_depth;
+            my_hits += p == 0;
+            atomicMax(&s_wdepth[k], L);
+          }
+          d.ilevel[slot] = L; /* 0: no update in this slot */
+        }
+      }
+      __syncthreads();
+    }
+    if (tid < nw) {
+      const int n_k = s_coff[tid + 1] - s_coff[tid];
+      s_nitems[tid] = (iterations + 1 - p0) * n_k;
+      s_region[tid] = (unsigned long long)stride * (unsigned long long)s_c0[tid];
+      d.world_levels[d.group_worlds[o0 + tid]] = s_wdepth[tid];
+    }
+    __syncthreads();
+  }
   if (d.phase_clock && tid == 0) d.phase_clock[8 * grp + 1] = clock64();
   /* 3. counting sort by level into a region of gdesc / ghist */
   int max_depth = my_depth, tot_items = my_items, tot_hits = my_hits;
@@ -2156,7 +2334,10 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
     const int n_items = s_nitems[k];
     const size_t region = (size_t)s_region[k];
 #pragma unroll 4
-    for (int t = tid; t < n_items; t += NT) atomicAdd(&hist[d.ilevel[region + t] - 1], 1);
+    for (int t = tid; t < n_items; t += NT) {
+      const int lvl = d.ilevel[region + t];
+      if (!PAR || lvl > 0) atomicAdd(&hist[lvl - 1], 1);
+    }
   }
   __syncthreads();
   if (wib == 0) { /* exclusive scan of the level counts by warp 0 */
@@ -2179,8 +2360,10 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
     const size_t region = (size_t)s_region[k];
 #pragma unroll 4
     for (int t = tid; t < n_items; t += NT) {
+      const int lvl = d.ilevel[region + t];
+      if (PAR && lvl <= 0) continue;
       const int4 u = d.idesc[region + t];
-      gdesc[atomicAdd(&hist[d.ilevel[region + t] - 1], 1)] = u;
+      gdesc[atomicAdd(&hist[lvl - 1], 1)] = u;
     }
   }
   __syncthreads();

@@ -130,18 +130,21 @@ def test_mixed_polygon_worlds():
     b.close()
 
 
-@pytest.mark.parametrize("wpg,warps", [(1, 2), (3, 4), (8, 8), (32, 4)])
-def test_cooperative_groups_do_not_change_results(wpg, warps):
-    """Several warps sharing a solver group (levels split across them)."""
+@pytest.mark.parametrize("wpg,warps,par", [(1, 2, True), (3, 4, True), (8, 8, True), (32, 4, True), (3, 4, False),
+                                           (32, 8, False)])
+def test_cooperative_groups_do_not_change_results(wpg, warps, par):
+    """Several warps sharing a solver group (levels split across them), with
+    the dependency levels found in parallel or by a walk over the updates."""
     sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
     b = batch_from_scene(sc)
     b.set_launch_groups(wpg, 32 * warps, warps)
+    b.set_parallel_levels(par)
     ow = oracle_worlds(sc)
     cfg = config_of(sc)
     b.step(cfg, 40)
     step_oracles(ow, sc, 40)
-    compare_bodies(b, ow, sc, f"cooperative {wpg}/{warps}")
-    compare_collision(b, ow, f"cooperative {wpg}/{warps}")
+    compare_bodies(b, ow, sc, f"cooperative {wpg}/{warps}/{par}")
+    compare_collision(b, ow, f"cooperative {wpg}/{warps}/{par}")
     b.close()
 
 
