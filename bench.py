@@ -686,7 +686,7 @@ def run_ours(args, rank, world, local):
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                 "traffic": items / solve_launches * (GROUP_SOLVE_DRAM_BYTES_PER_ITEM if "group" in solver_kernel
                                                      else SOLVER_DRAM_BYTES_PER_ITEM),
-                "traffic_source": ("ncu dram bytes per update of k_group_solve<4> (mixed, 256 worlds)"
+                "traffic_source": ("ncu dram bytes per update of k_group_solve<4, parallel levels> (mixed, 256 worlds)"
                                    if "group" in solver_kernel else
                                    "ncu dram bytes per update of k_schedule_solve (batched, 512 worlds)")
                                   + " x updates per launch",
@@ -879,9 +879,9 @@ SOLVER_FP64_OPS_PER_ITEM = 72.5
 # dram__bytes_write.sum = 12.70 MB over 370,978 updates): the working set is
 # L2-resident, so traffic is far below the algorithmic bytes.
 SOLVER_DRAM_BYTES_PER_ITEM = 34.2
-# the same for k_group_solve<4> (one ncu capture, mixed scene, 256 worlds,
-# settled frame): 25.78 MB over 865,243 updates.
-GROUP_SOLVE_DRAM_BYTES_PER_ITEM = 29.8
+# the same for k_group_solve<4> with parallel levels (one ncu capture, mixed
+# scene, 256 worlds, settled frame): 26.15 MB over 865,243 updates.
+GROUP_SOLVE_DRAM_BYTES_PER_ITEM = 30.2
 
 
 def main():
