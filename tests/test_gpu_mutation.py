@@ -87,3 +87,37 @@ def test_checkpoint_keeps_empty_slots(tmp_path):
         assert_bits_equal(ga[f], gc[f], f)
     a.close()
     c.close()
+
+
+def test_random_mutation_sequence_matches_the_oracle():
+    """Random deletes and appends (boxes, polygons and circles; in place, into
+    other-sized slots and at the end) interleaved with steps, in worlds large
+    enough for the grid broadphase and its incremental pair lists."""
+    rng = np.random.default_rng(12)
+    sc = scenes.subset_worlds(scenes.batched_balls(n_worlds=4, n_bodies=80), [0, 1, 2])
+    cfg = config_of(sc)
+    b = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+
+    def steps(n):
+        b.step(cfg, n)
+        step_oracles(ow, sc, n)
+
+    steps(10)
+    shapes = [scenes.rectangle_vertices(0.6, 0.6), np.array([[0.35, 0.0]]),
+              scenes.perturbed_polygon(np.random.default_rng(3), 5, 0.4)]
+    for _ in range(12):
+        w = int(rng.integers(0, 3))
+        active = ow[w].active()
+        if rng.random() < 0.5 and active[3:].sum() > 10:
+            slot = int(rng.choice(np.flatnonzero(active[3:])) + 3)  # not the container walls
+            b.delete_body(w, slot)
+            assert ow[w].delete(slot) == 0
+        else:
+            xy = shapes[int(rng.integers(0, len(shapes)))]
+            body = [float(rng.uniform(-0.5, 0.5)), 0.0, 0.0, float(rng.uniform(-3, 3)), float(rng.uniform(8, 12)),
+                    0.0, 1.0, 2.0, 0.3, 0.1]
+            assert b.append_body(w, body, xy) == ow[w].append(body, xy)
+        steps(int(rng.integers(1, 6)))
+    _compare(b, ow, "random mutations")
+    b.close()
