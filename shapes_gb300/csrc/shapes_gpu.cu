@@ -98,6 +98,9 @@ struct shapes_batch {
   uint64_t* boxk = nullptr;
   uint8_t* flags = nullptr;
   uint8_t* body_changed = nullptr; /* [N] scratch of set_bodies: pose inputs changed */
+  int32_t* export_keys = nullptr;  /* staging of get_contacts for pageable caller arrays */
+  double* export_vals = nullptr;
+  int64_t export_cap = 0;
   /* broadphase / narrowphase */
   int32_t pair_cap = 0, contact_cap = 0;
   int64_t item_cap = 0;
@@ -1315,6 +1318,8 @@ struct shapes_batch {
     dfree(phase_clock);
     dfree(counters);
     dfree(np_cls);
+    dfree(export_keys);
+    dfree(export_vals);
     dfree(lw_bcnt); dfree(lw_bstart); dfree(lw_bh); dfree(lw_bn); dfree(lw_done); dfree(lw_color_cnt); dfree(lw_ctl);
     dfree(world_residual);
     dfree(world_depth);
@@ -1814,19 +1819,40 @@ int shapes_batch_get_contacts(shapes_batch* b, int32_t* keys5, double* vals5, in
   const int64_t C = b->have_results ? b->stats.contacts : 0;
   if (capacity < C) return SHAPES_E_BUFFER;
   return guarded([&]() -> int {
-    std::vector<uint64_t> key(C);
-    std::vector<uint8_t> flip(C);
     if (C > 0) {
-      ck(cudaMemcpyAsync(key.data(), b->c_key[b->results_buf], sizeof(uint64_t) * C, cudaMemcpyDeviceToHost, b->stream), "download");
-      ck(cudaMemcpyAsync(flip.data(), b->c_flip, C, cudaMemcpyDeviceToHost, b->stream), "download");
-      ck(cudaMemcpyAsync(vals5, b->c_val, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, b->stream), "download");
+      /* decoded on the device; straight into the caller's arrays when both
+       * are mapped pinned host memory, else through a device staging area */
+      cudaPointerAttributes ak{}, av{};
+      const bool mk = cudaPointerGetAttributes(&ak, keys5) == cudaSuccess && ak.type == cudaMemoryTypeHost &&
+                      ak.devicePointer;
+      const bool mv = cudaPointerGetAttributes(&av, vals5) == cudaSuccess && av.type == cudaMemoryTypeHost &&
+                      av.devicePointer;
+      cudaGetLastError();
+      const int grid = (int)std::min<int64_t>((C + 255) / 256, 4096);
+      if (mk && mv) {
+        shapes::k_export_contacts<<<grid, 256, 0, b->stream>>>(
+            b->c_key[b->results_buf], b->c_flip, b->c_val, (int)C, static_cast<int32_t*>(ak.devicePointer),
+            static_cast<double*>(av.devicePointer));
+        ck(cudaGetLastError(), "launch");
+      } else {
+        if (b->export_cap < C) {
+          dfree(b->export_keys);
+          dfree(b->export_vals);
+          b->export_keys = nullptr;
+          b->export_vals = nullptr;
+          b->export_keys = dalloc<int32_t>(5 * (size_t)C, "cudaMalloc export");
+          b->export_vals = dalloc<double>(5 * (size_t)C, "cudaMalloc export");
+          b->export_cap = C;
+        }
+        shapes::k_export_contacts<<<grid, 256, 0, b->stream>>>(b->c_key[b->results_buf], b->c_flip, b->c_val,
+                                                              (int)C, b->export_keys, b->export_vals);
+        ck(cudaGetLastError(), "launch");
+        ck(cudaMemcpyAsync(keys5, b->export_keys, sizeof(int32_t) * 5 * C, cudaMemcpyDeviceToHost, b->stream),
+           "download");
+        ck(cudaMemcpyAsync(vals5, b->export_vals, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, b->stream),
+           "download");
+      }
       ck(cudaStreamSynchronize(b->stream), "download");
-    }
-    for (int64_t c = 0; c < C; ++c) {
-      int32_t k4[4];
-      decode_key(key[c], k4);
-      for (int q = 0; q < 4; ++q) keys5[5 * c + q] = k4[q];
-      keys5[5 * c + 4] = flip[c];
     }
     if (world_counts) {
       if (b->have_results) world_counts_from(b, b->cwo[b->results_buf], world_counts);

@@ -210,6 +210,26 @@ __global__ void k_copy10(Ptr10 p, int n, unsigned long long* bad_flag) {
   if (bad_flag && __any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(bad_flag, 1ull);
 }
 
+/* Contacts in the caller's layout (keys i, j, fa, fb, flip and values nx, ny,
+ * px, py, depth, five each), written to device memory or to mapped pinned
+ * host memory.  The key fields follow pack_key. */
+__global__ void k_export_contacts(const uint64_t* key, const uint8_t* flip, const double* val, int n,
+                                  int32_t* keys5, double* vals5) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const uint64_t k = key[c];
+    int32_t* ko = keys5 + 5 * (size_t)c;
+    ko[0] = (int32_t)(k >> 44);
+    ko[1] = (int32_t)((k >> 24) & 0xfffff);
+    ko[2] = (int32_t)((k >> 12) & 0xfff);
+    ko[3] = (int32_t)(k & 0xfff);
+    ko[4] = flip[c];
+    const double* vi = val + 5 * (size_t)c;
+    double* vo = vals5 + 5 * (size_t)c;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) vo[q] = vi[q];
+  }
+}
+
 /* Staged body state -> live arrays, one thread per body; changed[g] = 1 when
  * a field the pose depends on (position, rotation, inverse masses, which set
  * the static flag) differs bit for bit from the live value. */

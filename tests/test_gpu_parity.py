@@ -454,6 +454,17 @@ def test_pinned_host_buffers_round_trip():
     ga, gb = a.get_bodies(), b.get_bodies()
     for f in STATE_FIELDS:
         assert_bits_equal(ga[f], gb[f], f"pinned round trip {f}")
+    keys, vals, counts = b.get_contacts()  # pageable arrays: decoded on the device, then copied
+    cap = len(keys) + 8
+    pk = torch.empty(5 * cap, dtype=torch.int32, pin_memory=True)
+    pv = torch.empty(5 * cap, dtype=torch.float64, pin_memory=True)
+    wc = np.empty(b.n_worlds, dtype=np.int32)
+    _lib.check(L.shapes_batch_get_contacts(b.handle, ctypes.cast(pk.data_ptr(), _lib._ip),
+                                           ctypes.cast(pv.data_ptr(), _lib._dp), cap,
+                                           wc.ctypes.data_as(_lib._ip)), "get_contacts pinned")
+    assert np.array_equal(pk.numpy()[:5 * len(keys)].reshape(-1, 5), keys)
+    assert_bits_equal(pv.numpy()[:5 * len(keys)].reshape(-1, 5), vals, "pinned contacts")
+    assert np.array_equal(wc, counts)
     pin["vel_x"][5] = float("nan")
     assert L.shapes_batch_set_bodies(b.handle, ctypes.byref(desc)) == _lib.SHAPES_E_NAN
     gc = b.get_bodies()
