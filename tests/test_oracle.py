@@ -306,3 +306,16 @@ def test_balls_scene_settles(O):
     assert np.isfinite(b["pos_y"]).all()
     assert (b["pos_y"][1:] > -5.6).all() and (b["pos_y"][1:] < 0.0).all()
     assert len(w.contacts()[0]) >= 16
+
+
+def test_circle_benchmark_fixture(O):
+    """The reference's circle fixture (bench/Physics/Contact/Circle/Benchmark.hs:
+    `contact (Circle (-1, 0) 1.1) (Circle (1, 0) 1.1)`), penetrated circle first,
+    with every value restated in the reference's operation order."""
+    keys, vals = _collide_two(O, ("circle", 1.1, (1.0, 0.0)), ("circle", 1.1, (-1.0, 0.0)))
+    assert [list(k) for k in keys] == [[1, 0, 0, 0, 0]]
+    ax, bx, r = -1.0, 1.0, 1.1
+    ab_len = math.sqrt((bx - ax) * (bx - ax) + 0.0 * 0.0)
+    ux = (bx - ax) / ab_len
+    a1, b1 = r * ux + ax, (-r) * ux + bx
+    assert list(vals[0]) == [ux, 0.0, (a1 + b1) / 2.0, 0.0, r + r - ab_len]
