@@ -313,6 +313,7 @@ def new_batch(_lib, scene, stream, tuned=None):
         b.set_launch_groups(*tuned[:3])
         b.set_world_order(tuned[3])
         b.set_parallel_levels(tuned[4])
+        b.set_spread_heavy(tuned[5])
     return b
 
 
@@ -342,6 +343,7 @@ class Lanes:
             if tuned:
                 b.set_launch_groups(*tuned[:3])
                 b.set_parallel_levels(tuned[4])
+                b.set_spread_heavy(tuned[5])
             b.set_world_order(np.arange(len(sc["world_body_offsets"]) - 1, dtype=np.int32))
             self.handles.append(b)
         assert sum(len(w) for w in self.worlds) == W
@@ -488,11 +490,14 @@ def run_ours(args, rank, world, local):
         vals = [int(x) for x in args.packing.split(",")]
         wpg, thr, gw = vals[:3]
         par = bool(vals[3]) if len(vals) > 3 else True
-        tuned = (wpg, thr, gw, np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable").astype(np.int32), par)
+        spread = bool(vals[4]) if len(vals) > 4 else False
+        tuned = (wpg, thr, gw, np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable").astype(np.int32), par,
+                 spread)
     elif not args.no_tune:
         t = new_batch(_lib, scene, stream)
         t.step(cfg_for(plain_it, False), args.tune_after)
-        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(), t.parallel_levels())
+        tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(), t.parallel_levels(),
+                                                                         t.spread_heavy())
         t.close()
 
     n_worlds = len(scene["world_body_offsets"]) - 1
@@ -729,6 +734,7 @@ def run_ours(args, rank, world, local):
                        else "grid, full 3x3 search every frame",
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
                                           "warps_per_group": tuned[2], "parallel_levels": bool(tuned[4]),
+                                          "heavy_groups_spread": bool(tuned[5]),
                                           "world_order": "by size" if np.array_equal(
                                               tuned[3], np.argsort(-np.diff(scene["world_body_offsets"]),
                                                                    kind="stable")) else "by dependency levels"}
@@ -895,7 +901,7 @@ def main():
     ap.add_argument("--worlds", type=int, default=None, help="override the world count (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the solver-packing autotuner")
     ap.add_argument("--packing", default="", help="fixed solver packing 'worlds_per_group,threads,warps_per_group"
-                    "[,parallel_levels]' (size order) instead of the autotuner")
+                    "[,parallel_levels[,spread_heavy]]' (size order) instead of the autotuner")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
     ap.add_argument("--tune-steps", type=int, default=30, help="steps per autotuner trial")
     ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")

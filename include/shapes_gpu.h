@@ -245,6 +245,11 @@ int shapes_batch_set_group_warps(shapes_batch* b, int32_t warps);
  * Both give every update the same level. */
 int shapes_batch_set_parallel_levels(shapes_batch* b, int32_t enabled);
 int shapes_batch_get_parallel_levels(shapes_batch* b, int32_t* enabled);
+/* Cooperative groups: launch the heaviest groups first, one per SM, then the
+ * others lightest first (default 0: heaviest first throughout), so a heavy
+ * group shares its SM with light ones.  Results do not depend on it. */
+int shapes_batch_set_spread_heavy(shapes_batch* b, int32_t enabled);
+int shapes_batch_get_spread_heavy(shapes_batch* b, int32_t* enabled);
 /* The packing in use (any pointer may be NULL). */
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps);
 /* The order in which worlds are packed into groups: a permutation of

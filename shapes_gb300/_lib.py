@@ -127,6 +127,8 @@ SIGNATURES = [
     ("shapes_batch_set_group_warps", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_set_parallel_levels", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_get_parallel_levels", ctypes.c_int, [ctypes.c_void_p, _ip]),
+    ("shapes_batch_set_spread_heavy", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_get_spread_heavy", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_batches_step", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.POINTER(Config),
                                            ctypes.c_int32]),
     ("shapes_batches_step_io", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
@@ -368,6 +370,15 @@ class Batch:
     def set_parallel_levels(self, enabled: bool) -> None:
         """Cooperative groups: dependency levels in parallel (default) or by a walk over the updates."""
         check(lib().shapes_batch_set_parallel_levels(self._h, int(bool(enabled))), "shapes_batch_set_parallel_levels")
+
+    def set_spread_heavy(self, enabled: bool) -> None:
+        """Cooperative groups: heaviest groups first, one per SM, then lightest first."""
+        check(lib().shapes_batch_set_spread_heavy(self._h, int(bool(enabled))), "shapes_batch_set_spread_heavy")
+
+    def spread_heavy(self) -> bool:
+        v = ctypes.c_int32()
+        check(lib().shapes_batch_get_spread_heavy(self._h, ctypes.byref(v)), "shapes_batch_get_spread_heavy")
+        return bool(v.value)
 
     def set_group_warps(self, warps: int) -> None:
         """Warps cooperating on each solver group (1, 2, 4 or 8)."""

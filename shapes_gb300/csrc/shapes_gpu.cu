@@ -206,6 +206,17 @@ struct shapes_batch {
   int32_t solve_threads = 32;
   int32_t group_warps = 1; /* > 1: that many warps cooperate on each group (k_group_solve) */
   bool parallel_levels = true; /* cooperative groups: dependency levels by chunked fixed point */
+  bool spread_heavy = false;   /* cooperative groups: heaviest groups first, one per SM, then lightest first */
+  int num_sms() {
+    if (sm_count <= 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+      if (sm_count <= 0) sm_count = 1;
+    }
+    return sm_count;
+  }
+  int sm_count = 0;
   std::vector<int32_t> world_order; /* packing order of the worlds; empty = by body count */
   /* scans */
   int32_t* tile_sums = nullptr;
@@ -966,7 +977,8 @@ struct shapes_batch {
       stage(4, 1, [&]() {
 #define SHAPES_GROUP_SOLVE(PW, PL)                                                                              \
   shapes::k_group_solve<PW, PL><<<G, 32 * PW, bytes, stream>>>(d, cfg.iterations, cfg.warm_start, cfg.external, \
-                                                               cfg.accel_x, cfg.accel_y, cfg.dt, G, ints)
+                                                               cfg.accel_x, cfg.accel_y, cfg.dt, G, ints,  \
+                                                               spread_heavy ? num_sms() : 0)
         if (parallel_levels) {
           if (group_warps == 2) SHAPES_GROUP_SOLVE(2, true);
           else if (group_warps == 4) SHAPES_GROUP_SOLVE(4, true);
@@ -2018,10 +2030,10 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       return (b->h_world_body_off[a + 1] - b->h_world_body_off[a]) > (b->h_world_body_off[c + 1] - b->h_world_body_off[c]);
     });
     /* (worlds per group, threads per CTA, warps per group, level order,
-     * parallel levels) */
-    std::vector<std::array<int, 5>> cands;
-    auto add = [&](int wpg, int thr, int gw, int lo, int par) {
-      const std::array<int, 5> c{wpg, thr, gw, lo, par};
+     * parallel levels, heavy groups spread) */
+    std::vector<std::array<int, 6>> cands;
+    auto add = [&](int wpg, int thr, int gw, int lo, int par, int spread = 0) {
+      const std::array<int, 6> c{wpg, thr, gw, lo, par, spread};
       if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds && std::find(cands.begin(), cands.end(), c) == cands.end())
         cands.push_back(c);
     };
@@ -2030,14 +2042,17 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
         for (int thr : {32, 64, 128}) add(std::min(wpg, W), thr, 1, lo, 0);
       for (int wpg : {1, 2, base, base + 1, 2 * base, 3 * base, 4 * base})
         for (int gw : {2, 4, 8})
-          for (int par : {0, 1}) add(std::min(wpg, W), 32 * gw, gw, lo, par);
+          for (int par : {0, 1}) {
+            add(std::min(wpg, W), 32 * gw, gw, lo, par);
+            if (par) add(std::min(wpg, W), 32 * gw, gw, lo, par, 1);
+          }
     }
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     float best = 1e30f;
-    const bool par0 = b->parallel_levels;
-    std::array<int, 5> best_c{wpg0, thr0, gw0, -1, par0 ? 1 : 0};
+    const bool par0 = b->parallel_levels, spread0 = b->spread_heavy;
+    std::array<int, 6> best_c{wpg0, thr0, gw0, -1, par0 ? 1 : 0, spread0 ? 1 : 0};
     int rc = rc0;
     if (rc0 != SHAPES_OK) cands.clear();
     for (const auto& c : cands) {
@@ -2047,6 +2062,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->solve_threads = c[1];
       b->group_warps = c[2];
       b->parallel_levels = c[4] != 0;
+      b->spread_heavy = c[5] != 0;
       b->invalidate_graphs();
       if (c[3]) b->world_order = by_levels; else b->world_order.clear();
       b->make_groups(cfg->iterations);
@@ -2073,6 +2089,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->solve_threads = best_c[1];
       b->group_warps = best_c[2];
       b->parallel_levels = best_c[4] != 0;
+      b->spread_heavy = best_c[5] != 0;
       if (best_c[3]) b->world_order = by_levels; else b->world_order.clear();
     } else {
       b->worlds_per_group_override = wpg0;
@@ -2080,6 +2097,7 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       b->solve_threads = thr0;
       b->group_warps = gw0;
       b->parallel_levels = par0;
+      b->spread_heavy = spread0;
       b->world_order = order0;
     }
     b->invalidate_graphs();
@@ -2676,6 +2694,22 @@ int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t*
   if (worlds_per_group) *worlds_per_group = b->worlds_per_group_override;
   if (threads) *threads = b->solve_threads;
   if (group_warps) *group_warps = b->group_warps;
+  return SHAPES_OK;
+}
+
+int shapes_batch_set_spread_heavy(shapes_batch* b, int32_t enabled) {
+  if (!b) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->spread_heavy = enabled != 0;
+    b->invalidate_graphs();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_get_spread_heavy(shapes_batch* b, int32_t* enabled) {
+  if (!b || !enabled) return SHAPES_E_INVALID_ARG;
+  *enabled = b->spread_heavy ? 1 : 0;
   return SHAPES_OK;
 }
 

@@ -2033,7 +2033,7 @@ __global__ void k_schedule_solve(Dev d, int iterations, int warm_start, int exte
 template <int P, bool PAR>
 __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, int warm_start, int external,
                                                         double ax, double ay, double dt, int n_groups,
-                                                        int smem_ints) {
+                                                        int smem_ints, int heavy_first) {
   constexpr int NT = 32 * P;
   extern __shared__ __align__(16) int32_t s_dyn[];
   __shared__ int32_t s_delta[kMaxGroupWorlds];
@@ -2046,7 +2046,12 @@ __global__ void __launch_bounds__(32 * P) k_group_solve(Dev d, int iterations, i
   __shared__ int32_t s_gbase;
   if (d.counters[kCntOverflow]) return; /* buffers incomplete: the host retries */
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-  const int grp = blockIdx.x;
+  /* Groups come sorted heaviest first.  With heavy_first = h > 0 the first h
+   * CTAs (one wave over the SMs) take the h heaviest groups and the rest take
+   * the others lightest first, so that a heavy group starts beside light ones
+   * instead of beside the next heaviest. */
+  const int hf = min(heavy_first, n_groups);
+  const int grp = (int)blockIdx.x < hf ? (int)blockIdx.x : n_groups - 1 - ((int)blockIdx.x - hf);
   if (grp >= n_groups) return;
   const int o0 = d.group_world_off[grp], o1 = d.group_world_off[grp + 1];
   const int nw = o1 - o0;

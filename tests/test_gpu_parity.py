@@ -130,15 +130,17 @@ def test_mixed_polygon_worlds():
     b.close()
 
 
-@pytest.mark.parametrize("wpg,warps,par", [(1, 2, True), (3, 4, True), (8, 8, True), (32, 4, True), (3, 4, False),
-                                           (32, 8, False)])
-def test_cooperative_groups_do_not_change_results(wpg, warps, par):
+@pytest.mark.parametrize("wpg,warps,par,spread", [(1, 2, True, False), (3, 4, True, True), (8, 8, True, False),
+                                                  (32, 4, True, False), (3, 4, False, False), (32, 8, False, True),
+                                                  (1, 4, True, True)])
+def test_cooperative_groups_do_not_change_results(wpg, warps, par, spread):
     """Several warps sharing a solver group (levels split across them), with
     the dependency levels found in parallel or by a walk over the updates."""
     sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
     b = batch_from_scene(sc)
     b.set_launch_groups(wpg, 32 * warps, warps)
     b.set_parallel_levels(par)
+    b.set_spread_heavy(spread)
     ow = oracle_worlds(sc)
     cfg = config_of(sc)
     b.step(cfg, 40)
