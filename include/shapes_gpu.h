@@ -19,7 +19,8 @@
  *   - Body indices in keys and pairs are world-local slot indices, exactly the
  *     reference's World slot keys after `fromList` (World.hs:118-124).
  *   - Limits: at most 2^20 bodies per world, 3..64 vertices per convex hull
- *     (counter-clockwise, strictly convex), circles unsupported.
+ *     (counter-clockwise, strictly convex); a circle is one local point
+ *     (radius, 0).
  */
 #ifndef SHAPES_GPU_H
 #define SHAPES_GPU_H
@@ -32,7 +33,7 @@ extern "C" {
 
 #define SHAPES_OK 0
 #define SHAPES_E_INVALID_ARG (-1)
-#define SHAPES_E_UNSUPPORTED (-2) /* circles, more than 64 vertices, custom External */
+#define SHAPES_E_UNSUPPORTED (-2) /* more than 64 vertices, custom External */
 #define SHAPES_E_NONCONVEX (-3)   /* hull not strictly convex and counter-clockwise */
 #define SHAPES_E_CAPACITY (-4)    /* internal buffer could not grow */
 #define SHAPES_E_CUDA (-5)        /* CUDA runtime error (no device, launch failure) */
