@@ -705,6 +705,13 @@ def run_ours(args, rank, world, local):
                     "achieved_lane_ops_per_s": items * SOLVER_FP64_OPS_PER_ITEM / (solve_ms * 1e-3)}
             fp64["frac"] = fp64["achieved_lane_ops_per_s"] / fp64_peak
             roof["fp64"] = fp64
+            per_body = STEP_FP64_INST_PER_BODY_STEP.get(args.workload)
+            if per_body:  # the whole step against the FP64 pipe, at the timed throughput
+                roof["step_fp64"] = {
+                    "thread_instructions_per_body_step": per_body,
+                    "source": "ncu DADD+DMUL+DFMA thread-instruction counters of the timed steps, mixed scene",
+                    "achieved_per_s": per_body * value / world, "peak_per_s": fp64_peak,
+                    "frac": per_body * value / world / fp64_peak}
 
     # ---- CPU baseline (rank 0, N=1 only), bounded sample ---------------------
     cpu = None
@@ -885,6 +892,10 @@ SOLVER_FP64_OPS_PER_ITEM = 72.5
 # dram__bytes_write.sum = 12.70 MB over 370,978 updates): the working set is
 # L2-resident, so traffic is far below the algorithmic bytes.
 SOLVER_DRAM_BYTES_PER_ITEM = 34.2
+# FP64 thread-instructions (DADD + DMUL + DFMA, active lanes) per body-step of
+# the whole step on the mixed scene (ncu counters over the timed steps of one
+# handle over 1024 worlds x 256 bodies: 4.307e8 per step / 262,144 bodies).
+STEP_FP64_INST_PER_BODY_STEP = {"learned": 1643.0, "mixed": 1643.0}
 # the same for k_group_solve<4> with parallel levels (one ncu capture, mixed
 # scene, 256 worlds, settled frame): 26.15 MB over 865,243 updates.
 GROUP_SOLVE_DRAM_BYTES_PER_ITEM = 30.2
