@@ -94,6 +94,8 @@ struct shapes_batch {
   double* wy = nullptr;
   double* nx = nullptr;
   double* ny = nullptr;
+  double* plo = nullptr; /* [V] self extents of each edge (SAT) */
+  double* phi = nullptr;
   double* box = nullptr;
   uint64_t* boxk = nullptr;
   uint8_t* flags = nullptr;
@@ -392,6 +394,8 @@ struct shapes_batch {
     d.wy = wy;
     d.nx = nx;
     d.ny = ny;
+    d.plo = plo;
+    d.phi = phi;
     d.box = box;
     d.boxk = boxk;
     d.flags = flags;
@@ -1198,6 +1202,7 @@ struct shapes_batch {
       dfree(body_stage[k]);
     }
     dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags); dfree(body_changed);
+    dfree(plo); dfree(phi);
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off); dfree(last); dfree(last_hit); dfree(world_levels);
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(active);
@@ -1224,6 +1229,8 @@ struct shapes_batch {
     wy = dalloc<double>(V, "cudaMalloc");
     nx = dalloc<double>(V, "cudaMalloc");
     ny = dalloc<double>(V, "cudaMalloc");
+    plo = dalloc<double>(V, "cudaMalloc");
+    phi = dalloc<double>(V, "cudaMalloc");
     box = dalloc<double>(4 * (size_t)N, "cudaMalloc");
     boxk = dalloc<uint64_t>(4 * (size_t)N, "cudaMalloc");
     flags = dalloc<uint8_t>(N, "cudaMalloc");
@@ -1319,6 +1326,7 @@ struct shapes_batch {
       dfree(body_stage[k]);
     }
     dfree(wx); dfree(wy); dfree(nx); dfree(ny); dfree(box); dfree(boxk); dfree(flags); dfree(body_changed);
+    dfree(plo); dfree(phi);
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);

@@ -72,6 +72,8 @@ struct Dev {
   double* wy;
   double* nx;
   double* ny;
+  double* plo;      /* [V] per edge e: projection of vertex emin[e] on normal e (null: SAT computes it) */
+  double* phi;      /* [V] per edge e: projection of vertex emax[e] on normal e */
   double* box;      /* [4N] x0 x1 y0 y1 */
   uint64_t* boxk;   /* [4N] ordered keys of box */
   uint8_t* flags;   /* [N] */
@@ -410,6 +412,14 @@ __global__ void k_integrate_pose(Dev d, double dt, int advance, const uint8_t* o
       const double len = sqrt(ex * ex + ey * ey);
       d.nx[b0 + nv - 1] = ex / len;
       d.ny[b0 + nv - 1] = ey / len;
+    }
+    if (d.plo) { /* extentAlongSelf (ConvexHull.hs:107-118): the SAT's self extents, once per frame */
+      for (int e = 0; e < nv; ++e) {
+        const double dx = d.nx[b0 + e], dy = d.ny[b0 + e];
+        const int mi = b0 + d.emin[b0 + e], ma = b0 + d.emax[b0 + e];
+        d.plo[b0 + e] = d.wx[mi] * dx + d.wy[mi] * dy;
+        d.phi[b0 + e] = d.wx[ma] * dx + d.wy[ma] * dy;
+      }
     }
     d.box[4 * g + 0] = bx0;
     d.box[4 * g + 1] = bx1;
@@ -1051,6 +1061,8 @@ struct HullView {
   const double* ny;
   const int32_t* emin;
   const int32_t* emax;
+  const double* plo; /* null: computed per axis */
+  const double* phi;
   int nv;
 };
 
@@ -1063,6 +1075,8 @@ __device__ __forceinline__ HullView hull_view(const Dev& d, int g) {
   h.ny = d.ny + b0;
   h.emin = d.emin + b0;
   h.emax = d.emax + b0;
+  h.plo = d.plo ? d.plo + b0 : nullptr;
+  h.phi = d.phi ? d.phi + b0 : nullptr;
   h.nv = d.vert_off[g + 1] - b0;
   return h;
 }
@@ -1076,9 +1090,15 @@ __device__ __forceinline__ HullView hull_view(const Dev& d, int g) {
 __device__ __forceinline__ bool sat_axis(const HullView& se, int e, const HullView& sp,
                                          double* depth, int* pen) {
   const double dx = se.nx[e], dy = se.ny[e];
-  const int mi = se.emin[e], ma = se.emax[e];
-  const double sa = se.wx[mi] * dx + se.wy[mi] * dy;
-  const double sb = se.wx[ma] * dx + se.wy[ma] * dy;
+  double sa, sb;
+  if (se.plo) { /* the hull's extent along its own normal, computed once per frame by the pose */
+    sa = se.plo[e];
+    sb = se.phi[e];
+  } else {
+    const int mi = se.emin[e], ma = se.emax[e];
+    sa = se.wx[mi] * dx + se.wy[mi] * dy;
+    sb = se.wx[ma] * dx + se.wy[ma] * dy;
+  }
   /* one product of each projection on the integer pipe (mul_rn_int, exact),
    * the other on the FP64 pipe: the kernel is bound by FP64 throughput at
    * high occupancy, so the two pipes share the work */
