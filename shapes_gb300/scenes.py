@@ -476,6 +476,43 @@ def batched_balls(seed: int = 5, n_worlds: int = 256, n_bodies: int = 128, steps
     return scene
 
 
+def ragged_worlds(seed: int = 11) -> dict:
+    """Worlds of very different sizes, empty worlds first, in the middle and
+    last; a lone falling box; a lone static circle; a world of overlapping
+    static bodies only (no pairs: Broadphase/Grid.hs:82-83); a slab moving sideways
+    (static, non-zero velocity) under boxes; a body with infinite linear but
+    finite rotational mass (not static: Constraint.hs:122-125); circles on a
+    slab; a 5-body column; a 101-body box grid (grid broadphase)."""
+    rng = np.random.default_rng(seed)
+    b = SceneBuilder()
+    sq = rectangle_vertices(1.0, 1.0)
+    b.end_world()  # 0: empty
+    b.add(sq, (0.0, 3.0), 0.1, vel=(0.3, 0.0), rot_vel=0.2)
+    b.end_world()  # 1: one dynamic box, nothing to hit
+    b.end_world()  # 2: empty
+    b.add_circle(0.5, (0.0, 5.0), static=True)
+    b.end_world()  # 3: one static circle
+    b.add(rectangle_vertices(4.0, 1.0), (0.0, 0.0), static=True)
+    b.add(sq, (0.5, 0.2), 0.3, static=True)
+    b.add_circle(0.7, (-1.0, 0.4), static=True)
+    b.end_world()  # 4: static bodies overlapping one another
+    b.add(rectangle_vertices(30.0, 1.0), (0.0, -0.5), vel=(0.5, 0.0), static=True)
+    for k in range(4):
+        b.add(sq, (-3.0 + 2.0 * k, 0.5 + 0.02 * k), rng.uniform(-0.05, 0.05), mass=1.0, inertia=1.0 / 6.0)
+    b.add(rectangle_vertices(3.0, 0.4), (0.0, 1.18), rot_vel=0.3, mass=1.0, inertia=0.8)
+    b.rows["inv_mass_lin"][-1] = 0.0  # linear mass infinite, rotation free
+    b.end_world()  # 5: moving static slab, a rotation-only body resting on boxes
+    b.add(rectangle_vertices(10.0, 1.0), (0.0, -0.5), static=True)
+    for k in range(3):
+        b.add_circle(0.5, (-1.0 + 1.0 * k, 0.5 + 1.1 * k), mass=1.0, mu=0.2, bounce=0.3)
+    b.end_world()  # 6: circles on a slab
+    column_world(b, rng, 5)  # 7
+    box_grid_world(b, rng, cols=10, rows=10)  # 8: grid broadphase (>= 64 bodies)
+    b.end_world()  # 9: empty, last
+    return b.build(dt=1.0 / 60.0, baumgarte=DEFAULT_BAUMGARTE, slop=DEFAULT_SLOP,
+                   accel=(0.0, -9.8), iterations=4, steps=60)
+
+
 def subset_worlds(scene: dict, worlds) -> dict:
     """A scene holding only the given worlds of `scene` (in the given order)."""
     off = scene["world_body_offsets"]

@@ -256,3 +256,36 @@ def test_trained_network_lowers_the_residual_of_new_contacts(gpu):
     assert predicted > 0
     assert learned < 0.85 * plain, (learned, plain)
     net.close()
+
+
+def test_learned_start_on_ragged_and_empty_worlds(gpu):
+    """Empty, one-body and static-only worlds next to busy ones: predictions,
+    samples and the judge run, empty worlds keep a zero residual and stay
+    learned, and two runs give the same bits."""
+    from shapes_gb300 import scenes
+
+    sc = scenes.ragged_worlds()
+    runs = []
+    for _ in range(2):
+        b = gpu.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], sc["local_xy"],
+                      sc["shape_kind"])
+        net = gpu.Mlp(3)
+        b.set_mlp(net)
+        b.step(_cfg(gpu, sc, learned=True), 20)
+        assert b.stats()["predicted"] >= 0
+        b.collect(10000)
+        b.step(_cfg(gpu, sc, learned=True), 1)
+        feat, tgt = b.samples()
+        assert np.all(np.isfinite(feat)) and np.all(np.isfinite(tgt))
+        b.collect(0)
+        b.set_judge(max_residual=np.zeros(b.n_worlds))
+        b.step(_cfg(gpu, sc, learned=True), 1)
+        res, depth = b.world_metrics()
+        assert np.all(np.isfinite(res)) and np.all(np.isfinite(depth))
+        assert res[[0, 2, 9]].tolist() == [0.0] * 3
+        assert np.array_equal(b.learned_mask() == 0, res > 0)
+        runs.append(b.get_bodies())
+        b.close()
+        net.close()
+    for f in gpu.BODY_FIELDS:
+        assert np.array_equal(runs[0][f].view(np.uint64), runs[1][f].view(np.uint64)), f

@@ -130,6 +130,38 @@ def test_mixed_polygon_worlds():
     b.close()
 
 
+@pytest.mark.parametrize("incremental", [False, True])
+def test_ragged_and_empty_worlds(incremental):
+    sc = scenes.ragged_worlds()
+    off = sc["world_body_offsets"]
+    assert list(np.diff(off)) == [0, 1, 0, 1, 3, 6, 4, 5, 101, 0]
+    b = batch_from_scene(sc)
+    b.set_incremental(incremental)
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    for n in (1, 29, 30):
+        b.step(cfg, n)
+        step_oracles(ow, sc, n)
+        compare_bodies(b, ow, sc, f"ragged +{n}")
+        compare_collision(b, ow, "ragged")
+    _, pc = b.get_pairs()
+    _, _, cc = b.get_contacts()
+    assert pc[[0, 1, 2, 3, 4, 9]].tolist() == [0] * 6 and cc[[0, 1, 2, 3, 4, 9]].tolist() == [0] * 6
+    assert pc[5] > 0 and pc[6] > 0 and pc[8] > 0
+    got = b.get_bodies()
+    assert got["pos_x"][off[5]] != sc["bodies"]["pos_x"][off[5]]  # the static slab moved
+    cfg.flags = _lib.SHAPES_FLAG_RESIDUAL
+    b.step(cfg, 1)
+    step_oracles(ow, sc, 1)
+    res, depth = b.world_metrics()
+    for w, o in enumerate(ow):
+        want = o.residual()
+        assert abs(res[w] - want) <= 1e-12 * max(1.0, abs(want)), (w, res[w], want)
+    assert res[[0, 2, 9]].tolist() == [0.0] * 3 and depth[[0, 2, 9]].tolist() == [0.0] * 3
+    compare_bodies(b, ow, sc, "ragged after metrics")
+    b.close()
+
+
 @pytest.mark.parametrize("wpg,warps,par,spread", [(1, 2, True, False), (3, 4, True, True), (8, 8, True, False),
                                                   (32, 4, True, False), (3, 4, False, False), (32, 8, False, True),
                                                   (1, 4, True, True)])

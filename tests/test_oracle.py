@@ -319,3 +319,25 @@ def test_circle_benchmark_fixture(O):
     ux = (bx - ax) / ab_len
     a1, b1 = r * ux + ax, (-r) * ux + bx
     assert list(vals[0]) == [ux, 0.0, (a1 + b1) / 2.0, 0.0, r + r - ab_len]
+
+
+def test_ragged_and_empty_worlds_in_the_oracle(O):
+    """Empty worlds step without pairs; static-only overlaps make no pair;
+    a static body with a velocity moves; a body with infinite linear mass does
+    not fall (constantAccel skips it) but turns on the boxes it rests on."""
+    sc = scenes.ragged_worlds()
+    off = sc["world_body_offsets"]
+    ow = [O.world_from_scene(sc, w) for w in range(len(off) - 1)]
+    c = sc["config"]
+    O.batch_step(ow, c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"], True, True, 60, 2)
+    for o in ow:
+        o.collide()
+    npairs = [len(o.pairs()) for o in ow]
+    assert [npairs[w] for w in (0, 1, 2, 3, 4, 9)] == [0] * 6
+    assert npairs[5] >= 5 and npairs[6] > 0 and npairs[8] > 100
+    slab = ow[5].bodies()
+    x = sc["bodies"]["pos_x"][off[5]]
+    for _ in range(60):
+        x = (0.5 * c["dt"]) + x  # advanceObj (Constraint.hs:225-229) on the static slab
+    assert slab["pos_x"][0] == x
+    assert slab["pos_y"][5] == sc["bodies"]["pos_y"][off[5] + 5] and slab["rot"][5] != 0.0
