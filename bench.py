@@ -620,17 +620,12 @@ def run_ours(args, rank, world, local):
         ln.step(cfg, args.warmup)
     else:
         b.step(cfg, args.warmup)
-    bufs = []  # per handle: (input Bodies, output Bodies, keep-alive tensors)
+    states, keep = [], []  # per handle: the body state in pinned host memory (Bodies struct, tensors)
     for h in handles:
-        hin = {f: torch.empty(h.n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
-        hout = {f: torch.empty(h.n_bodies, dtype=torch.float64, pin_memory=True) for f in _lib.BODY_FIELDS}
         st0 = h.get_bodies()
-        for f in _lib.BODY_FIELDS:
-            hin[f].copy_(torch.from_numpy(st0[f]))
-        bufs.append([_lib.Bodies(*[ctypes.cast(hin[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]),
-                     _lib.Bodies(*[ctypes.cast(hout[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]),
-                     (hin, hout)])
-    L = _lib.lib()
+        pin = {f: torch.from_numpy(st0[f]).pin_memory() for f in _lib.BODY_FIELDS}
+        states.append(_lib.Bodies(*[ctypes.cast(pin[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]))
+        keep.append(pin)
     e_steps = args.steps
     barrier(world)
     torch.cuda.synchronize()
@@ -639,28 +634,15 @@ def run_ours(args, rank, world, local):
     if ln:
         for st_ in ln.streams:
             st_.wait_event(e0)
-
-    def e2e_loop(h, bf):
-        # body state in from pinned host memory, one step, state back out, each step
-        # (shapes_batches_step_io on this handle: one wait per step)
-        for _ in range(e_steps):
-            _lib.check(_lib.step_many_io([h], cfg, [bf[0]], [bf[1]]), "shapes_batches_step_io")
-            bf[0], bf[1] = bf[1], bf[0]  # next step's input is this step's result
-
-    if len(handles) > 1:  # one host thread per handle: each handle's copies overlap the others' steps
-        import threading
-
-        ths = [threading.Thread(target=e2e_loop, args=(h, bf)) for h, bf in zip(handles, bufs)]
-        for t_ in ths:
-            t_.start()
-        for t_ in ths:
-            t_.join()
+    # every step of every handle: state in from pinned host memory, one step, state
+    # back out and waited for (shapes_batches_run_io: one host thread per handle, so
+    # each handle's copies and host turn overlap the other handles' steps)
+    _lib.check(_lib.run_io(handles, cfg, e_steps, states), "shapes_batches_run_io")
+    if ln:
         for st_ in ln.streams:
             ev = torch.cuda.Event()
             ev.record(st_)
             stream.wait_event(ev)
-    else:
-        e2e_loop(handles[0], bufs[0])
     e1.record(stream)
     torch.cuda.synchronize()
     barrier(world)

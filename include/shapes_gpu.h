@@ -163,6 +163,27 @@ int shapes_batches_step(shapes_batch* const* bs, int32_t n, const shapes_config*
 int shapes_batches_step_io(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, const shapes_bodies* in,
                            shapes_bodies* out);
 
+/* Called on the host after step `step` of handle `handle_index` has written
+ * its result into state[handle_index]; the caller may read and change that
+ * state before the next upload.  Non-zero stops that handle's loop.  Calls
+ * for different handles may come from different threads at once. */
+typedef int (*shapes_step_callback)(void* user, int32_t handle_index, int32_t step);
+
+/* nsteps steps of n handles whose body state lives in caller host memory:
+ * every step of handle k uploads and checks state[k] (as
+ * shapes_batch_set_bodies), steps, writes the result back into state[k] and
+ * waits for it, then calls on_step (may be NULL).  Each handle runs its steps
+ * in order on a host thread of its own, so one handle's copies and host turn
+ * overlap the others' steps.  Pinned buffers are resolved once per call and
+ * copied by a kernel over the host link.  Returns the first error; a handle
+ * whose input holds a non-finite value stops with SHAPES_E_NAN, its device
+ * state as before that step (state[k] is then unspecified); the others run
+ * to the end.  No counterpart in the
+ * reference (its state is a Haskell value that each updateWorld returns,
+ * Engine/Main.hs:71-84). */
+int shapes_batches_run_io(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, int32_t nsteps,
+                          shapes_bodies* state, shapes_step_callback on_step, void* user);
+
 /* Broadphase + contact generation on the current poses only (no forces, no
  * solve); results readable with the pair/contact getters.
  * Replaces: G.culledKeys . G.toGrid (Engine/Main.hs:75) followed by

@@ -58,6 +58,10 @@ class Bodies(ctypes.Structure):
         "inv_mass_lin", "inv_mass_rot", "mu", "bounce")]
 
 
+# shapes_step_callback: (user, handle index, step) -> non-zero stops that handle
+STEP_CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32)
+
+
 BODY_FIELDS = [f[0] for f in Bodies._fields_]
 
 
@@ -134,6 +138,9 @@ SIGNATURES = [
     ("shapes_batches_step_io", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                                               ctypes.POINTER(Config), ctypes.POINTER(Bodies),
                                               ctypes.POINTER(Bodies)]),
+    ("shapes_batches_run_io", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                             ctypes.POINTER(Config), ctypes.c_int32, ctypes.POINTER(Bodies),
+                                             STEP_CALLBACK, ctypes.c_void_p]),
     ("shapes_batch_get_launch", ctypes.c_int, [ctypes.c_void_p, _ip, _ip, _ip]),
     ("shapes_batch_set_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_batch_get_world_order", ctypes.c_int, [ctypes.c_void_p, _ip]),
@@ -228,6 +235,20 @@ def step_many_io(batches, cfg: "Config", inputs, outputs) -> int:
     ins = (Bodies * n)(*inputs)
     outs = (Bodies * n)(*outputs)
     return int(lib().shapes_batches_step_io(arr, n, ctypes.byref(cfg), ins, outs))
+
+
+def run_io(batches, cfg: "Config", nsteps: int, states, on_step=None) -> int:
+    """`nsteps` steps of several handles whose body state lives in host
+    memory (`states`: Bodies structs, one per handle): every step uploads,
+    steps and writes the result back in place (shapes_batches_run_io, one
+    host thread per handle).  on_step(k, s), if given, runs after step s of
+    handle k and may change states[k]; a true return stops that handle.
+    Returns the status (0 or the first error)."""
+    n = len(batches)
+    arr = (ctypes.c_void_p * n)(*[b.handle for b in batches])
+    st = (Bodies * n)(*states)
+    cb = STEP_CALLBACK(lambda _user, k, s: int(bool(on_step(k, s)))) if on_step else STEP_CALLBACK()
+    return int(lib().shapes_batches_run_io(arr, n, ctypes.byref(cfg), nsteps, st, cb, None))
 
 
 class Batch:

@@ -21,7 +21,7 @@ PROBE_LIB = OUT_DIR / "libshapes_probe.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
-              "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-shared"]
+              "-Xcompiler", "-fPIC,-ffp-contract=off,-O2,-pthread", "-shared", "-lpthread"]
 
 SOURCES = [CSRC / "shapes_gpu.cu", CSRC / "mlp.cu"]
 HEADERS = [CSRC / "step_kernels.cuh", CSRC / "large_world.cuh", CSRC / "learned.cuh", CSRC / "fp64_ops.cuh",

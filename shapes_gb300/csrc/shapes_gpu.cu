@@ -21,6 +21,8 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/shapes_gpu.h"
@@ -1014,38 +1016,51 @@ struct shapes_batch {
     stage(5, 1, [&]() { shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, cfg.dt, 1); });
   }
 
+  /* The state a refused or regrown step returns to: the pose-and-velocity
+   * fields, the cache (keys, Lagrangians, world offsets), the learned mask and
+   * the sample count, copied in one launch. */
+  void snapshot_segments(shapes::Segments& sg, int& n, bool to_snap, int cap) {
+    n = 0;
+    auto add = [&](void* live, void* snap, unsigned long long bytes) {
+      sg.src[n] = to_snap ? live : snap;
+      sg.dst[n] = to_snap ? snap : live;
+      sg.bytes[n] = bytes;
+      ++n;
+    };
+    for (int k = 0; k < 6; ++k) add(body[k], snap_body[k], sizeof(double) * (unsigned long long)N);
+    add(c_key[cache_buf], snap_key, sizeof(uint64_t) * (unsigned long long)cap);
+    add(lam[cache_buf], snap_lam, sizeof(double) * 2ull * (unsigned long long)cap);
+    add(cwo[cache_buf], snap_cwo, sizeof(int32_t) * (unsigned long long)(W + 1));
+    if (learned_mask) add(learned_mask, snap_mask, (unsigned long long)W);
+    if (ds_count) add(ds_count, snap_ds_count, sizeof(unsigned long long));
+  }
+  void copy_segments(const shapes::Segments& sg, int n) {
+    unsigned long long most = 0;
+    for (int k = 0; k < n; ++k) most = std::max(most, sg.bytes[k]);
+    const unsigned blocks = (unsigned)std::max<unsigned long long>(1, std::min<unsigned long long>((most / 8 + 255) / 256, 512));
+    shapes::k_copy_segments<<<dim3(blocks, (unsigned)n), 256, 0, stream>>>(sg);
+    ck(cudaGetLastError(), "launch");
+  }
   void snapshot() {
-    for (int k = 0; k < 6; ++k)
-      ck(cudaMemcpyAsync(snap_body[k], body[k], sizeof(double) * N, cudaMemcpyDeviceToDevice, stream), "snapshot");
-    ck(cudaMemcpyAsync(snap_key, c_key[cache_buf], sizeof(uint64_t) * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
-    ck(cudaMemcpyAsync(snap_lam, lam[cache_buf], sizeof(double) * 2 * contact_cap, cudaMemcpyDeviceToDevice, stream), "snapshot");
-    ck(cudaMemcpyAsync(snap_cwo, cwo[cache_buf], sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "snapshot");
-    if (learned_mask)
-      ck(cudaMemcpyAsync(snap_mask, learned_mask, W, cudaMemcpyDeviceToDevice, stream), "snapshot");
-    if (ds_count)
-      ck(cudaMemcpyAsync(snap_ds_count, ds_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream),
-         "snapshot");
+    shapes::Segments sg{};
+    int n = 0;
+    snapshot_segments(sg, n, true, contact_cap);
+    copy_segments(sg, n);
   }
 
   /* Restore into buffer `buf` (which becomes the cache buffer). */
   void restore(int saved_cap) {
-    for (int k = 0; k < 6; ++k)
-      ck(cudaMemcpyAsync(body[k], snap_body[k], sizeof(double) * N, cudaMemcpyDeviceToDevice, stream), "restore");
-    ck(cudaMemcpyAsync(c_key[cache_buf], snap_key, sizeof(uint64_t) * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
-    ck(cudaMemcpyAsync(lam[cache_buf], snap_lam, sizeof(double) * 2 * saved_cap, cudaMemcpyDeviceToDevice, stream), "restore");
-    ck(cudaMemcpyAsync(cwo[cache_buf], snap_cwo, sizeof(int32_t) * (W + 1), cudaMemcpyDeviceToDevice, stream), "restore");
-    if (learned_mask)
-      ck(cudaMemcpyAsync(learned_mask, snap_mask, W, cudaMemcpyDeviceToDevice, stream), "restore");
-    if (ds_count)
-      ck(cudaMemcpyAsync(ds_count, snap_ds_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream),
-         "restore");
+    shapes::Segments sg{};
+    int n = 0;
+    snapshot_segments(sg, n, false, saved_cap);
+    copy_segments(sg, n);
   }
 
   /* Asynchronous body-state upload for shapes_batches_step_io: caller arrays
    * into the staging arrays with the finiteness check into the bad-input
    * counter, then the staged state into the live arrays unless the check
    * failed, and a re-pose of the bodies whose pose inputs changed. */
-  void io_upload(const shapes_bodies* in);
+  void io_upload(const shapes_bodies* in, double* const* mapped = nullptr);
   void io_commit() {
     shapes::Ptr10 p{};
     for (int k = 0; k < 10; ++k) {
@@ -1058,7 +1073,11 @@ struct shapes_batch {
     shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, 0.0, 0, body_changed);
     ck(cudaGetLastError(), "launch");
   }
-  void io_download(shapes_bodies* out);
+  void io_download(shapes_bodies* out, double* const* mapped = nullptr);
+  /* After an io step was enqueued: waits, and on refused input undoes the
+   * step (SHAPES_E_NAN); otherwise finishes it, re-running the staged input
+   * alone after a buffer regrowth. */
+  int io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out = nullptr);
 
   /* One call of `nsteps` steps (or one collide when !solve) in three parts,
    * so that several handles can have their steps in flight at once
@@ -1069,7 +1088,9 @@ struct shapes_batch {
    * restored and grown, and the call must be enqueued again. */
   static constexpr int kRunRetry = 1;
   int run_retries = 0, run_saved_cache_buf = 0, run_saved_cap = 0;
-  unsigned long long run_counters[shapes::kCntSlots] = {0};
+  /* pinned host copy of the step counters (kCntSlots), so that reading them
+   * back is an asynchronous copy and the wait happens where the caller waits */
+  unsigned long long* run_counters = nullptr;
 
   void prepare(const shapes_config& cfg, bool solve) {
     ensure_items(solve ? cfg.iterations : 0);
@@ -1095,7 +1116,13 @@ struct shapes_batch {
     results_buf = wb;
   }
   void enqueue_end() {
-    ck(cudaMemcpyAsync(run_counters, counters, sizeof(run_counters), cudaMemcpyDeviceToHost, stream), "read counters");
+    if (!run_counters) {
+      ck(cudaMallocHost(&run_counters, sizeof(unsigned long long) * shapes::kCntSlots), "cudaMallocHost");
+      std::memset(run_counters, 0, sizeof(unsigned long long) * shapes::kCntSlots);
+    }
+    ck(cudaMemcpyAsync(run_counters, counters, sizeof(unsigned long long) * shapes::kCntSlots, cudaMemcpyDeviceToHost,
+                       stream),
+       "read counters");
   }
   void enqueue(const shapes_config& cfg, int32_t nsteps, bool solve) {
     enqueue_begin(solve);
@@ -1349,6 +1376,7 @@ struct shapes_batch {
     for (int k = 0; k < 6; ++k) dfree(snap_body[k]);
     dfree(snap_cwo);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    if (run_counters) cudaFreeHost(run_counters);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 };
@@ -1578,32 +1606,71 @@ int shapes_batches_step_io(shapes_batch* const* bs, int32_t n, const shapes_conf
     }
     int rc = SHAPES_OK;
     for (int32_t k = 0; k < n; ++k) {
-      shapes_batch* b = bs[k];
-      ck(cudaStreamSynchronize(b->stream), "step");
-      int r;
-      if (b->run_counters[shapes::kCntBadInput]) { /* refused: undo the step taken on the old state */
-        b->cache_buf = b->run_saved_cache_buf;
-        b->restore(b->run_saved_cap);
-        b->pose(0, 0.0);
-        ck(cudaStreamSynchronize(b->stream), "restore");
-        b->have_results = false;
-        r = SHAPES_E_NAN;
-      } else {
-        r = b->finish(*cfg, true);
-        while (r == shapes_batch::kRunRetry) { /* grown and restored: the staged input again, alone */
-          b->enqueue_begin(true);
-          b->io_commit();
-          b->enqueue_one(*cfg, true);
-          b->io_download(&out[k]);
-          b->enqueue_end();
-          r = b->finish(*cfg, true);
-        }
-        b->residual_valid = r == SHAPES_OK && ((cfg->flags & SHAPES_FLAG_RESIDUAL) || b->learned_on(*cfg));
-      }
+      const int r = bs[k]->io_finish(*cfg, &out[k]);
       if (r != SHAPES_OK && rc == SHAPES_OK) rc = r;
     }
     return rc;
   });
+}
+
+static bool mapped_host10(double* const host[10], double* dev[10]);
+
+int shapes_batches_run_io(shapes_batch* const* bs, int32_t n, const shapes_config* cfg, int32_t nsteps,
+                          shapes_bodies* state, shapes_step_callback on_step, void* user) {
+  if (!bs || n < 1 || nsteps < 0 || !state) return SHAPES_E_INVALID_ARG;
+  for (int32_t k = 0; k < n; ++k) {
+    if (!bs[k] || !body_arrays_ok(&state[k])) return SHAPES_E_INVALID_ARG;
+    for (int32_t j = 0; j < k; ++j)
+      if (bs[j] == bs[k] || bs[j]->stream == bs[k]->stream) return SHAPES_E_INVALID_ARG;
+  }
+  const int rc0 = check_cfg(cfg);
+  if (rc0 != SHAPES_OK) return rc0;
+  std::vector<int> status(n, SHAPES_OK);
+  std::vector<std::string> detail(n);
+  /* handle k's loop: its steps in order, one wait per step */
+  auto lane = [&](int32_t k) {
+    shapes_batch* b = bs[k];
+    status[k] = guarded([&]() -> int {
+      ck(cudaSetDevice(b->device), "cudaSetDevice");
+      double* bp[10];
+      body_ptrs(&state[k], bp);
+      double* mapped[10];
+      const bool is_mapped = mapped_host10(bp, mapped); /* resolved once for the whole run */
+      double* const* mp = is_mapped ? mapped : nullptr;
+      for (int32_t s = 0; s < nsteps; ++s) {
+        b->prepare(*cfg, true);
+        b->run_retries = 0;
+        b->enqueue_begin(true);
+        b->io_upload(&state[k], mp);
+        b->io_commit();
+        b->enqueue_one(*cfg, true);
+        b->io_download(&state[k], mp);
+        b->enqueue_end();
+        const int r = b->io_finish(*cfg, &state[k], mp);
+        if (r != SHAPES_OK) return r;
+        if (on_step && on_step(user, k, s) != 0) break;
+      }
+      return SHAPES_OK;
+    });
+    detail[k] = g_last_error;
+  };
+  std::vector<std::thread> threads;
+  try {
+    for (int32_t k = 1; k < n; ++k) threads.emplace_back(lane, k);
+  } catch (const std::system_error&) {
+    for (auto& t : threads) t.join();
+    g_last_error = "could not start a host thread";
+    return SHAPES_E_CAPACITY;
+  }
+  lane(0);
+  for (auto& t : threads) t.join();
+  for (int32_t k = 0; k < n; ++k)
+    if (status[k] != SHAPES_OK) {
+      g_last_error = detail[k];
+      return status[k];
+    }
+  g_last_error.clear();
+  return SHAPES_OK;
 }
 
 int shapes_batch_collide(shapes_batch* b) {
@@ -1632,13 +1699,40 @@ static bool mapped_host10(double* const host[10], double* dev[10]) {
   return true;
 }
 
-static dim3 copy10_grid(int n) { return dim3((unsigned)std::min<int64_t>((n + 255) / 256, 1024), 10); }
+static dim3 copy10_grid(int n) {
+  const int64_t per_block = 256 * shapes::kCopy10PerThread;
+  return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, 1024)), 10);
+}
 
-void shapes_batch::io_upload(const shapes_bodies* in) {
+int shapes_batch::io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out) {
+  ck(cudaStreamSynchronize(stream), "step");
+  if (run_counters[shapes::kCntBadInput]) { /* refused: undo the step taken on the old state */
+    cache_buf = run_saved_cache_buf;
+    restore(run_saved_cap);
+    pose(0, 0.0);
+    ck(cudaStreamSynchronize(stream), "restore");
+    have_results = false;
+    return SHAPES_E_NAN;
+  }
+  int r = finish(cfg, true);
+  while (r == kRunRetry) { /* grown and restored: the staged input again, alone */
+    enqueue_begin(true);
+    io_commit();
+    enqueue_one(cfg, true);
+    io_download(out, mapped_out);
+    enqueue_end();
+    r = finish(cfg, true);
+  }
+  residual_valid = r == SHAPES_OK && ((cfg.flags & SHAPES_FLAG_RESIDUAL) || learned_on(cfg));
+  return r;
+}
+
+void shapes_batch::io_upload(const shapes_bodies* in, double* const* mapped) {
   double* bp[10];
   body_ptrs(in, bp);
   double* dp[10];
-  if (mapped_host10(bp, dp)) {
+  if (mapped || mapped_host10(bp, dp)) {
+    if (mapped) std::copy(mapped, mapped + 10, dp);
     shapes::Ptr10 p{};
     for (int k = 0; k < 10; ++k) {
       p.src[k] = dp[k];
@@ -1655,11 +1749,12 @@ void shapes_batch::io_upload(const shapes_bodies* in) {
   ck(cudaGetLastError(), "launch");
 }
 
-void shapes_batch::io_download(shapes_bodies* out) {
+void shapes_batch::io_download(shapes_bodies* out, double* const* mapped) {
   double* bp[10];
   body_ptrs(out, bp);
   double* dp[10];
-  if (mapped_host10(bp, dp)) {
+  if (mapped || mapped_host10(bp, dp)) {
+    if (mapped) std::copy(mapped, mapped + 10, dp);
     shapes::Ptr10 p{};
     for (int k = 0; k < 10; ++k) {
       p.src[k] = body[k];

@@ -200,16 +200,76 @@ struct Ptr10 {
   double* dst[10];
 };
 
+/* Ten arrays of n doubles, array blockIdx.y; non-finite values set *bad_flag.
+ * When both ends are 16-byte aligned each thread keeps four 16-byte loads in
+ * flight, so a copy over the host link needs few blocks (copy10_grid sizes
+ * the grid for kCopy10PerThread doubles a thread) and leaves the SMs to the
+ * steps of other handles. */
+constexpr int kCopy10PerThread = 8;
+
 __global__ void k_copy10(Ptr10 p, int n, unsigned long long* bad_flag) {
   const double* __restrict__ src = p.src[blockIdx.y];
   double* __restrict__ dst = p.dst[blockIdx.y];
   bool bad = false;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double v = src[i];
-    bad |= !isfinite(v);
-    dst[i] = v;
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+    const double2* __restrict__ s2 = reinterpret_cast<const double2*>(src);
+    double2* __restrict__ d2 = reinterpret_cast<double2*>(dst);
+    const int n2 = n >> 1;
+    for (; i + 3 * stride < n2; i += 4 * stride) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = s2[i + u * stride];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        bad |= !isfinite(v[u].x) || !isfinite(v[u].y);
+        d2[i + u * stride] = v[u];
+      }
+    }
+    for (; i < n2; i += stride) {
+      const double2 v = s2[i];
+      bad |= !isfinite(v.x) || !isfinite(v.y);
+      d2[i] = v;
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+      const double v = src[n - 1];
+      bad |= !isfinite(v);
+      dst[n - 1] = v;
+    }
+  } else {
+    for (; i < n; i += stride) {
+      const double v = src[i];
+      bad |= !isfinite(v);
+      dst[i] = v;
+    }
   }
   if (bad_flag && __any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(bad_flag, 1ull);
+}
+
+/* Up to kMaxSegments device-to-device copies in one launch (the retry
+ * snapshot of a step and its restore): blockIdx.y picks the segment; every
+ * segment starts on an allocation base (8-byte aligned), so whole 8-byte
+ * words are copied and the last bytes singly. */
+constexpr int kMaxSegments = 12;
+struct Segments {
+  const void* src[kMaxSegments];
+  void* dst[kMaxSegments];
+  unsigned long long bytes[kMaxSegments];
+};
+
+__global__ void k_copy_segments(Segments s) {
+  const int k = blockIdx.y;
+  const unsigned long long nb = s.bytes[k], nw = nb >> 3;
+  const uint64_t* __restrict__ sw = static_cast<const uint64_t*>(s.src[k]);
+  uint64_t* __restrict__ dw = static_cast<uint64_t*>(s.dst[k]);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (unsigned long long i = t; i < nw; i += stride) dw[i] = sw[i];
+  if (t < (nb & 7ull)) {
+    const unsigned long long b = (nw << 3) + t;
+    static_cast<uint8_t*>(s.dst[k])[b] = static_cast<const uint8_t*>(s.src[k])[b];
+  }
 }
 
 /* Contacts in the caller's layout (keys i, j, fa, fb, flip and values nx, ny,

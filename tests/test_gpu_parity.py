@@ -595,3 +595,81 @@ def test_batches_step_io_matches_separate_calls():
         assert_bits_equal(keep[0][1][f].numpy(), want0[f], f"other handle still stepped {f}")
     for h in hs + refs:
         h.close()
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_batches_run_io_matches_separate_calls(pinned):
+    """Host-resident state stepped by shapes_batches_run_io (one host thread
+    per handle) equals set_bodies + step + get_bodies on each handle, with the
+    callback changing a body between steps; a non-finite value written by the
+    callback stops that handle with SHAPES_E_NAN and its state as before that
+    step while the other handles run to the end."""
+    import ctypes
+    import threading
+
+    import torch
+
+    big = scenes.subset_worlds(scenes.batched_columns(n_worlds=48), list(range(30)))
+    parts = [scenes.subset_worlds(big, list(range(k, 30, 3))) for k in range(3)]
+    cfg = config_of(parts[0])
+    streams = [torch.cuda.Stream() for _ in parts]
+    hs, refs, states, keep = [], [], [], []
+    for sc_, st in zip(parts, streams):
+        h, r = batch_from_scene(sc_), batch_from_scene(sc_)
+        h.set_stream(st.cuda_stream)
+        h.step(cfg, 20)
+        r.step(cfg, 20)
+        cur = h.get_bodies()
+        arrs = {f: torch.from_numpy(cur[f].copy()) for f in _lib.BODY_FIELDS}
+        if pinned:
+            arrs = {f: a.pin_memory() for f, a in arrs.items()}
+        states.append(_lib.Bodies(*[ctypes.cast(arrs[f].data_ptr(), _lib._dp) for f in _lib.BODY_FIELDS]))
+        keep.append(arrs)
+        hs.append(h)
+        refs.append(r)
+    lock = threading.Lock()
+    seen = []
+
+    def on_step(k, s):
+        with lock:
+            seen.append((k, s))
+        if k == 1 and s == 2:
+            keep[1]["vel_x"][4] += 0.25  # the next step starts from the changed state
+        return False
+
+    assert _lib.run_io(hs, cfg, 5, states, on_step) == 0
+    assert sorted(seen) == [(k, s) for k in range(3) for s in range(5)]
+    for k, r in enumerate(refs):
+        for s in range(5):
+            r.step(cfg, 1)
+            if k == 1 and s == 2:
+                b = r.get_bodies()
+                b["vel_x"][4] += 0.25
+                r.set_bodies(b)
+        want = r.get_bodies()
+        for f in STATE_FIELDS:
+            assert_bits_equal(keep[k][f].numpy(), want[f], f"run_io handle {k} {f}")
+            assert_bits_equal(hs[k].get_bodies()[f], want[f], f"run_io device state {k} {f}")
+
+    def poison(k, s):
+        if k == 2 and s == 1:
+            keep[2]["pos_y"][3] = float("nan")
+        return False
+
+    refs[0].step(cfg, 3)
+    refs[1].step(cfg, 3)
+    refs[2].step(cfg, 2)  # handle 2: steps 0 and 1 taken, step 2 refused
+    assert _lib.run_io(hs, cfg, 3, states, poison) == _lib.SHAPES_E_NAN
+    for k in range(3):
+        want = refs[k].get_bodies()
+        for f in STATE_FIELDS:
+            assert_bits_equal(hs[k].get_bodies()[f], want[f], f"after the refusal, handle {k} {f}")
+    # a callback that asks to stop ends that handle's loop
+    assert _lib.run_io(hs[:1], cfg, 4, states[:1], lambda k, s: True) == 0
+    refs[0].step(cfg, 1)
+    want = refs[0].get_bodies()
+    for f in STATE_FIELDS:
+        assert_bits_equal(hs[0].get_bodies()[f], want[f], f"stopped after one step {f}")
+        assert_bits_equal(keep[0][f].numpy(), want[f], f"stopped after one step, host state {f}")
+    for h in hs + refs:
+        h.close()
