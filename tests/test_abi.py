@@ -42,6 +42,18 @@ def test_strerror_and_argument_errors(built):
     h = ctypes.c_void_p()
     assert L.shapes_batch_create(0, None, None, None, None, None, ctypes.byref(h)) == _lib.SHAPES_E_INVALID_ARG
     assert L.shapes_batch_step(None, None, 1) == _lib.SHAPES_E_INVALID_ARG
+    # the multi-handle entry points refuse missing handles, counts and buffers
+    cfg = _lib.make_config(1.0 / 60.0)
+    none = (ctypes.c_void_p * 1)(None)
+    bodies = (_lib.Bodies * 1)()
+    assert L.shapes_batches_step(None, 1, ctypes.byref(cfg), 1) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batches_step_io(none, 1, ctypes.byref(cfg), bodies, bodies) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batches_run_io(none, 0, ctypes.byref(cfg), 1, bodies, _lib.STEP_CALLBACK(),
+                                   None) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batches_run_io(none, 1, ctypes.byref(cfg), -1, bodies, _lib.STEP_CALLBACK(),
+                                   None) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batches_run_io(none, 1, ctypes.byref(cfg), 1, bodies, _lib.STEP_CALLBACK(),
+                                   None) == _lib.SHAPES_E_INVALID_ARG
 
 
 def test_product_does_not_import_oracle():
