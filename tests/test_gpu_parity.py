@@ -673,3 +673,37 @@ def test_batches_run_io_matches_separate_calls(pinned):
         assert_bits_equal(keep[0][f].numpy(), want[f], f"stopped after one step, host state {f}")
     for h in hs + refs:
         h.close()
+
+
+def test_run_io_with_ragged_and_empty_worlds():
+    """Two handles over the ragged scene (empty, one-body and static-only
+    worlds in both) stepped by shapes_batches_run_io from pageable host
+    arrays equal the oracle's worlds."""
+    import ctypes
+
+    import torch
+
+    sc = scenes.ragged_worlds()
+    parts = [scenes.subset_worlds(sc, list(range(0, 5))), scenes.subset_worlds(sc, list(range(5, 10)))]
+    cfg = config_of(sc)
+    streams = [torch.cuda.Stream() for _ in parts]
+    hs, states, keep = [], [], []
+    for p, st in zip(parts, streams):
+        h = batch_from_scene(p)
+        h.set_stream(st.cuda_stream)
+        cur = h.get_bodies()
+        arrs = {f: np.ascontiguousarray(cur[f]) for f in _lib.BODY_FIELDS}
+        states.append(_lib.Bodies(*[arrs[f].ctypes.data_as(_lib._dp) for f in _lib.BODY_FIELDS]))
+        keep.append(arrs)
+        hs.append(h)
+    assert _lib.run_io(hs, cfg, 25, states) == 0
+    for p, h, arrs in zip(parts, hs, keep):
+        ow = oracle_worlds(p)
+        step_oracles(ow, p, 25)
+        compare_bodies(h, ow, p, "run_io ragged")
+        off = p["world_body_offsets"]
+        for w, o in enumerate(ow):
+            want = o.bodies()
+            for f in STATE_FIELDS:
+                assert_bits_equal(arrs[f][off[w]:off[w + 1]], want[f], f"run_io ragged host state {w} {f}")
+        h.close()
