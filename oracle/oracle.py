@@ -67,6 +67,11 @@ def lib() -> ctypes.CDLL:
         L.oracle_unordered_pairs_count.restype = ctypes.c_int64
         L.oracle_unordered_pairs_count.argtypes = [ctypes.c_int32]
         L.oracle_sincos.argtypes = [_dp, _dp, _dp, ctypes.c_int64]
+        L.oracle_sincos_phase.argtypes = [ctypes.c_int32, _dp, _dp, ctypes.POINTER(ctypes.c_uint8), ctypes.c_int64]
+        L.oracle_sincos_vs_libm.argtypes = [_dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), _dp, ctypes.c_int64]
+        L.oracle_world_set_trig.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+        L.oracle_world_trig_mismatches.restype = ctypes.c_int64
+        L.oracle_world_trig_mismatches.argtypes = [ctypes.c_void_p]
         L.oracle_world_delete.restype = ctypes.c_int32
         L.oracle_world_delete.argtypes = [ctypes.c_void_p, ctypes.c_int32]
         L.oracle_world_append.restype = ctypes.c_int32
@@ -108,6 +113,15 @@ class OracleWorld:
              nsteps=1):
         cfg = np.array([dt, baumgarte, slop, accel[0], accel[1]], dtype=np.float64)
         lib().oracle_world_step(self._h, _p(cfg, _dp), iterations, int(warm_start), int(external), nsteps)
+
+    def set_trig(self, libm: bool) -> None:
+        """Rotations from the host libm's sin/cos (libm=True, what the
+        reference calls) or from shapes_sincos (the default); re-poses."""
+        lib().oracle_world_set_trig(self._h, int(bool(libm)))
+
+    def trig_mismatches(self) -> int:
+        """libm mode: poses so far whose libm sin or cos differs from shapes_sincos."""
+        return int(lib().oracle_world_trig_mismatches(self._h))
 
     def collide(self):
         lib().oracle_world_collide(self._h)
@@ -226,3 +240,25 @@ def sincos(x: np.ndarray):
     c = np.empty_like(x)
     lib().oracle_sincos(_p(x, _dp), _p(s, _dp), _p(c, _dp), len(x))
     return s, c
+
+
+def sincos_phase(x: np.ndarray, mode: int):
+    """shapes_sincos's phases separately: mode 0 the accurate phase, 1 the fast
+    phase's unrounded (s_hi, s_lo, c_hi, c_lo) and a decided flag, 2 libm."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty((len(x), 4), dtype=np.float64)
+    ok = np.empty(len(x), dtype=np.uint8)
+    lib().oracle_sincos_phase(mode, _p(x, _dp), _p(out, _dp), ok.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                              len(x))
+    return out, ok.astype(bool)
+
+
+def sincos_vs_libm(x: np.ndarray, cap: int = 1000):
+    """(sin mismatches, cos mismatches, accurate-phase calls, mismatching args)
+    of shapes_sincos against the host libm over x."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    counts = (ctypes.c_int64 * 3)()
+    bad = np.empty(cap, dtype=np.float64)
+    lib().oracle_sincos_vs_libm(_p(x, _dp), len(x), counts, _p(bad, _dp), cap)
+    nb = min(cap, int(counts[0]) + int(counts[1]))
+    return int(counts[0]), int(counts[1]), int(counts[2]), bad[:nb]

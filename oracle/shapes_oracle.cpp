@@ -15,7 +15,10 @@
  * behaviour follows the reference too.
  *
  * Deviations, all deliberate and shared with the CUDA path:
- *   - sin/cos come from shapes_sincos() instead of libm (see shapes_sincos.h);
+ *   - sin/cos come from shapes_sincos() (correctly rounded, see
+ *     shapes_sincos.h) instead of libm; a world can be switched to the host
+ *     libm's sin and cos (oracle_world_set_trig), which is what the reference
+ *     calls, to measure how far the two choices drift apart;
  *   - the solver sweep count is a parameter (the reference hard-codes 2 sweeps,
  *     Engine/Main.hs:81-82; iterations=2 reproduces it);
  *   - warm starting can be switched off (the reference always warm-starts).
@@ -91,6 +94,8 @@ struct ContactConstraint {
 
 struct World {
   double residual = 0.0; /* RMS of one non-applying sweep after the last step */
+  bool trig_libm = false; /* rotations from the host libm's sin and cos instead of shapes_sincos */
+  int64_t trig_mismatches = 0; /* libm mode: poses whose libm sin or cos differs from shapes_sincos */
   std::vector<Body> bodies;
   /* EmptiesVector (Utils/EmptiesVector.hs): filled slots, and the empty
    * slots as a stack (delete pushes, append pops: the last slot freed is the
@@ -165,9 +170,17 @@ static void init_hull(Hull& h, int nv, const double* xy) {
  * joinTransforms (Transform.hs:73-77) of translate (outer) and rotate (inner),
  * multiplied as 3x3 matrices (MatrixTemplate.hs:47-67), applied by afmul
  * (Linear.hs:217-220) to each local vertex; normals re-derived per edge. */
-static void pose_hull(const Body& b, Hull& h) {
+static void pose_hull(const Body& b, Hull& h, bool trig_libm, int64_t* mismatches) {
   double s, c;
-  shapes_sincos(b.th, &s, &c);
+  if (trig_libm) { /* rotate22 (Linear.hs:353-357): cosDouble# and sinDouble# are libm's cos and sin */
+    c = std::cos(b.th);
+    s = std::sin(b.th);
+    double s2, c2;
+    shapes_sincos(b.th, &s2, &c2);
+    if (std::memcmp(&s, &s2, 8) != 0 || std::memcmp(&c, &c2, 8) != 0) ++*mismatches;
+  } else {
+    shapes_sincos(b.th, &s, &c);
+  }
   const double T[3][3] = {{1.0, 0.0, b.px}, {0.0, 1.0, b.py}, {0.0, 0.0, 1.0}};
   const double R[3][3] = {{c, -s, 0.0}, {s, c, 0.0}, {0.0, 0.0, 1.0}};
   double M[3][3];
@@ -854,7 +867,7 @@ static void step_world(World& w, const StepConfig& cfg) {
   }
   /* 7. moveShapes (World.hs:136-140) */
   for (size_t i = 0; i < w.bodies.size(); ++i)
-    if (w.active[i]) pose_hull(w.bodies[i], w.hulls[i]);
+    if (w.active[i]) pose_hull(w.bodies[i], w.hulls[i], w.trig_libm, &w.trig_mismatches);
 }
 
 static StepConfig make_cfg(const double* c5, int32_t iterations, int32_t warm_start, int32_t external) {
@@ -882,7 +895,7 @@ void* oracle_world_create(int32_t n, const double* bodies10, const int32_t* vert
     const double* r = bodies10 + 10 * (size_t)i;
     w->bodies[i] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
     init_hull(w->hulls[i], vert_off[i + 1] - vert_off[i], local_xy + 2 * (size_t)vert_off[i]);
-    pose_hull(w->bodies[i], w->hulls[i]);
+    pose_hull(w->bodies[i], w->hulls[i], w->trig_libm, &w->trig_mismatches);
   }
   return w;
 }
@@ -919,7 +932,7 @@ int32_t oracle_world_append(void* h, const double* body10, int32_t nv, const dou
   const double* r = body10;
   w.bodies[slot] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
   init_hull(w.hulls[slot], nv, local_xy);
-  pose_hull(w.bodies[slot], w.hulls[slot]);
+  pose_hull(w.bodies[slot], w.hulls[slot], w.trig_libm, &w.trig_mismatches);
   w.active[slot] = 1;
   return slot;
 }
@@ -932,7 +945,7 @@ void oracle_world_set_bodies(void* h, const double* bodies10) {
   for (size_t i = 0; i < w.bodies.size(); ++i) {
     const double* r = bodies10 + 10 * i;
     w.bodies[i] = Body{r[0], r[1], r[2], r[3], r[4], r[5], r[6], r[7], r[8], r[9]};
-    pose_hull(w.bodies[i], w.hulls[i]);
+    pose_hull(w.bodies[i], w.hulls[i], w.trig_libm, &w.trig_mismatches);
   }
 }
 
@@ -1108,5 +1121,66 @@ int64_t oracle_unordered_pairs_count(int32_t n) {
 void oracle_sincos(const double* x, double* s, double* c, int64_t n) {
   for (int64_t k = 0; k < n; ++k) shapes_sincos(x[k], &s[k], &c[k]);
 }
+
+/* The two phases of shapes_sincos separately (tests of the function itself):
+ * mode 0 the accurate phase alone; mode 1 the fast phase's unrounded
+ * double-double results (s hi, s lo, c hi, c lo in out4, ok[k] = 0 where it
+ * declines); mode 2 the host libm's sin and cos. */
+void oracle_sincos_phase(int32_t mode, const double* x, double* out4, uint8_t* ok, int64_t n) {
+  for (int64_t k = 0; k < n; ++k) {
+    double* o = out4 + 4 * k;
+    if (mode == 0) {
+      shapes_sincos_accurate(x[k], &o[0], &o[2]);
+      o[1] = o[3] = 0.0;
+      ok[k] = 1;
+    } else if (mode == 1) {
+      ok[k] = (uint8_t)shapes_sincos_fast(x[k], o);
+    } else {
+      o[0] = std::sin(x[k]);
+      o[2] = std::cos(x[k]);
+      o[1] = o[3] = 0.0;
+      ok[k] = 1;
+    }
+  }
+}
+
+/* Counts, over n arguments, how often shapes_sincos differs from the host
+ * libm (sin and cos separately) and how often the fast phase could not decide
+ * (counts3 = sin mismatches, cos mismatches, accurate-phase calls).  Stores
+ * up to `cap` mismatching arguments. */
+void oracle_sincos_vs_libm(const double* x, int64_t n, int64_t* counts3, double* bad, int64_t cap) {
+  int64_t ns = 0, nc = 0, na = 0, nb = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    double s, c, o[4];
+    shapes_sincos(x[k], &s, &c);
+    const double ax = std::fabs(x[k]);
+    if (ax >= 0x1p-27 && ax < 0x1p16 &&
+        !(shapes_sincos_fast(x[k], o) && shapes_sc_decided(o[0], o[1]) && shapes_sc_decided(o[2], o[3])))
+      ++na;
+    const double ls = std::sin(x[k]), lc = std::cos(x[k]);
+    const bool ds = std::memcmp(&s, &ls, 8) != 0, dc = std::memcmp(&c, &lc, 8) != 0;
+    ns += ds;
+    nc += dc;
+    if ((ds || dc) && nb < cap) bad[nb++] = x[k];
+  }
+  counts3[0] = ns;
+  counts3[1] = nc;
+  counts3[2] = na;
+}
+
+/* Selects the rotation source of one world (0: shapes_sincos, 1: the host
+ * libm's sin and cos) and re-poses its shapes with it.  The world's count of
+ * libm poses that differ from shapes_sincos restarts at 0. */
+void oracle_world_set_trig(void* h, int32_t libm) {
+  World& w = *static_cast<World*>(h);
+  w.trig_libm = libm != 0;
+  w.trig_mismatches = 0;
+  for (size_t i = 0; i < w.bodies.size(); ++i)
+    if (w.active[i]) pose_hull(w.bodies[i], w.hulls[i], w.trig_libm, &w.trig_mismatches);
+}
+
+/* libm mode: how many poses so far used a libm sin or cos that differs from
+ * the correctly rounded shapes_sincos value (every pose counts once). */
+int64_t oracle_world_trig_mismatches(void* h) { return static_cast<World*>(h)->trig_mismatches; }
 
 }  // extern "C"

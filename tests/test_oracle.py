@@ -78,10 +78,12 @@ def test_sincos_accuracy(O):
         worst = max(worst, _ulp_err(si, ws), _ulp_err(ci, wc))
         same += int(si == ws) + int(ci == wc)
     assert worst <= 1.0, worst
-    assert same / (2 * len(xs)) > 0.95
+    assert same / (2 * len(xs)) > 0.99  # the rest are the libm's rounding errors (tests/test_sincos.py)
     assert math.copysign(1.0, O.sincos(np.array([-0.0]))[0][0]) == -1.0
-    s, c = O.sincos(np.array([math.inf, math.nan, 1e300]))
+    s, c = O.sincos(np.array([math.inf, -math.inf, math.nan]))
     assert np.isnan(s).all() and np.isnan(c).all()
+    s, c = O.sincos(np.array([1e300]))  # huge arguments are reduced exactly (Payne-Hanek)
+    assert abs(_ulp_err(s[0], math.sin(1e300))) <= 1.0 and abs(_ulp_err(c[0], math.cos(1e300))) <= 1.0
 
 
 def grid_culled_keys(world_xy, vert_off, static):
