@@ -77,6 +77,13 @@ WORKLOADS = {
 }
 PLAIN_ITERATIONS = {"learned": 8, "batched": 8, "single": 4, "mixed": 8, "contacts": 0, "container": 4,
                     "balls": 8}
+# Untimed steps (plain start) run from the initial state before the warm-up, by
+# both arms, so that the timed window sees the settled, contact-heavy pile (the
+# many-world scenes reach their plateau of about 550 contacts per 256-body
+# world by step 300).  The container's drop lasts thousands of steps and its
+# CPU sample is one thread: it settles nothing by default.
+SETTLE = {"learned": 300, "batched": 300, "single": 300, "mixed": 300, "contacts": 0, "container": 0,
+          "balls": 300}
 
 
 def make_scene(workload: str, seed_offset: int = 0, worlds: int | None = None):
@@ -228,9 +235,10 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "of fallback"}
 
 
-def cpu_oracle_rate(scene, steps: int, warmup: int, nthreads: int, world_fraction: float = 1.0, seed: int = 0):
-    """Steps a sample of the scene's worlds on the CPU oracle; returns
-    (body-steps/s, bodies in sample, steps, seconds)."""
+def cpu_oracle_rate(scene, steps: int, warmup: int, nthreads: int, world_fraction: float = 1.0, seed: int = 0,
+                    settle: int = 0):
+    """Steps a sample of the scene's worlds on the CPU oracle (`settle` + `warmup`
+    untimed steps first); returns (body-steps/s, bodies in sample, steps, seconds)."""
     from oracle import oracle as O
     from shapes_gb300 import scenes
 
@@ -243,14 +251,14 @@ def cpu_oracle_rate(scene, steps: int, warmup: int, nthreads: int, world_fractio
     worlds = [O.world_from_scene(scene, w) for w in range(W)]
     c = scene["config"]
     args = (c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"])
-    if warmup:
-        O.batch_step(worlds, *args, nsteps=warmup, nthreads=nthreads)
+    if settle + warmup:
+        O.batch_step(worlds, *args, nsteps=settle + warmup, nthreads=nthreads)
     secs = O.batch_step(worlds, *args, nsteps=steps, nthreads=nthreads)
     n = int(scene["world_body_offsets"][-1])
     return n * steps / secs, n, steps, secs
 
 
-def cpu_sample(workload, scene, steps, warmup, cores):
+def cpu_sample(workload, scene, steps, warmup, cores, settle=0):
     """The oracle on a bounded sample of the workload: (rate, description)."""
     from oracle import oracle as O
 
@@ -265,13 +273,16 @@ def cpu_sample(workload, scene, steps, warmup, cores):
         w = O.world_from_scene(scene)
         c = scene["config"]
         k = min(steps, 3 if workload == "container" else 300)
+        if settle + warmup:
+            w.step(c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"], nsteps=settle + warmup)
         t0 = time.perf_counter()
         w.step(c["dt"], c["baumgarte"], c["slop"], c["accel"], c["iterations"], nsteps=k)
         secs = time.perf_counter() - t0
-        return n * k / secs, f"{n} bodies x {k} steps from the initial state, 1 thread (one world), {secs:.1f} s", 1
+        return n * k / secs, (f"{n} bodies x {k} steps after {settle} settle + {warmup} warm-up steps, 1 thread "
+                              f"(one world), {secs:.1f} s"), 1
     cs = min(steps, 300)
-    rate, n, s_, secs = cpu_oracle_rate(scene, cs, warmup, cores)
-    return rate, (f"all {n} bodies x {s_} steps after {warmup} warm-up, plain start, "
+    rate, n, s_, secs = cpu_oracle_rate(scene, cs, warmup, cores, settle=settle)
+    return rate, (f"all {n} bodies x {s_} steps after {settle} settle + {warmup} warm-up steps, plain start, "
                   f"{int(scene['config']['iterations'])} sweeps, {secs:.1f} s on {cores} threads"), cores
 
 
@@ -287,12 +298,13 @@ def run_reference(args, rank, world):
     cores = multiprocessing.cpu_count()
     scene = make_scene(args.workload, worlds=args.worlds)
     n = int(scene["world_body_offsets"][-1])
-    rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, cores)
+    rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, cores, settle=args.settle)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / rate, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "bodies": n},
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "bodies": n,
+                   "settle_steps": args.settle},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": used, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -376,15 +388,19 @@ class Lanes:
             b.close()
 
 
-def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10, coloured=False):
-    """Steps a fresh copy with the residual flag: (mean over steps of the
-    world-mean residual, mean over sampled steps of the world-mean largest
-    depth, per-world max residual, per-world max depth, contacts started by
-    the network)."""
+def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10, coloured=False, settle=0,
+                settle_iterations=None):
+    """Steps a fresh copy `settle` steps with the plain start, then `steps` steps
+    with the residual flag: (mean over steps of the world-mean residual, mean
+    over sampled steps of the world-mean largest depth, per-world max residual,
+    per-world max depth, contacts started by the network)."""
     c = scene["config"]
     cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], iterations, residual=True,
                            learned=net is not None, coloured=coloured)
     b = new_batch(_lib, scene, stream)
+    if settle:
+        b.step(_lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], settle_iterations or iterations,
+                                coloured=coloured), settle)
     if net is not None:
         b.set_mlp(net)
     W = b.n_worlds
@@ -456,20 +472,21 @@ def run_ours(args, rank, world, local):
     run_it, run_learned = plain_it, False
     if args.workload == "learned":
         net, train_info = train_network(_lib, stream, args, rank)
-        qs = min(args.steps, args.quality_steps)
-        p_res, p_dep, p_wres, p_wdep, _ = quality_run(_lib, scene, stream, plain_it, qs)
+        qs = args.quality_steps
+        kw = {"settle": args.settle, "settle_iterations": plain_it}
+        p_res, p_dep, p_wres, p_wdep, _ = quality_run(_lib, scene, stream, plain_it, qs, **kw)
         sweep = []
         for it in range(1, plain_it + 1):
-            l_res, l_dep, _, _, pred = quality_run(_lib, scene, stream, it, qs, net=net)
+            l_res, l_dep, _, _, pred = quality_run(_lib, scene, stream, it, qs, net=net, **kw)
             row = {"iterations": it, "learned_residual": l_res, "learned_depth": l_dep,
                    "predicted_per_step": pred / qs}
             if args.plain_sweep or it == plain_it:
-                q = (p_res, p_dep) if it == plain_it else quality_run(_lib, scene, stream, it, qs)[:2]
+                q = (p_res, p_dep) if it == plain_it else quality_run(_lib, scene, stream, it, qs, **kw)[:2]
                 row["plain_residual"], row["plain_depth"] = q
             sweep.append(row)
         matched = [r_["iterations"] for r_ in sweep
                    if r_["learned_residual"] <= p_res and r_["learned_depth"] <= p_dep]
-        learned = {"training": train_info, "quality_steps": qs,
+        learned = {"training": train_info, "quality_steps": qs, "quality_after_settle_steps": args.settle,
                    "plain": {"iterations": plain_it, "residual": p_res, "depth": p_dep},
                    "sweep": sweep, "matched_iterations": min(matched) if matched else None,
                    "judge": "per world: back to the plain start once its residual exceeds the plain run's "
@@ -503,11 +520,16 @@ def run_ours(args, rank, world, local):
     n_worlds = len(scene["world_body_offsets"]) - 1
     lanes = args.lanes if args.lanes > 0 else (8 if n_worlds >= 256 else 4 if n_worlds >= 64 else 1)
 
-    def timed(it, use_net):
-        """K steps after W warm-up from a fresh copy; returns (ms, batch)."""
+    cfg_settle = cfg_for(plain_it, False)
+
+    def timed(it, use_net, settle=args.settle):
+        """K steps after `settle` (plain start) and W warm-up steps from a fresh
+        copy; returns (ms, batch)."""
         cfg = cfg_for(it, use_net)
         if lanes > 1:
             ln = Lanes(_lib, scene, lanes, tuned, torch)
+            if settle:
+                ln.step(cfg_settle, settle)
             if use_net:
                 ln.set_mlp(net, p_wres, p_wdep)
             ln.step(cfg, args.warmup)
@@ -520,12 +542,16 @@ def run_ours(args, rank, world, local):
             barrier(world)
             ln.close()
             b = new_batch(_lib, scene, stream, tuned)  # the single handle for stats and the profiled pass
+            if settle:
+                b.step(cfg_settle, settle)
             if use_net:
                 b.set_mlp(net)
                 b.set_judge(p_wres, p_wdep)
             b.step(cfg, args.warmup + args.steps)
             return t0.elapsed_time(t1), b, cfg
         b = new_batch(_lib, scene, stream, tuned)
+        if settle:
+            b.step(cfg_settle, settle)
         if use_net:
             b.set_mlp(net)
             b.set_judge(p_wres, p_wdep)
@@ -555,6 +581,16 @@ def run_ours(args, rank, world, local):
         learned["learned_value"] = total_bodies * args.steps / (max_over_ranks(learned_ms, world) * 1e-3)
         if max_over_ranks(learned_ms, world) >= max_over_ranks(plain_ms, world):
             run_it, run_learned = plain_it, False
+    free_fall = None
+    if args.settle:
+        # the same window from the initial state (the pile still falling), reported beside the value
+        ff_ms, bff, _ = timed(run_it, run_learned, settle=0)
+        st_ff = bff.stats()
+        bff.close()
+        free_fall = {"value": total_bodies * args.steps / (max_over_ranks(ff_ms, world) * 1e-3),
+                     "ms_per_step": max_over_ranks(ff_ms, world) / args.steps,
+                     "window": f"steps {args.warmup + 1}-{args.warmup + args.steps} from the initial state",
+                     "last_step": {"pairs": st_ff["pairs"], "contacts": st_ff["contacts"]}}
     with ClockSampler(local) as clocks:
         ms, b, cfg = timed(run_it, run_learned)
     st = b.stats()
@@ -616,6 +652,11 @@ def run_ours(args, rank, world, local):
             b.set_mlp(net)
             b.set_judge(p_wres, p_wdep)
         handles = [b]
+    if args.settle:
+        if ln:
+            ln.step(cfg_settle, args.settle)
+        else:
+            b.step(cfg_settle, args.settle)
     if ln:
         ln.step(cfg, args.warmup)
     else:
@@ -653,54 +694,42 @@ def run_ours(args, rank, world, local):
     else:
         b.close()
 
-    # ---- roofline of the dominant kernel (profiled pass) -------------------
-    solve_ms, solve_launches = prof["solve"]
-    items = st_prof["solver_items"]
+    # ---- roofline of the dominant stage (profiled pass of the same window) -
     solver_kernel = "k_schedule_solve" if not tuned or tuned[2] == 1 else f"k_group_solve<{tuned[2]}>"
     if args.workload == "container":
         solver_kernel = "k_lw_color_pass + k_lw_color_seq" if args.coloured else "k_lw_ordered"
+    items = st_prof["solver_items"]
     if items == 0 and st_prof["contacts"] > 0:
         # large-world solvers count no items: the last step's contacts x (sweeps + warm-start pass)
-        # per profiled step; the stage holds every kernel of the solve (ordered: one launch a step)
         items = st_prof["contacts"] * (run_it + 1) * prof_steps
-    peaks = measured_peaks()
-    roof = None
-    if solve_launches and solve_ms > 0:
-        avg_ms = solve_ms / solve_launches
-        bytes_per_launch = items / solve_launches * SOLVER_BYTES_PER_ITEM
-        achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-        roof = {"kernel": solver_kernel, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                "traffic": items / solve_launches * (GROUP_SOLVE_DRAM_BYTES_PER_ITEM if "group" in solver_kernel
-                                                     else SOLVER_DRAM_BYTES_PER_ITEM),
-                "traffic_source": ("ncu dram bytes per update of k_group_solve<4, parallel levels> (mixed, 256 worlds)"
-                                   if "group" in solver_kernel else
-                                   "ncu dram bytes per update of k_schedule_solve (batched, 512 worlds)")
-                                  + " x updates per launch",
-                "bytes_per_item": SOLVER_BYTES_PER_ITEM,
-                "items_per_launch": items / solve_launches, "avg_launch_ms": avg_ms}
-        fp64_peak = measure_fp64_peak()
-        if fp64_peak:
-            fp64 = {"kernel": solver_kernel, "peak_lane_ops_per_s": fp64_peak,
-                    "peak_source": "measured by this script (fp64 add/mul chains)",
-                    "ops_per_item": SOLVER_FP64_OPS_PER_ITEM,
-                    "achieved_lane_ops_per_s": items * SOLVER_FP64_OPS_PER_ITEM / (solve_ms * 1e-3)}
-            fp64["frac"] = fp64["achieved_lane_ops_per_s"] / fp64_peak
-            roof["fp64"] = fp64
-            per_body = STEP_FP64_INST_PER_BODY_STEP.get(args.workload)
-            if per_body:  # the whole step against the FP64 pipe, at the timed throughput
-                roof["step_fp64"] = {
-                    "thread_instructions_per_body_step": per_body,
-                    "source": "ncu DADD+DMUL+DFMA thread-instruction counters of the timed steps, mixed scene",
-                    "achieved_per_s": per_body * value / world, "peak_per_s": fp64_peak,
-                    "frac": per_body * value / world / fp64_peak}
+    vbar = (len(scene["local_xy"]) // 2) / max(n_bodies, 1)  # mean vertices per body
+    units = stage_units(n_bodies, st_prof, items, prof_steps)
+    roof = stage_roofline(prof, units, vbar, solver_kernel, measured_peaks())
+    fp64_peak = measure_fp64_peak()
+    if roof and fp64_peak:
+        # FP64 lane-operations of the whole step from per-unit counts (ncu) times
+        # this window's own units (bodies, pairs, contacts, solver updates)
+        ops = sum(FP64_OPS_PER_UNIT[k] * units[k] / prof_steps for k in FP64_OPS_PER_UNIT if k in units)
+        step_ms = ms_max / args.steps
+        roof["step_fp64"] = {
+            "lane_ops_per_step": ops, "per_unit": FP64_OPS_PER_UNIT, "units_per_step":
+                {k: units[k] / prof_steps for k in FP64_OPS_PER_UNIT if k in units},
+            "source": FP64_OPS_SOURCE, "achieved_per_s": ops / (step_ms * 1e-3), "peak_per_s": fp64_peak,
+            "peak_source": "measured by this script (fp64 add/mul chains)",
+            "frac": ops / (step_ms * 1e-3) / fp64_peak}
+        k = roof["stage"]
+        if k in FP64_OPS_PER_UNIT:
+            stage_ops = FP64_OPS_PER_UNIT[k] * units[k] / prof[k][1]
+            roof["fp64"] = {"lane_ops_per_launch": stage_ops, "achieved_per_s": stage_ops / (roof["avg_launch_ms"] * 1e-3),
+                            "peak_per_s": fp64_peak, "frac": stage_ops / (roof["avg_launch_ms"] * 1e-3) / fp64_peak}
 
     # ---- CPU baseline (rank 0, N=1 only), bounded sample ---------------------
     cpu = None
     if world == 1 and rank == 0 and not args.no_cpu:
         import multiprocessing
 
-        rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, multiprocessing.cpu_count())
+        rate, sample, used = cpu_sample(args.workload, scene, args.steps, args.warmup, multiprocessing.cpu_count(),
+                                        settle=args.settle)
         cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port", "sample": sample}
 
     if rank == 0:
@@ -711,6 +740,10 @@ def run_ours(args, rank, world, local):
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload],
                        "bodies_per_gpu": n_bodies, "worlds_per_gpu": int(len(scene["world_body_offsets"]) - 1),
                        "iterations": run_it, "start": "learned" if run_learned else "plain (previous-frame cache)",
+                       "settle_steps": args.settle,
+                       "window": f"steps {args.settle + args.warmup + 1}-{args.settle + args.warmup + args.steps} "
+                                 f"(after {args.settle} untimed settle steps with the plain start and {args.warmup} "
+                                 "warm-up steps)",
                        "large_world_solver": ("coloured" if args.coloured else "ordered")
                        if args.workload == "container" else None,
                        "parallelism": f"worlds sharded, {world} rank(s)" + (
@@ -736,6 +769,7 @@ def run_ours(args, rank, world, local):
             "clocks": clocks.summary(),
             "stages_ms_per_step": {k: v[0] / prof_steps for k, v in prof.items()},
             "last_step": {"pairs": st["pairs"], "contacts": st["contacts"]},
+            "free_fall": free_fall,
         }
         if learned is not None:
             line["learned"] = learned
@@ -860,28 +894,95 @@ def run_contacts(args, rank, world, local, scene, stream):
     return 0
 
 
+def stage_units(n_bodies, st, items, steps):
+    """Work units of each stage over `steps` profiled steps (pairs and contacts
+    are the last step's, taken as the window's per-step count)."""
+    return {"integrate": n_bodies * steps, "broadphase": n_bodies * steps, "narrowphase": st["pairs"] * steps,
+            "build": st["contacts"] * steps, "solve": items, "pairs": st["pairs"] * steps,
+            "contacts": st["contacts"] * steps}
+
+
+def stage_bytes(stage, units, vbar):
+    """Algorithmic DRAM bytes of a stage over its units (per-unit figures below)."""
+    if stage == "integrate":
+        return units["integrate"] * (POSE_BYTES_FIXED + POSE_BYTES_PER_VERTEX * vbar)
+    if stage == "broadphase":
+        return units["broadphase"] * BROADPHASE_BYTES_PER_BODY + units["pairs"] * BROADPHASE_BYTES_PER_PAIR
+    if stage == "narrowphase":
+        return units["pairs"] * (32 * 2 * vbar + 8 + 2 * 44) + units["contacts"] * 57
+    if stage == "build":
+        return units["build"] * BUILD_BYTES_PER_CONTACT
+    if stage == "solve":
+        return units["solve"] * SOLVER_BYTES_PER_ITEM
+    return None
+
+
+STAGE_KERNELS = {"integrate": "k_integrate_pose", "broadphase": "grid / incremental pair kernels",
+                 "narrowphase": "k_narrowphase (+ class sort)", "build": "k_build", "schedule": "levels",
+                 "scan": "scans", "learned": "k_learned_features + k_mlp_predict"}
+
+
+def stage_roofline(prof, units, vbar, solver_kernel, peaks):
+    """Roofline of the stage with the largest share of the profiled window:
+    algorithmic bytes per launch over its average launch time."""
+    ranked = sorted(((v[0], k) for k, v in prof.items() if v[1] > 0), reverse=True)
+    for ms, k in ranked:
+        by = stage_bytes(k, units, vbar)
+        if by is None:
+            continue
+        launches = prof[k][1]
+        avg_ms = ms / launches
+        per_launch = by / launches
+        achieved = per_launch / (avg_ms * 1e-3) / 1e9
+        kernel = solver_kernel if k == "solve" else STAGE_KERNELS.get(k, k)
+        dram = STAGE_DRAM_BYTES_PER_UNIT.get(k if k != "solve" or "group" in solver_kernel else "solve_schedule")
+        unit_key = k
+        return {"kernel": kernel, "stage": k, "stage_share": ms / sum(v[0] for v in prof.values()),
+                "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                "traffic": dram[0] * units[unit_key] / launches if dram else None,
+                "traffic_source": dram[1] if dram else "no ncu capture of this stage",
+                "algorithmic_bytes_per_launch": per_launch, "units_per_launch": units[unit_key] / launches,
+                "avg_launch_ms": avg_ms}
+    return None
+
+
+# Algorithmic bytes of k_integrate_pose per body: velocities, position and
+# angle, inverse masses and the vertex offset read (24 + 24 + 16 + 8); position
+# and angle, box, box keys and flags written (24 + 32 + 32 + 1); per vertex the
+# local point and the two extent indices read (16 + 8), the world point, unit
+# normal and the two self extents written (16 + 16 + 16).
+POSE_BYTES_FIXED = 24 + 24 + 16 + 8 + 24 + 32 + 32 + 1
+POSE_BYTES_PER_VERTEX = 16 + 8 + 16 + 16 + 16
+# broadphase: box keys and flags read per body, one (i, j) pair written.
+BROADPHASE_BYTES_PER_BODY = 32 + 1
+BROADPHASE_BYTES_PER_PAIR = 8
+# k_build per contact: contact key and values (57) + both bodies' positions
+# and inverse masses (2 x 32) + the previous cache entry (32) read; the
+# 152-byte constraint lines + the new cache entry (32) written.
+BUILD_BYTES_PER_CONTACT = 57 + 64 + 32 + 152 + 32
+# DRAM bytes per unit measured by ncu (dram__bytes_read.sum + write.sum over
+# the launch's units), for the `traffic` field: the settled mixed scene (128
+# worlds x 256 bodies, step 306: 68,786 pairs, 70,521 contacts, 634,429 solver
+# updates), profiles/fp64_units_mixed128.md.
+STAGE_DRAM_BYTES_PER_UNIT = {
+    "solve": (30.2, "ncu dram bytes per update of k_group_solve<4, parallel levels> (mixed, 256 worlds) x updates"),
+    "solve_schedule": (30.5, "ncu dram bytes per update of k_schedule_solve (settled mixed, 128 worlds) x updates"),
+    "narrowphase": (123.5, "ncu dram bytes per pair of k_narrowphase (settled mixed, 128 worlds) x pairs"),
+    "build": (147.0, "ncu dram bytes per contact of k_build (settled mixed, 128 worlds) x contacts"),
+    "integrate": (177.0, "ncu dram bytes per body of k_integrate_pose (settled mixed, 128 worlds) x bodies"),
+}
+# FP64 lane-operations (ncu DADD + DMUL + DFMA thread instructions, predicated
+# on) per unit of each stage, same capture: per solver update, per pair, per
+# contact, per body.  The broadphase, scans and schedule issue none.
+FP64_OPS_PER_UNIT = {"solve": 68.5, "narrowphase": 264.5, "build": 84.6, "integrate": 328.6}
+FP64_OPS_SOURCE = ("ncu dadd+dmul+dfma thread-instruction counts per unit of each kernel (settled mixed scene, "
+                   "profiles/fp64_units_mixed128.md), times this window's units")
+
 # Algorithmic bytes per broadphase pair in the narrowphase: both hulls' posed
 # vertices and edge normals (32 B per vertex, 5.5 vertices on average), the
 # pair's two body indices, and two fixed output slots (2 x (4 + 40) B).
 NARROWPHASE_BYTES_PER_PAIR = 32 * 11 + 8 + 2 * 44
-
-# FP64 lane-operations per solver update: ncu's dadd + dmul + dfma thread
-# instruction counts of one k_schedule_solve launch (26.9 M) divided by its
-# 370,978 updates (batched workload, 512 worlds, settled frame); the hand count
-# is 69 per sweep update and 36 per warm-start update.
-SOLVER_FP64_OPS_PER_ITEM = 72.5
-# DRAM bytes per solver update in the same capture (dram__bytes_read.sum +
-# dram__bytes_write.sum = 12.70 MB over 370,978 updates): the working set is
-# L2-resident, so traffic is far below the algorithmic bytes.
-SOLVER_DRAM_BYTES_PER_ITEM = 34.2
-# FP64 thread-instructions (DADD + DMUL + DFMA, active lanes) per body-step of
-# the whole step on the mixed scene (ncu counters over the timed steps of one
-# handle over 1024 worlds x 256 bodies: 4.307e8 per step / 262,144 bodies).
-STEP_FP64_INST_PER_BODY_STEP = {"learned": 1643.0, "mixed": 1643.0}
-# the same for k_group_solve<4> with parallel levels (one ncu capture, mixed
-# scene, 256 worlds, settled frame): 26.15 MB over 865,243 updates.
-GROUP_SOLVE_DRAM_BYTES_PER_ITEM = 30.2
-
 
 def main():
     ap = argparse.ArgumentParser()
@@ -897,7 +998,12 @@ def main():
                     "[,parallel_levels[,spread_heavy]]' (size order) instead of the autotuner")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
     ap.add_argument("--tune-steps", type=int, default=30, help="steps per autotuner trial")
-    ap.add_argument("--quality-steps", type=int, default=300, help="steps of each residual/penetration run")
+    ap.add_argument("--quality-steps", type=int, default=100,
+                    help="steps of each residual/penetration run (after the settle steps)")
+    ap.add_argument("--settle", type=int, default=-1,
+                    help="untimed steps (plain start) from the initial state before the warm-up, in both arms "
+                         "(-1: the workload's default, 300 for the many-world scenes and the single world, 0 for "
+                         "the container and contacts)")
     ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
     ap.add_argument("--lanes", type=int, default=0,
@@ -914,6 +1020,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
+    if args.settle < 0:
+        args.settle = SETTLE[args.workload]
     global INCREMENTAL_PAIRS
     INCREMENTAL_PAIRS = not args.no_incremental
     rank, world, local = dist_init()
