@@ -9,12 +9,12 @@ seeded scene generators (`scenes`).
 """
 from ._lib import Batch, Config, ShapesError, lib, make_config  # noqa: F401
 from .engine import (ContactBehavior, EngineConfig, EngineState, change_scene, init_engine,  # noqa: F401
-                     make_constant_accel, make_hull, make_physical_obj, make_rectangle_hull, make_world,
+                     make_circle, make_constant_accel, make_hull, make_physical_obj, make_rectangle_hull, make_world,
                      make_world_obj, run_engine, run_world, step_world, update_world)
 
 __all__ = [
     "Batch", "Config", "ShapesError", "lib", "make_config",
     "ContactBehavior", "EngineConfig", "EngineState", "init_engine", "change_scene", "update_world",
     "step_world", "run_engine", "run_world", "make_physical_obj", "make_world", "make_world_obj",
-    "make_constant_accel", "make_hull", "make_rectangle_hull",
+    "make_circle", "make_constant_accel", "make_hull", "make_rectangle_hull",
 ]

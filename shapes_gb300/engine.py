@@ -8,7 +8,9 @@ shapes/src/Physics/Engine/Main.hs:32-98).  State lives on the device behind a
 Differences forced by the boundary:
   - `External` is data, not a closure: `make_constant_accel` (External.hs:23-28)
     or None (`const id`).
-  - circles are rejected (`make_circle` raises; the ABI returns UNSUPPORTED).
+  - a circle (`make_circle`, Engine.hs:53-54) crosses the ABI as one local
+    point (radius, 0) with kind SHAPES_SHAPE_CIRCLE; its centre is the body's
+    position, as `circleWithRadius` makes it.
   - the solver sweep count is `EngineConfig.iterations` (the reference
     hard-codes 2 sweeps, Engine/Main.hs:81-82).
 """

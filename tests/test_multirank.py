@@ -54,3 +54,12 @@ def test_rank_failure_is_seen_on_the_host(tmp_path):
     codes = _launch("fail", tmp_path, timeout=180)
     assert codes[1] == 3
     assert codes[0] != 0  # rank 0's barrier/collective errors out instead of hanging
+
+
+def test_sharded_worlds_equal_one_run(tmp_path):
+    """Worlds are independent: each rank steps its shard of one scene on the
+    oracle, and the union of the shards equals one process stepping every
+    world (the property the world-sharded bench relies on)."""
+    codes = _launch("shard", tmp_path, timeout=300)
+    assert codes == [0, 0]
+    assert (tmp_path / "r0.txt").read_text().startswith("ok 12 worlds over 2 ranks")
