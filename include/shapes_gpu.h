@@ -350,14 +350,23 @@ void shapes_batch_destroy(shapes_batch* b);
  *   held by every GPU that loads the library until the process exits.
  *   The first call on a device looks up the array's device address
  *   (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   The address is kept for the life of the process: after cudaDeviceReset
+ *   on that device the function must not be called again.
  *   All calls share the one array: calls that overlap on the GPU (different
  *   streams, threads or processes sharing the library) race.  The call
  *   synchronizes `cuda_stream` (NULL = legacy default stream) before it
  *   returns, so consecutive calls on one stream are safe.
  *   Inputs (device): pos_x, pos_y, rot, inv_mass_lin, inv_mass_rot [n];
- *   vert_offsets [n+1] (vert_offsets[0] = 0, 3..64 vertices per body,
- *   checked on the device); local_verts_xy [2*n_verts], counter-clockwise
- *   convex hulls.  Outputs (device): pairs_ij [2*pair_capacity],
+ *   vert_offsets [n+1]; local_verts_xy [2*n_verts].  Only convex hulls are
+ *   accepted (no circles): every body needs 3..64 vertices (vert_offsets[0]
+ *   = 0, vert_offsets[n] = n_verts) forming a strictly convex,
+ *   counter-clockwise polygon of finite points, and finite position, angle
+ *   and inverse masses.  These are checked on the device before any other
+ *   kernel runs: bad offsets or a zero-length edge give
+ *   SHAPES_E_INVALID_ARG, a non-finite value SHAPES_E_NAN, a hull that is not
+ *   strictly convex and counter-clockwise SHAPES_E_NONCONVEX (as
+ *   shapes_batch_create), with the reason in shapes_last_error_detail.
+ *   Outputs (device): pairs_ij [2*pair_capacity],
  *   contact_keys5 / contact_vals5 [5*contact_capacity] in the layouts of
  *   shapes_batch_get_pairs / shapes_batch_get_contacts; *n_pairs and
  *   *n_contacts (host) are set even when the capacities are too small

@@ -2920,11 +2920,20 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaPlan.total];
 
 namespace {
 
+/* Reasons the set-up kernel rejects an input (bits of the bad-input counter). */
+constexpr unsigned long long kNaBadOffsets = 1, kNaBadNaN = 2, kNaBadNonconvex = 4, kNaBadEdge = 8;
+
 /* Per-call set-up in scratch: the one-world offsets, de-interleaved local
- * vertices and zeroed row modes; checks the caller's vertex offsets so that
- * no later kernel can index outside the vertex arrays.  The counters were
- * zeroed by the host before this kernel. */
-__global__ void k_noalloc_setup(int n, int nv, const int32_t* vert_off, const double* local_xy,
+ * vertices and zeroed row modes.  Validates the caller's input as
+ * shapes_batch_create does on the host, so that no later kernel indexes
+ * outside the vertex arrays or meets a hull it cannot handle: every body needs
+ * 3..64 vertices inside [0, n_verts) (offsets starting at 0 and ending at
+ * n_verts), a strictly convex counter-clockwise hull of finite points with no
+ * zero-length edge (the same products and comparisons as the host check), and
+ * finite position, angle and inverse masses.  The counters were zeroed by the
+ * host before this kernel. */
+__global__ void k_noalloc_setup(int n, int nv, const int32_t* vert_off, const double* local_xy, const double* px,
+                                const double* py, const double* th, const double* iml, const double* imr,
                                 unsigned char* base) {
   int32_t* wbo = reinterpret_cast<int32_t*>(base + kNaPlan.world_body_off);
   int32_t* bw = reinterpret_cast<int32_t*>(base + kNaPlan.body_world);
@@ -2936,13 +2945,32 @@ __global__ void k_noalloc_setup(int n, int nv, const int32_t* vert_off, const do
   if (t0 == 0) {
     wbo[0] = 0;
     wbo[1] = n;
-    if (vert_off[0] != 0 || vert_off[n] != nv) atomicOr(&cnt[shapes::kCntBadInput], 1ull);
+    if (vert_off[0] != 0 || vert_off[n] != nv) atomicOr(&cnt[shapes::kCntBadInput], kNaBadOffsets);
   }
   for (int i = t0; i < n; i += stride) {
     bw[i] = 0;
     mode[i] = 0;
-    const int c = vert_off[i + 1] - vert_off[i];
-    if (c < 3 || c > shapes::kMaxVerts) atomicOr(&cnt[shapes::kCntBadInput], 1ull);
+    unsigned long long bad = 0;
+    if (!isfinite(px[i]) || !isfinite(py[i]) || !isfinite(th[i]) || !isfinite(iml[i]) || !isfinite(imr[i]))
+      bad |= kNaBadNaN;
+    const int o0 = vert_off[i], o1 = vert_off[i + 1], c = o1 - o0;
+    if (o0 < 0 || o1 > nv || c < 3 || c > shapes::kMaxVerts) {
+      bad |= kNaBadOffsets;
+    } else { /* the hull lies inside the caller's vertex array: check it */
+      const double* xy = local_xy + 2 * (size_t)o0;
+      for (int k = 0; k < 2 * c; ++k)
+        if (!isfinite(xy[k])) bad |= kNaBadNaN;
+      if (!(bad & kNaBadNaN)) {
+        for (int k = 0; k < c; ++k) {
+          const int k1 = k + 1 < c ? k + 1 : k + 1 - c, k2 = k + 2 < c ? k + 2 : k + 2 - c;
+          const double ex = xy[2 * k1] - xy[2 * k], ey = xy[2 * k1 + 1] - xy[2 * k + 1];
+          const double fx = xy[2 * k2] - xy[2 * k1], fy = xy[2 * k2 + 1] - xy[2 * k1 + 1];
+          if (ex == 0.0 && ey == 0.0) bad |= kNaBadEdge;
+          else if (ex * fy - ey * fx <= 0.0) bad |= kNaBadNonconvex;
+        }
+      }
+    }
+    if (bad) atomicOr(&cnt[shapes::kCntBadInput], bad);
   }
   for (int v = t0; v < nv; v += stride) {
     lx[v] = local_xy[2 * (size_t)v];
@@ -3006,8 +3034,10 @@ extern "C" int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, con
                                       double* contact_vals5, int64_t contact_capacity, void* cuda_stream,
                                       int64_t* n_pairs, int64_t* n_contacts) {
   if (!pos_x || !pos_y || !rot || !inv_mass_lin || !inv_mass_rot || !vert_offsets || !local_verts_xy || !n_pairs ||
-      !n_contacts || n_bodies < 1 || n_verts < 3 * n_bodies)
+      !n_contacts || n_bodies < 1 || n_verts < 3 * n_bodies) {
+    g_last_error = "shapes_collide_noalloc: a null pointer, no bodies, or fewer than 3 vertices per body";
     return SHAPES_E_INVALID_ARG;
+  }
   if (n_bodies > kNaMaxBodies || n_verts > kNaMaxVerts) {
     g_last_error = "shapes_collide_noalloc: more than SHAPES_NOALLOC_MAX_BODIES bodies or SHAPES_NOALLOC_MAX_VERTS vertices";
     return SHAPES_E_CAPACITY;
@@ -3070,8 +3100,8 @@ extern "C" int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, con
   cudaError_t e = cudaMemsetAsync(d.counters, 0, 8 * sizeof(unsigned long long), st);
   unsigned long long cnt[8] = {0};
   if (e == cudaSuccess) {
-    k_noalloc_setup<<<grid_for(std::max(n_bodies, n_verts), 256), 256, 0, st>>>(n_bodies, n_verts, vert_offsets,
-                                                                                 local_verts_xy, base);
+    k_noalloc_setup<<<grid_for(std::max(n_bodies, n_verts), 256), 256, 0, st>>>(
+        n_bodies, n_verts, vert_offsets, local_verts_xy, pos_x, pos_y, rot, inv_mass_lin, inv_mass_rot, base);
     e = cudaMemcpyAsync(cnt, d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -3080,7 +3110,21 @@ extern "C" int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, con
     g_last_error = std::string("shapes_collide_noalloc: ") + cudaGetErrorString(e);
     return SHAPES_E_CUDA;
   }
-  if (cnt[shapes::kCntBadInput]) return SHAPES_E_INVALID_ARG;
+  if (const unsigned long long bad = cnt[shapes::kCntBadInput]) {
+    if (bad & (kNaBadOffsets | kNaBadEdge)) {
+      g_last_error = (bad & kNaBadOffsets)
+                         ? "shapes_collide_noalloc: vert_offsets must start at 0, end at n_verts and give every body "
+                           "3..64 vertices (circles are not accepted)"
+                         : "shapes_collide_noalloc: a hull has a zero-length edge";
+      return SHAPES_E_INVALID_ARG;
+    }
+    if (bad & kNaBadNaN) {
+      g_last_error = "shapes_collide_noalloc: a position, angle, inverse mass or hull point is not finite";
+      return SHAPES_E_NAN;
+    }
+    g_last_error = "shapes_collide_noalloc: a hull is not strictly convex and counter-clockwise";
+    return SHAPES_E_NONCONVEX;
+  }
   shapes::k_init_extents<<<grid_for(n_verts, 128), 128, 0, st>>>(d);
   shapes::k_integrate_pose<<<grid_for(n_bodies, 128), 128, 0, st>>>(d, 0.0, 0);
   shapes::k_broadphase<true><<<grid_for((long long)n_bodies * 32, 256), 256, 0, st>>>(d);
@@ -3104,8 +3148,14 @@ extern "C" int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, con
     g_last_error = "shapes_collide_noalloc: more than SHAPES_NOALLOC_MAX_PAIRS broadphase pairs";
     return SHAPES_E_CAPACITY;
   }
-  if (*n_pairs > pair_capacity || *n_contacts > contact_capacity) return SHAPES_E_BUFFER;
-  if ((*n_pairs > 0 && !pairs_ij) || (*n_contacts > 0 && (!contact_keys5 || !contact_vals5))) return SHAPES_E_INVALID_ARG;
+  if (*n_pairs > pair_capacity || *n_contacts > contact_capacity) {
+    g_last_error = "shapes_collide_noalloc: pair_capacity or contact_capacity below *n_pairs / *n_contacts";
+    return SHAPES_E_BUFFER;
+  }
+  if ((*n_pairs > 0 && !pairs_ij) || (*n_contacts > 0 && (!contact_keys5 || !contact_vals5))) {
+    g_last_error = "shapes_collide_noalloc: null output buffer";
+    return SHAPES_E_INVALID_ARG;
+  }
   if (*n_pairs > 0 || *n_contacts > 0) {
     k_noalloc_out<<<grid_for(std::max(*n_pairs, *n_contacts), 256), 256, 0, st>>>(
         (int)*n_pairs, (int)*n_contacts, base, pairs_ij, contact_keys5, contact_vals5);
