@@ -146,6 +146,7 @@ struct shapes_batch {
   int32_t* slot_feat = nullptr;
   double* slot_val = nullptr;
   int32_t* np_perm = nullptr;
+  int32_t* pose_order = nullptr; /* [N] bodies grouped by vertex count within chunks of 1024 */
   int32_t* np_cls = nullptr; /* [2 * kNpClasses + 1] */
   int32_t* world_pair_off = nullptr;
   /* contacts: ping-pong between two buffers, the cache of step s is the
@@ -377,6 +378,7 @@ struct shapes_batch {
     d.world_body_off = world_body_off;
     d.body_world = body_world;
     d.vert_off = vert_off;
+    d.pose_order = pose_order;
     d.lx = lx;
     d.ly = ly;
     d.radius = radius;
@@ -1223,6 +1225,7 @@ struct shapes_batch {
     free_step_buffers();
     dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly); dfree(emin); dfree(emax);
     dfree(radius);
+    dfree(pose_order);
     radius = nullptr;
     for (int k = 0; k < 10; ++k) {
       dfree(body[k]);
@@ -1281,6 +1284,28 @@ struct shapes_batch {
        "upload");
     ck(cudaMemcpy(body_world, h_body_world.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
     ck(cudaMemcpy(vert_off, vert_offsets, sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "upload");
+    {
+      /* pose order: stable counting sort by vertex count within each chunk of
+       * 1024 bodies (a warp of the pose kernel then runs one loop length;
+       * chunks keep the gathers local) */
+      std::vector<int32_t> order(N);
+      constexpr int32_t kChunk = 1024;
+      for (int32_t c0 = 0; c0 < N; c0 += kChunk) {
+        const int32_t c1 = std::min<int32_t>(N, c0 + kChunk);
+        int32_t cnt[shapes::kMaxVerts + 2] = {0};
+        for (int32_t b = c0; b < c1; ++b) ++cnt[std::min<int32_t>(vert_offsets[b + 1] - vert_offsets[b], shapes::kMaxVerts + 1)];
+        int32_t pos[shapes::kMaxVerts + 2];
+        int32_t acc = c0;
+        for (int k = 0; k < shapes::kMaxVerts + 2; ++k) {
+          pos[k] = acc;
+          acc += cnt[k];
+        }
+        for (int32_t b = c0; b < c1; ++b)
+          order[pos[std::min<int32_t>(vert_offsets[b + 1] - vert_offsets[b], shapes::kMaxVerts + 1)]++] = b;
+      }
+      pose_order = dalloc<int32_t>(std::max<int32_t>(N, 1), "cudaMalloc");
+      if (N) ck(cudaMemcpy(pose_order, order.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "upload");
+    }
     /* a circle's one local point (radius, 0) becomes radius[b] and the local
      * centre (0, 0) (circleWithRadius, Contact/Circle.hs:24-25) */
     h_radius.assign(N, 0.0);
@@ -1348,6 +1373,7 @@ struct shapes_batch {
     free_step_buffers();
     dfree(world_body_off); dfree(body_world); dfree(vert_off); dfree(lx); dfree(ly);
     dfree(emin); dfree(emax);
+    dfree(pose_order);
     for (int k = 0; k < 10; ++k) {
       dfree(body[k]);
       dfree(body_stage[k]);

@@ -110,6 +110,8 @@ struct Dev {
   int32_t* slot_off;   /* [pair_cap+1] scanned */
   int32_t* slot_feat;  /* [2*pair_cap] fa | fb<<12 | flip<<24 */
   int32_t* np_perm;    /* [pair_cap] pairs in processing order, grouped by vertex-count class */
+  const int32_t* pose_order; /* [n_bodies] pose-kernel order: within chunks of 1024 bodies, grouped by vertex
+                                count, so that a warp's vertex loops have one length (null: index order) */
   int32_t* np_cls;     /* [2 * kNpClasses + 1] class counts, then offsets and cursors */
   double* slot_val;    /* [2*pair_cap*5] nx ny px py depth */
   uint64_t* c_key;     /* [contact_cap] packed world-local key */
@@ -368,9 +370,14 @@ __global__ void k_init_extents(Dev d) {
  * toTransform (Transform.hs:34-38, 73-77; MatrixTemplate.hs:47-67), afmul
  * (Linear.hs:217-220) per vertex, unitEdgeNormal (ConvexHull.hs:218-226) per
  * edge, then hullToAabb (Aabb.hs:81-84, 106-110) and its ordered keys.
- * One thread per body. */
+ * One thread per body, bodies taken in pose_order: the FP64 pipe charges a
+ * warp instruction in full whatever its active lanes, so a warp whose hulls
+ * have 3..8 vertices would run 8 iterations for all of them; grouped by vertex
+ * count, its loops have one length.  Each body still writes only its own
+ * outputs, so the order changes no result. */
 __global__ void k_integrate_pose(Dev d, double dt, int advance, const uint8_t* only = nullptr) {
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < d.n_bodies; t += gridDim.x * blockDim.x) {
+    const int g = d.pose_order ? d.pose_order[t] : t;
     if (only && !only[g]) continue; /* re-pose: this body's pose inputs did not change */
     if (d.active && !d.active[g]) { /* empty slot: left as it was, out of the broadphase */
       d.flags[g] = kFlagInactive;
