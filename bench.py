@@ -389,7 +389,7 @@ class Lanes:
 
 
 def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10, coloured=False, settle=0,
-                settle_iterations=None):
+                settle_iterations=None, collect=0):
     """Steps a fresh copy `settle` steps with the plain start, then `steps` steps
     with the residual flag: (mean over steps of the world-mean residual, mean
     over sampled steps of the world-mean largest depth, per-world max residual,
@@ -403,6 +403,8 @@ def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10
                                 coloured=coloured), settle)
     if net is not None:
         b.set_mlp(net)
+    if collect:
+        b.collect(collect)
     W = b.n_worlds
     res_sum, dep_sum, n_dep, predicted = 0.0, 0.0, 0, 0
     wres = np.zeros(W)
@@ -420,31 +422,68 @@ def quality_run(_lib, scene, stream, iterations, steps, net=None, depth_every=10
             dep_sum += float(d.mean())
             n_dep += 1
             np.maximum(wdep, d, out=wdep)
+    samples = b.samples() if collect else None
     b.close()
+    if collect:
+        return res_sum / steps, dep_sum / max(n_dep, 1), wres, wdep, predicted, samples
     return res_sum / steps, dep_sum / max(n_dep, 1), wres, wdep, predicted
 
 
+def train_source(args) -> str:
+    """Scene generator the network's samples come from: the timed workload's
+    own generator with held-out seeds (the learned and mixed workloads), else
+    the batched workload."""
+    if args.train_source != "auto":
+        return args.train_source
+    return "learned" if args.workload in ("learned", "mixed") else "batched"
+
+
 def train_network(_lib, stream, args, rank):
-    """Samples of new contacts from plain runs of the batched workload (a
-    different seed from every timed scene), then Adam on the tensor cores."""
+    """Samples of new contacts (features before the solve, final Lagrangians
+    after plain sweeps) from plain runs of a scene with seeds no timed scene
+    uses, then Adam on the tensor cores; 10 % of the samples are held out."""
     t0 = time.time()
-    sc = make_scene("batched", seed_offset=100 + rank, worlds=args.train_worlds)
+    src = train_source(args)
+    sc = make_scene(src, seed_offset=100 + rank, worlds=args.train_worlds)
     c = sc["config"]
-    cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], PLAIN_ITERATIONS["batched"])
+    cfg = _lib.make_config(c["dt"], c["baumgarte"], c["slop"], c["accel"], PLAIN_ITERATIONS[src])
     b = new_batch(_lib, sc, stream)
     b.collect(args.train_samples)
     b.step(cfg, args.train_steps)
     feat, tgt = b.samples()
     b.close()
     t1 = time.time()
+    perm = np.random.default_rng(7).permutation(len(feat))
+    n_ho = len(feat) // 10
+    ho, tr = perm[:n_ho], perm[n_ho:]
     net = _lib.Mlp(seed=1)
-    net.fit_normalization(feat, tgt)
-    losses = net.train(feat, tgt, epochs=args.train_epochs, batch=4096, lr=2e-3, seed=1)
+    net.fit_normalization(feat[tr], tgt[tr])
+    losses = net.train(feat[tr], tgt[tr], epochs=args.train_epochs, batch=4096, lr=2e-3, seed=1)
+    _, ho_loss = net.gradient(feat[ho][: 1 << 20], tgt[ho][: 1 << 20])
     torch_sync()
-    return net, {"samples": int(len(feat)), "source": f"plain runs of the batched workload (seed offset {100 + rank}, "
-                 f"{args.train_worlds} worlds x {args.train_steps} steps)", "epochs": args.train_epochs,
-                 "batch": 4096, "lr": 2e-3, "first_loss": float(losses[0]), "final_loss": float(losses[-1]),
+    return net, {"samples": int(len(feat)), "held_out": int(n_ho),
+                 "source": f"plain runs of the {src} workload's generator (seed offset {100 + rank}, "
+                           f"{args.train_worlds} worlds x {args.train_steps} steps from the initial state, "
+                           f"{PLAIN_ITERATIONS[src]} sweeps)",
+                 "epochs": args.train_epochs, "batch": 4096, "lr": 2e-3,
+                 "loss_curve": [float(x) for x in np.asarray(losses)[:: max(1, len(losses) // 20)]],
+                 "first_loss": float(losses[0]), "final_loss": float(losses[-1]), "held_out_loss": float(ho_loss),
                  "collect_s": t1 - t0, "train_s": time.time() - t1}
+
+
+def prediction_stats(net, feat, tgt) -> dict:
+    """The network on new contacts of a window of the timed scene: how often the
+    normal prediction is clamped to 0, mean predicted vs converged impulses, and
+    the fraction of the targets' variance the predictions explain."""
+    if len(feat) == 0:
+        return {"contacts": 0}
+    pred = net.forward(feat)
+    out = {"contacts": int(len(feat)), "clamped_to_zero": float((pred[:, 0] <= 0).mean()),
+           "pred_normal_mean": float(pred[:, 0].mean()), "target_normal_mean": float(tgt[:, 0].mean())}
+    for k, name in ((0, "normal"), (1, "friction")):
+        var = float(tgt[:, k].var())
+        out[f"r2_{name}"] = 1.0 - float(((pred[:, k] - tgt[:, k]) ** 2).mean()) / var if var > 0 else None
+    return out
 
 
 def torch_sync():
@@ -472,25 +511,33 @@ def run_ours(args, rank, world, local):
     run_it, run_learned = plain_it, False
     if args.workload == "learned":
         net, train_info = train_network(_lib, stream, args, rank)
-        qs = args.quality_steps
-        kw = {"settle": args.settle, "settle_iterations": plain_it}
-        p_res, p_dep, p_wres, p_wdep, _ = quality_run(_lib, scene, stream, plain_it, qs, **kw)
-        sweep = []
-        for it in range(1, plain_it + 1):
-            l_res, l_dep, _, _, pred = quality_run(_lib, scene, stream, it, qs, net=net, **kw)
-            row = {"iterations": it, "learned_residual": l_res, "learned_depth": l_dep,
-                   "predicted_per_step": pred / qs}
-            if args.plain_sweep or it == plain_it:
-                q = (p_res, p_dep) if it == plain_it else quality_run(_lib, scene, stream, it, qs, **kw)[:2]
+        windows = {}
+        for wname, w_settle, w_steps in (("landing", args.landing_from, args.quality_steps),
+                                         ("settled", args.settle, args.quality_steps)):
+            kw = {"settle": w_settle, "settle_iterations": plain_it}
+            p_res, p_dep, w_wres, w_wdep, _, smp = quality_run(_lib, scene, stream, plain_it, w_steps, collect=1 << 21,
+                                                               **kw)
+            sweep = []
+            for it in range(1, plain_it + 1):
+                l_res, l_dep, _, _, pred = quality_run(_lib, scene, stream, it, w_steps, net=net, **kw)
+                row = {"iterations": it, "learned_residual": l_res, "learned_depth": l_dep,
+                       "predicted_per_step": pred / w_steps}
+                q = (p_res, p_dep) if it == plain_it else quality_run(_lib, scene, stream, it, w_steps, **kw)[:2]
                 row["plain_residual"], row["plain_depth"] = q
-            sweep.append(row)
-        matched = [r_["iterations"] for r_ in sweep
-                   if r_["learned_residual"] <= p_res and r_["learned_depth"] <= p_dep]
-        learned = {"training": train_info, "quality_steps": qs, "quality_after_settle_steps": args.settle,
-                   "plain": {"iterations": plain_it, "residual": p_res, "depth": p_dep},
-                   "sweep": sweep, "matched_iterations": min(matched) if matched else None,
-                   "judge": "per world: back to the plain start once its residual exceeds the plain run's "
-                            "largest residual of that world, or its largest depth the plain run's"}
+                sweep.append(row)
+            m_l = [r_["iterations"] for r_ in sweep if r_["learned_residual"] <= p_res and r_["learned_depth"] <= p_dep]
+            m_p = [r_["iterations"] for r_ in sweep if r_["plain_residual"] <= p_res and r_["plain_depth"] <= p_dep]
+            windows[wname] = {"steps": f"{w_settle + 1}-{w_settle + w_steps} from the initial state",
+                              "plain": {"iterations": plain_it, "residual": p_res, "depth": p_dep},
+                              "sweep": sweep, "matched_iterations": min(m_l) if m_l else None,
+                              "plain_matched_iterations": min(m_p) if m_p else None,
+                              "new_contact_predictions": prediction_stats(net, *smp)}
+            if wname == "settled":
+                p_wres, p_wdep, matched = w_wres, w_wdep, m_l
+        learned = {"training": train_info, "windows": windows,
+                   "matched_iterations": windows["settled"]["matched_iterations"],
+                   "judge": "per world: back to the plain start once its residual exceeds the plain run's largest "
+                            "residual of that world, or its largest depth the plain run's"}
         if matched:
             run_it, run_learned = min(matched), True
 
@@ -1004,7 +1051,6 @@ def main():
                     help="untimed steps (plain start) from the initial state before the warm-up, in both arms "
                          "(-1: the workload's default, 300 for the many-world scenes and the single world, 0 for "
                          "the container and contacts)")
-    ap.add_argument("--plain-sweep", action="store_true", help="also sweep the plain start over 1-8 sweeps")
     ap.add_argument("--coloured", action="store_true", help="large worlds: graph-coloured sweep")
     ap.add_argument("--lanes", type=int, default=0,
                     help="handles (one CUDA stream each) the worlds are sharded over and stepped together "
@@ -1013,10 +1059,15 @@ def main():
                     help="grid worlds search every body's 3x3 cells every frame (no fat-box pair lists)")
     ap.add_argument("--large-quality", action="store_true",
                     help="container: residual, depth and speed of ordered vs coloured, with and without the network")
-    ap.add_argument("--train-worlds", type=int, default=4096, help="worlds of the sample-collection run")
-    ap.add_argument("--train-steps", type=int, default=300, help="steps of the sample-collection run")
+    ap.add_argument("--train-source", choices=["auto", "batched", "learned"], default="auto",
+                    help="scene generator of the training samples (auto: the timed workload's own generator with "
+                         "held-out seeds for the learned and mixed workloads, else the batched workload)")
+    ap.add_argument("--train-worlds", type=int, default=2048, help="worlds of the sample-collection run")
+    ap.add_argument("--train-steps", type=int, default=400, help="steps of the sample-collection run")
+    ap.add_argument("--landing-from", type=int, default=50,
+                    help="first step of the landing window of the learned sweep (new contacts are numerous there)")
     ap.add_argument("--train-samples", type=int, default=2_000_000, help="at most this many training samples")
-    ap.add_argument("--train-epochs", type=int, default=10, help="Adam epochs over the samples")
+    ap.add_argument("--train-epochs", type=int, default=40, help="Adam epochs over the samples")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -391,7 +391,7 @@ int shapes_collide_noalloc(int32_t n_bodies, const double* pos_x, const double* 
  * entry.  Parameters: 9538 floats, W1[64][16] b1[64] W2[64][64] b2[64]
  * W3[64][64] b3[64] W4[2][64] b4[2] (row = output).  Normalisation: 36
  * floats, feature mean[16], feature 1/scale[16], target mean[2], target
- * scale[2]; the network sees (f - mean) / scale and predicts
+ * scale[2]; the network sees (f - mean) / scale clipped to [-8, 8] and predicts
  * (target - mean) / scale.  Features, in order: J_n.v, J_f.v, b_n, J_n M^-1
  * J_n^T, J_f M^-1 J_f^T, the isolated normal and friction updates, pair
  * friction, depth, normal x, normal y, one step of acceleration as a normal

@@ -59,10 +59,14 @@ def _mm(a, b):
     return (np.asarray(a, np.float64) @ np.asarray(b, np.float64)).astype(np.float32)
 
 
+CLIP = 8.0  # normalised inputs are clipped to [-CLIP, CLIP] (fmin/fmax: a NaN becomes the bound)
+
+
 def normalise_inputs(feat, norm):
     norm = np.asarray(norm, dtype=np.float32)
     f = np.asarray(feat, dtype=np.float32)
-    return bf16((f - norm[:N_IN]) * norm[N_IN:2 * N_IN])
+    x = (f - norm[:N_IN]) * norm[N_IN:2 * N_IN]
+    return bf16(np.fmin(np.fmax(x, np.float32(-CLIP)), np.float32(CLIP)))
 
 
 def forward(params, norm, feat):
@@ -114,6 +118,7 @@ def forward64(params, norm, feat):
     P = unpack(params, np.float64)
     norm = np.asarray(norm, np.float64)
     x = (np.asarray(feat, np.float64) - norm[:N_IN]) * norm[N_IN:2 * N_IN]
+    x = np.fmin(np.fmax(x, -CLIP), CLIP)
     z1 = x @ P["W1"].T + P["b1"]
     h1 = np.maximum(z1, 0)
     z2 = h1 @ P["W2"].T + P["b2"]

@@ -131,4 +131,88 @@ __device__ __forceinline__ double mul_rn_int(double a, double b) {
   return __dmul_rn(a, b);
 }
 
+/* a + b in binary64, round to nearest even, computed on the integer pipe
+ * (host and device: the same integer steps, so the host can check it against
+ * its own hardware addition).  Fast path: both operands normal with biased
+ * exponents in [64, 1982]; the result is then normal (an exact cancellation
+ * gives +0, as IEEE round-to-nearest does), and nothing overflows.
+ * Algorithm (the textbook one with guard bits and a sticky bit): order the
+ * operands by magnitude; significands with the implicit one, shifted left by
+ * 10 so that the leading one sits at bit 62 and 10 guard bits lie below the
+ * last place; the smaller is shifted right by the exponent difference with
+ * every bit shifted out ORed into bit 0 (sticky); add the significands for
+ * equal signs (a carry out of bit 62 shifts right by one, again keeping a
+ * sticky bit), subtract them otherwise (renormalising left by the leading
+ * zero count); keep 53 bits and round on the 10 bits below, ties to even.
+ * When a sticky bit was set, the sum is an odd number of guard units and the
+ * exact value lies within one unit of it, so it falls on the same side of the
+ * rounding midpoint (an even number of units) and never on it.  The rounding
+ * carry moves into the exponent field by integer addition.  Anything else
+ * (zeros, subnormals, extreme exponents, infinities, NaN) uses the hardware
+ * addition. */
+__host__ __device__ __forceinline__ double add_rn_int(double a, double b) {
+#if defined(__CUDA_ARCH__)
+  uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+#else
+  uint64_t ua, ub;
+  __builtin_memcpy(&ua, &a, 8);
+  __builtin_memcpy(&ub, &b, 8);
+#endif
+  uint64_t xa = ua & 0x7fffffffffffffffull, xb = ub & 0x7fffffffffffffffull;
+  const uint32_t ea0 = (uint32_t)(xa >> 52), eb0 = (uint32_t)(xb >> 52);
+  if (ea0 - 64u <= 1918u && eb0 - 64u <= 1918u) {
+    if (xa < xb) { /* |a| >= |b| from here on */
+      const uint64_t t = ua;
+      ua = ub;
+      ub = t;
+      const uint64_t tx = xa;
+      xa = xb;
+      xb = tx;
+    }
+    const uint32_t ea = (uint32_t)(xa >> 52), d = ea - (uint32_t)(xb >> 52);
+    const uint64_t ma = ((xa & 0x000fffffffffffffull) | 0x0010000000000000ull) << 10;
+    uint64_t mb = ((xb & 0x000fffffffffffffull) | 0x0010000000000000ull) << 10;
+    if (d >= 63u) {
+      mb = 1ull; /* only the sticky bit is left */
+    } else if (d) {
+      const uint64_t sticky = (mb << (64u - d)) != 0ull ? 1ull : 0ull;
+      mb = (mb >> d) | sticky;
+    }
+    uint64_t sm;
+    int64_t e = (int64_t)ea;
+    if (((ua ^ ub) >> 63) == 0ull) {
+      sm = ma + mb;
+      if (sm >> 63) {
+        sm = (sm >> 1) | (sm & 1ull);
+        e += 1;
+      }
+    } else {
+      sm = ma - mb;
+      if (sm == 0ull) return 0.0;
+#if defined(__CUDA_ARCH__)
+      const int lz = __clzll((long long)sm) - 1;
+#else
+      const int lz = __builtin_clzll(sm) - 1;
+#endif
+      sm <<= lz;
+      e -= lz;
+    }
+    const uint64_t m = sm >> 10, rem = sm & 0x3ffull;
+    const uint64_t up = (rem > 0x200ull || (rem == 0x200ull && (m & 1ull))) ? 1ull : 0ull;
+    const uint64_t r = ((((uint64_t)(e - 1)) << 52) + m + up) | (ua & 0x8000000000000000ull);
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)r);
+#else
+    double out;
+    __builtin_memcpy(&out, &r, 8);
+    return out;
+#endif
+  }
+#if defined(__CUDA_ARCH__)
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+
 }  // namespace shapes

@@ -51,7 +51,7 @@ extern "C" int shapes_probe_fp64(double* lane_ops_per_s) {
 
 namespace {
 
-__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+__host__ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   /* splitmix64 finaliser (Steele, Lea, Flood 2014) */
   x += 0x9e3779b97f4a7c15ull;
   x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -332,4 +332,184 @@ extern "C" int shapes_probe_tc05_gemm(const float* A, const float* B, int N, int
   cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(dErr);
   if (e != cudaSuccess) return -5;
   return herr ? -6 : 0;
+}
+
+/* ---- add_rn_int: checks against the hardware addition and throughput ---- */
+
+__host__ __device__ __forceinline__ double bits_to_double(unsigned long long u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double d;
+  __builtin_memcpy(&d, &u, 8);
+  return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ unsigned long long double_to_bits(double d) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long u;
+  __builtin_memcpy(&u, &d, 8);
+  return u;
+#endif
+}
+
+/* Operand classes for add_rn_int: random exponents over the fast range and
+ * beyond it, close exponents, near and exact cancellation, shifts past the
+ * significand, neighbours of the rounding midpoint, powers of two, all-ones
+ * significands, and zeros, subnormals, infinities and NaN. */
+__host__ __device__ void add_operands(unsigned long long k, unsigned long long seed, double* a, double* b) {
+  const unsigned long long r0 = mix64(k ^ seed), r1 = mix64(r0), r2 = mix64(r1), r3 = mix64(r2);
+  const int cls = (int)(r3 % 10);
+  long long ea = 40 + (long long)(r1 % 1970), eb;
+  unsigned long long ma = r0, mb = r2 >> 3;
+  switch (cls) {
+    case 0: eb = 40 + (long long)(r2 % 1970); break;
+    case 1: eb = ea + (long long)(r2 % 7) - 3; break;
+    case 2: eb = ea; mb = ma ^ (r2 & 0xffull); break;
+    case 3: eb = ea - (long long)(r2 % 70); break;
+    case 4: eb = ea - 53 - (long long)(r2 % 3); ma &= ~0xfffull; break;
+    case 5: eb = ea - (long long)(r2 % 60); mb = 1ull << (r2 % 52); break;
+    case 6: eb = ea; mb = ma; break;
+    case 7: eb = ea - 1 - (long long)(r2 % 5); ma = 0xfffffffffffffull; mb = 0xfffffffffffffull; break;
+    default: eb = 40 + (long long)(r2 % 1970); break;
+  }
+  if (eb < 1) eb = 1;
+  if (eb > 2046) eb = 2046;
+  *a = bits_to_double(((r0 >> 63) << 63) | ((unsigned long long)ea << 52) | (ma & 0xfffffffffffffull));
+  *b = bits_to_double(((r1 >> 63) << 63) | ((unsigned long long)eb << 52) | (mb & 0xfffffffffffffull));
+  if (cls >= 8) {
+    const int pick = (int)((r3 >> 8) % 6);
+    const unsigned long long sp = pick == 0 ? 0x7ff0000000000000ull
+                                : pick == 1 ? 0xfff0000000000000ull
+                                : pick == 2 ? 0x7ff8000000000000ull
+                                : pick == 3 ? ((r0 >> 63) << 63) | (ma & 0xfffffffffffffull) /* subnormal */
+                                : pick == 4 ? ((r3 & 16) ? 0x8000000000000000ull : 0ull)
+                                            : 0x7fefffffffffffffull;
+    if (r3 & 32) *a = bits_to_double(sp); else *b = bits_to_double(sp);
+  }
+  if (r3 & 0x100) {
+    const double t = *a;
+    *a = *b;
+    *b = t;
+  }
+}
+
+__global__ void k_add_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                            double* first) {
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    double a, b;
+    add_operands(k, seed, &a, &b);
+    const double q = shapes::add_rn_int(a, b);
+    const double ref = __dadd_rn(a, b);
+    const bool same = __double_as_longlong(q) == __double_as_longlong(ref) || (q != q && ref != ref);
+    if (!same && atomicAdd(bad, 1ull) == 0) {
+      first[0] = a;
+      first[1] = b;
+    }
+  }
+}
+
+extern "C" int shapes_probe_add_check(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                                      double* first_ab) {
+  unsigned long long* d_bad = nullptr;
+  double* d_first = nullptr;
+  if (cudaMalloc(&d_bad, sizeof(unsigned long long)) != cudaSuccess) return -5;
+  if (cudaMalloc(&d_first, 2 * sizeof(double)) != cudaSuccess) return -5;
+  cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  cudaMemset(d_first, 0, 2 * sizeof(double));
+  k_add_check<<<152 * 16, 256>>>(n, seed, d_bad, d_first);
+  cudaMemcpy(bad, d_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaMemcpy(first_ab, d_first, 2 * sizeof(double), cudaMemcpyDeviceToHost);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  return err == cudaSuccess ? 0 : -5;
+}
+
+/* The same integer steps on the host against the host's own addition (no
+ * GPU needed): n pairs from the same operand classes. */
+extern "C" int shapes_probe_add_check_host(unsigned long long n, unsigned long long seed, unsigned long long* bad,
+                                           double* first_ab) {
+  unsigned long long nb = 0;
+  for (unsigned long long k = 0; k < n; ++k) {
+    double a, b;
+    add_operands(k, seed, &a, &b);
+    const double q = shapes::add_rn_int(a, b);
+    volatile double va = a, vb = b;
+    const double ref = va + vb;
+    const bool same = double_to_bits(q) == double_to_bits(ref) || (q != q && ref != ref);
+    if (!same && nb++ == 0) {
+      first_ab[0] = a;
+      first_ab[1] = b;
+    }
+  }
+  *bad = nb;
+  return 0;
+}
+
+/* Sums per second (whole GPU) of independent chains: NF on the FP64 pipe and
+ * NI through add_rn_int in the same warps, and the same split for products
+ * (mul_rn_int).  out6: adds {FP64 only, integer only, 4 + 4 mixed}, products
+ * {FP64 only, integer only, 4 + 4 mixed}. */
+template <int NF, int NI, bool ADD>
+__global__ void k_split_chains(double* out, int iters) {
+  double f[NF > 0 ? NF : 1], g[NI > 0 ? NI : 1];
+#pragma unroll
+  for (int k = 0; k < NF; ++k) f[k] = 1.0 + threadIdx.x * 1e-6 + 0.1 * k;
+#pragma unroll
+  for (int k = 0; k < NI; ++k) g[k] = 1.25 + threadIdx.x * 1e-6 + 0.1 * k;
+  const double c = ADD ? 1.0000000001 : 0.99999999999;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) f[k] = ADD ? __dadd_rn(f[k], c) : __dmul_rn(f[k], c);
+#pragma unroll
+    for (int k = 0; k < NI; ++k) g[k] = ADD ? shapes::add_rn_int(g[k], c) : shapes::mul_rn_int(g[k], c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < NF; ++k) s += f[k];
+#pragma unroll
+  for (int k = 0; k < NI; ++k) s += g[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <int NF, int NI, bool ADD>
+static double split_rate(double* d, int blocks, int threads) {
+  const int iters = 2000;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float ms = 0.f;
+  for (int rep = 0; rep < 2; ++rep) {
+    cudaEventRecord(e0);
+    k_split_chains<NF, NI, ADD><<<blocks, threads>>>(d, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms > 0.f ? (double)blocks * threads * iters * (NF + NI) / (ms * 1e-3) : 0.0;
+}
+
+extern "C" int shapes_probe_split_rates(double* out6) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -5;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -5;
+  const int threads = 256, blocks = sms * 4;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * threads * blocks) != cudaSuccess) return -5;
+  out6[0] = split_rate<8, 0, true>(d, blocks, threads);
+  out6[1] = split_rate<0, 8, true>(d, blocks, threads);
+  out6[2] = split_rate<4, 4, true>(d, blocks, threads);
+  out6[3] = split_rate<8, 0, false>(d, blocks, threads);
+  out6[4] = split_rate<0, 8, false>(d, blocks, threads);
+  out6[5] = split_rate<4, 4, false>(d, blocks, threads);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(d);
+  return err == cudaSuccess ? 0 : -5;
 }

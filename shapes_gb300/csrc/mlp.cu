@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(128) k_mlp_predict(PredictArgs a) {
 #pragma unroll
     for (int k = 0; k < kIn; ++k) {
       const float f = valid ? a.feat[(size_t)row * kIn + k] : 0.f;
-      x[k] = valid ? (f - snorm[k]) * snorm[kIn + k] : 0.f;
+      x[k] = valid ? fminf(fmaxf((f - snorm[k]) * snorm[kIn + k], -kClip), kClip) : 0.f;
     }
     const float mu = valid ? a.feat[(size_t)row * kIn + kFMu] : 0.f;
     *reinterpret_cast<uint4*>(sm + kPredX + kmaj(t, 0, kIn)) = tc05::pack8(x);
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) k_mlp_train(TrainArgs a) {
   float x[kIn];
 #pragma unroll
   for (int k = 0; k < kIn; ++k)
-    x[k] = valid ? (a.feat[(size_t)smp * kIn + k] - snorm[k]) * snorm[kIn + k] : 0.f;
+    x[k] = valid ? fminf(fmaxf((a.feat[(size_t)smp * kIn + k] - snorm[k]) * snorm[kIn + k], -kClip), kClip) : 0.f;
   *reinterpret_cast<uint4*>(sm + kTrX + kmaj(t, 0, kIn)) = tc05::pack8(x);
   *reinterpret_cast<uint4*>(sm + kTrX + kmaj(t, 8, kIn)) = tc05::pack8(x + 8);
 #pragma unroll

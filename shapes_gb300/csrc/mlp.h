@@ -19,6 +19,10 @@ constexpr int oW1 = 0, oB1 = 1024, oW2 = 1088, oB2 = 5184, oW3 = 5248, oB3 = 934
 constexpr int kParams = 9538;
 /* normalisation: feature mean[16], feature 1/scale[16], output mean[2], output scale[2] */
 constexpr int kNorm = 36;
+/* Normalised inputs are clipped to [-kClip, kClip]: a contact whose features
+ * lie far outside the training data (another friction range, another scene)
+ * then cannot drive the network arbitrarily far. */
+constexpr float kClip = 8.f;
 constexpr int kTile = 128;
 
 /* Feature indices (raw, before normalisation). */

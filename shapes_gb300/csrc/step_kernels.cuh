@@ -1720,6 +1720,34 @@ __device__ __forceinline__ void apply_impulse(const double j[6], double l, doubl
   v[5] = v[5] + (j[5] * l) * m[5];
 }
 
+/* Where the impulse application's products run in sweep updates (every
+ * variant gives the same bits: mul_rn_int is the correctly rounded product):
+ * 0 the FP64 pipe; 1 all ten products of an impulse on the integer pipe;
+ * 2 the six products by the inverse masses; 3 the four products J * lambda. */
+#ifndef SHAPES_SOLVER_INT_MUL
+#define SHAPES_SOLVER_INT_MUL 0
+#endif
+
+template <int MODE>
+__device__ __forceinline__ double imul_a(double a, double b) { /* J * lambda */
+  return (MODE == 1 || MODE == 3) ? mul_rn_int(a, b) : a * b;
+}
+template <int MODE>
+__device__ __forceinline__ double imul_m(double a, double b) { /* (J * lambda) * invMass */
+  return (MODE == 1 || MODE == 2) ? mul_rn_int(a, b) : a * b;
+}
+
+template <int MODE>
+__device__ __forceinline__ void apply_impulse_split(const double j[6], double l, double v[6], const double m[6]) {
+  const double p3 = imul_a<MODE>(j[3], l), p4 = imul_a<MODE>(j[4], l);
+  v[0] = v[0] + imul_m<MODE>(-p3, m[0]);
+  v[1] = v[1] + imul_m<MODE>(-p4, m[1]);
+  v[2] = v[2] + imul_m<MODE>(imul_a<MODE>(j[2], l), m[2]);
+  v[3] = v[3] + imul_m<MODE>(p3, m[3]);
+  v[4] = v[4] + imul_m<MODE>(p4, m[4]);
+  v[5] = v[5] + imul_m<MODE>(imul_a<MODE>(j[5], l), m[5]);
+}
+
 /* J . v as a left fold (Shapes/Linear/Template.hs:108-110). */
 __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
   double s = j[0] * v[0];
@@ -1825,8 +1853,13 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item, int ga, 
     lf_apply = acc2 - cf;
     *lam2 = make_double2(ln_cache, acc2);
   }
-  apply_impulse(j_n, ln_apply, v, m);
-  apply_impulse(j_f, lf_apply, v, m);
+  if (SHAPES_SOLVER_INT_MUL == 0 || (item & kWarmBit)) {
+    apply_impulse(j_n, ln_apply, v, m);
+    apply_impulse(j_f, lf_apply, v, m);
+  } else {
+    apply_impulse_split<SHAPES_SOLVER_INT_MUL>(j_n, ln_apply, v, m);
+    apply_impulse_split<SHAPES_SOLVER_INT_MUL>(j_f, lf_apply, v, m);
+  }
   if (info & kInfoDynA) vs.store(ga, delta, v[0], v[1], v[2]);
   if (info & kInfoDynB) vs.store(gb, delta, v[3], v[4], v[5]);
 }

@@ -25,6 +25,8 @@ def probe(built):
                                            ctypes.POINTER(ctypes.c_ulonglong)]
     lib.shapes_probe_mul_check.argtypes = lib.shapes_probe_div_check.argtypes
     lib.shapes_probe_mul_rate.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    lib.shapes_probe_add_check.argtypes = lib.shapes_probe_div_check.argtypes
+    lib.shapes_probe_split_rates.argtypes = [ctypes.POINTER(ctypes.c_double)]
     return lib
 
 
@@ -62,3 +64,21 @@ def test_integer_pipe_multiply_rate(probe):
     assert probe.shapes_probe_mul_rate(rates) == 0
     assert rates[0] > 0 and rates[1] > 0
     print(f"multiplies/s: hardware {rates[0]:.3e}, integer pipe {rates[1]:.3e}")
+
+
+@pytest.mark.parametrize("seed", [31, 32, 33, 34])
+def test_integer_pipe_add_matches_hardware(probe, seed):
+    bad = ctypes.c_ulonglong()
+    first = (ctypes.c_double * 2)()
+    assert probe.shapes_probe_add_check(1 << 28, seed, ctypes.byref(bad), first) == 0
+    assert bad.value == 0, f"{bad.value} mismatches, first a={first[0]!r} b={first[1]!r}"
+
+
+def test_split_rates(probe):
+    """Sums and products per second with chains on the FP64 pipe, on the
+    integer pipe (add_rn_int / mul_rn_int) and split 4 + 4 in the same warps."""
+    r = (ctypes.c_double * 6)()
+    assert probe.shapes_probe_split_rates(r) == 0
+    assert all(x > 0 for x in r)
+    print(f"adds/s: FP64 {r[0]:.3e}, integer {r[1]:.3e}, split {r[2]:.3e}; "
+          f"products/s: FP64 {r[3]:.3e}, integer {r[4]:.3e}, split {r[5]:.3e}")
