@@ -147,6 +147,11 @@ struct shapes_batch {
   double* slot_val = nullptr;
   int32_t* np_perm = nullptr;
   int32_t* pose_order = nullptr; /* [N] bodies grouped by vertex count within chunks of 1024 */
+  int32_t* ext_chunk = nullptr;      /* extent reduction: chunk body ranges, per-world chunk offsets, partials */
+  int32_t* ext_chunk_off = nullptr;
+  double* ext_part_sum = nullptr;
+  int32_t* ext_part_cnt = nullptr;
+  int32_t n_ext_chunks = 0;
   int32_t* np_cls = nullptr; /* [2 * kNpClasses + 1] */
   int32_t* world_pair_off = nullptr;
   /* contacts: ping-pong between two buffers, the cache of step s is the
@@ -379,6 +384,11 @@ struct shapes_batch {
     d.body_world = body_world;
     d.vert_off = vert_off;
     d.pose_order = pose_order;
+    d.ext_chunk = ext_chunk;
+    d.ext_chunk_off = ext_chunk_off;
+    d.ext_part_sum = ext_part_sum;
+    d.ext_part_cnt = ext_part_cnt;
+    d.n_ext_chunks = n_ext_chunks;
     d.lx = lx;
     d.ly = ly;
     d.radius = radius;
@@ -864,6 +874,28 @@ struct shapes_batch {
     ck(cudaMemcpy(grid_T, T.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
     ck(cudaMemcpy(grid_base, base.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload grid");
     ck(cudaMemset(row_mode, 0, N), "memset");
+    {
+      /* chunks of at most 4096 bodies, never crossing a world (empty worlds have none) */
+      dfree(ext_chunk); dfree(ext_chunk_off); dfree(ext_part_sum); dfree(ext_part_cnt);
+      std::vector<int32_t> ranges, choff(W + 1, 0);
+      for (int w = 0; w < W; ++w) {
+        choff[w] = (int32_t)(ranges.size() / 2);
+        for (int32_t b = h_world_body_off[w]; b < h_world_body_off[w + 1]; b += 4096) {
+          ranges.push_back(b);
+          ranges.push_back(std::min<int32_t>(b + 4096, h_world_body_off[w + 1]));
+        }
+      }
+      n_ext_chunks = (int32_t)(ranges.size() / 2);
+      choff[W] = n_ext_chunks;
+      ext_chunk = dalloc<int32_t>(std::max<size_t>(ranges.size(), 1), "cudaMalloc grid");
+      ext_chunk_off = dalloc<int32_t>((size_t)W + 1, "cudaMalloc grid");
+      ext_part_sum = dalloc<double>(std::max<int32_t>(n_ext_chunks, 1), "cudaMalloc grid");
+      ext_part_cnt = dalloc<int32_t>(std::max<int32_t>(n_ext_chunks, 1), "cudaMalloc grid");
+      if (n_ext_chunks)
+        ck(cudaMemcpy(ext_chunk, ranges.data(), sizeof(int32_t) * ranges.size(), cudaMemcpyHostToDevice),
+           "upload grid");
+      ck(cudaMemcpy(ext_chunk_off, choff.data(), sizeof(int32_t) * (W + 1), cudaMemcpyHostToDevice), "upload grid");
+    }
     setup_incremental();
   }
   int32_t smem_last_cap = 0; /* bodies whose last level fits the solver's shared memory */
@@ -906,9 +938,10 @@ struct shapes_batch {
     ck(cudaMemsetAsync(counters + shapes::kCntGroupAlloc, 0, sizeof(unsigned long long), stream), "memset");
     const bool inc = any_grid && d.nbr != nullptr;
     if (inc) {
-      stage(0, 6, [&]() {
+      stage(0, 7, [&]() {
         ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
-        shapes::k_inc_stats<<<W, 256, 0, stream>>>(d);
+        if (n_ext_chunks) shapes::k_extent_parts<<<n_ext_chunks, 256, 0, stream>>>(d, 1);
+        shapes::k_inc_stats<<<grid_for(W, 128), 128, 0, stream>>>(d);
         shapes::k_inc_mark<<<grid_for(N, 256), 256, 0, stream>>>(d);
         shapes::k_inc_decide<<<grid_for(W, 128), 128, 0, stream>>>(d);
         shapes::k_inc_remove<<<grid_for(N, 128), 128, 0, stream>>>(d);
@@ -920,9 +953,10 @@ struct shapes_batch {
         shapes::k_inc_query<<<grid_for(N, 128), 128, 0, stream>>>(d);
       });
     } else if (any_grid) {
-      stage(0, 3, [&]() {
+      stage(0, 4, [&]() {
         ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
-        shapes::k_grid_stats<<<W, 256, 0, stream>>>(d);
+        if (n_ext_chunks) shapes::k_extent_parts<<<n_ext_chunks, 256, 0, stream>>>(d, 0);
+        shapes::k_grid_stats<<<grid_for(W, 128), 128, 0, stream>>>(d);
         shapes::k_grid_bin<<<grid_for(N, 256), 256, 0, stream>>>(d);
       });
       scan(bucket_cnt, n_buckets, nullptr, bucket_off);
@@ -1383,6 +1417,7 @@ struct shapes_batch {
     dfree(row_cnt); dfree(row_off); dfree(world_pair_off);
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
+    dfree(ext_chunk); dfree(ext_chunk_off); dfree(ext_part_sum); dfree(ext_part_cnt);
     free_incremental();
     dfree(radius);
     dfree(metric_part);

@@ -110,6 +110,11 @@ struct Dev {
   int32_t* slot_off;   /* [pair_cap+1] scanned */
   int32_t* slot_feat;  /* [2*pair_cap] fa | fb<<12 | flip<<24 */
   int32_t* np_perm;    /* [pair_cap] pairs in processing order, grouped by vertex-count class */
+  const int32_t* ext_chunk;     /* [2 * n_ext_chunks] body range [b0, b1) of each extent-reduction chunk */
+  const int32_t* ext_chunk_off; /* [n_worlds + 1] each world's chunks */
+  double* ext_part_sum;         /* [n_ext_chunks] chunk sums of box extents */
+  int32_t* ext_part_cnt;        /* [n_ext_chunks] chunk counts */
+  int32_t n_ext_chunks;
   const int32_t* pose_order; /* [n_bodies] pose-kernel order: within chunks of 1024 bodies, grouped by vertex
                                 count, so that a warp's vertex loops have one length (null: index order) */
   int32_t* np_cls;     /* [2 * kNpClasses + 1] class counts, then offsets and cursors */
@@ -599,12 +604,21 @@ __device__ __forceinline__ uint32_t cell_bucket(int cx, int cy, int T) {
 }
 
 /* One CTA per world: mean of max(width, height) over finite boxes -> 1/s. */
-__global__ void k_grid_stats(Dev d) {
+/* Mean box extent of each grid world, which sets its cell size (2x the mean).
+ * The cell size only decides how fast the grid finds the pairs, never which
+ * pairs it finds (any positive size gives the pairs of culledKeys), so the sum
+ * may be split: one block per chunk of at most 4096 bodies of one world
+ * (k_extent_parts), then one thread per world adds its chunks in order
+ * (deterministic; a world of one chunk sums exactly as one block would).  A
+ * single large world thus spreads over the GPU instead of one SM. */
+__global__ void k_extent_parts(Dev d, int inc) {
   __shared__ double s_sum[32];
   __shared__ int s_cnt[32];
-  const int wld = blockIdx.x;
-  if (d.grid_T[wld] == 0) return;
-  const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
+  const int k = blockIdx.x;
+  if (k >= d.n_ext_chunks) return;
+  const int b0 = d.ext_chunk[2 * k], b1 = d.ext_chunk[2 * k + 1];
+  const int wld = d.body_world[b0];
+  if (d.grid_T[wld] == 0 || (inc && d.inc_state[wld] != 0)) return;
   double sum = 0.0;
   int cnt = 0;
   for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
@@ -628,16 +642,36 @@ __global__ void k_grid_stats(Dev d) {
   if (threadIdx.x == 0) {
     double t = 0.0;
     int c = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      t += s_sum[k];
-      c += s_cnt[k];
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      t += s_sum[q];
+      c += s_cnt[q];
     }
-    const double s = c > 0 ? 2.0 * t / c : 0.0;
-    const double inv = (s > 0.0 && small_mag(s) && small_mag(1.0 / s)) ? 1.0 / s : 0.0;
-    d.grid_inv_s[wld] = inv;
-    d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
-    d.large_cnt[wld] = 0;
+    d.ext_part_sum[k] = t;
+    d.ext_part_cnt[k] = c;
   }
+}
+
+/* Twice the mean extent over a world's chunks, added in chunk order. */
+__device__ __forceinline__ double world_cell_size(const Dev& d, int wld) {
+  double t = 0.0;
+  int c = 0;
+  for (int k = d.ext_chunk_off[wld]; k < d.ext_chunk_off[wld + 1]; ++k) {
+    t += d.ext_part_sum[k];
+    c += d.ext_part_cnt[k];
+  }
+  return c > 0 ? 2.0 * t / c : 0.0;
+}
+
+/* One thread per world: cell size, its reciprocal and the size limit of a
+ * grid body. */
+__global__ void k_grid_stats(Dev d) {
+  const int wld = blockIdx.x * blockDim.x + threadIdx.x;
+  if (wld >= d.n_worlds || d.grid_T[wld] == 0) return;
+  const double s = world_cell_size(d, wld);
+  const double inv = (s > 0.0 && small_mag(s) && small_mag(1.0 / s)) ? 1.0 / s : 0.0;
+  d.grid_inv_s[wld] = inv;
+  d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
+  d.large_cnt[wld] = 0;
 }
 
 /* One thread per body: grid bodies get a cell and a bucket count, the rest go
@@ -821,53 +855,20 @@ __device__ __forceinline__ bool fat_box(const Dev& d, int g, int wld, double fb[
  * mean extent (as k_grid_stats) and the margin s/32; every world clears its
  * large list and moved count. */
 __global__ void k_inc_stats(Dev d) {
-  __shared__ double s_sum[32];
-  __shared__ int s_cnt[32];
-  const int wld = blockIdx.x;
-  if (d.grid_T[wld] == 0) return;
+  const int wld = blockIdx.x * blockDim.x + threadIdx.x;
+  if (wld >= d.n_worlds || d.grid_T[wld] == 0) return;
   if (d.inc_state[wld] != 0) {
-    if (threadIdx.x == 0) {
-      d.large_cnt[wld] = 0;
-      d.inc_moved[wld] = 0;
-    }
-    return;
-  }
-  const int b0 = d.world_body_off[wld], b1 = d.world_body_off[wld + 1];
-  double sum = 0.0;
-  int cnt = 0;
-  for (int g = b0 + threadIdx.x; g < b1; g += blockDim.x) {
-    const double w = d.box[4 * g + 1] - d.box[4 * g + 0];
-    const double h = d.box[4 * g + 3] - d.box[4 * g + 2];
-    const double e = w > h ? w : h;
-    if (small_mag(e)) {
-      sum += e;
-      ++cnt;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s_sum[threadIdx.x >> 5] = sum;
-    s_cnt[threadIdx.x >> 5] = cnt;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    int c = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      t += s_sum[k];
-      c += s_cnt[k];
-    }
-    const double sz = c > 0 ? 2.0 * t / c : 0.0;
-    const double inv = (sz > 0.0 && small_mag(sz) && small_mag(1.0 / sz)) ? 1.0 / sz : 0.0;
-    d.grid_inv_s[wld] = inv;
-    d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
-    d.inc_margin[wld] = inv > 0.0 ? 0.03125 / inv : 0.0;
     d.large_cnt[wld] = 0;
     d.inc_moved[wld] = 0;
+    return;
   }
+  const double sz = world_cell_size(d, wld);
+  const double inv = (sz > 0.0 && small_mag(sz) && small_mag(1.0 / sz)) ? 1.0 / sz : 0.0;
+  d.grid_inv_s[wld] = inv;
+  d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
+  d.inc_margin[wld] = inv > 0.0 ? 0.03125 / inv : 0.0;
+  d.large_cnt[wld] = 0;
+  d.inc_moved[wld] = 0;
 }
 
 /* One thread per body of a grid world: moved or not, and the large list. */
@@ -1720,34 +1721,6 @@ __device__ __forceinline__ void apply_impulse(const double j[6], double l, doubl
   v[5] = v[5] + (j[5] * l) * m[5];
 }
 
-/* Where the impulse application's products run in sweep updates (every
- * variant gives the same bits: mul_rn_int is the correctly rounded product):
- * 0 the FP64 pipe; 1 all ten products of an impulse on the integer pipe;
- * 2 the six products by the inverse masses; 3 the four products J * lambda. */
-#ifndef SHAPES_SOLVER_INT_MUL
-#define SHAPES_SOLVER_INT_MUL 0
-#endif
-
-template <int MODE>
-__device__ __forceinline__ double imul_a(double a, double b) { /* J * lambda */
-  return (MODE == 1 || MODE == 3) ? mul_rn_int(a, b) : a * b;
-}
-template <int MODE>
-__device__ __forceinline__ double imul_m(double a, double b) { /* (J * lambda) * invMass */
-  return (MODE == 1 || MODE == 2) ? mul_rn_int(a, b) : a * b;
-}
-
-template <int MODE>
-__device__ __forceinline__ void apply_impulse_split(const double j[6], double l, double v[6], const double m[6]) {
-  const double p3 = imul_a<MODE>(j[3], l), p4 = imul_a<MODE>(j[4], l);
-  v[0] = v[0] + imul_m<MODE>(-p3, m[0]);
-  v[1] = v[1] + imul_m<MODE>(-p4, m[1]);
-  v[2] = v[2] + imul_m<MODE>(imul_a<MODE>(j[2], l), m[2]);
-  v[3] = v[3] + imul_m<MODE>(p3, m[3]);
-  v[4] = v[4] + imul_m<MODE>(p4, m[4]);
-  v[5] = v[5] + imul_m<MODE>(imul_a<MODE>(j[5], l), m[5]);
-}
-
 /* J . v as a left fold (Shapes/Linear/Template.hs:108-110). */
 __device__ __forceinline__ double dot6(const double j[6], const double v[6]) {
   double s = j[0] * v[0];
@@ -1853,13 +1826,8 @@ __device__ __forceinline__ void solve_item(const Dev& d, uint32_t item, int ga, 
     lf_apply = acc2 - cf;
     *lam2 = make_double2(ln_cache, acc2);
   }
-  if (SHAPES_SOLVER_INT_MUL == 0 || (item & kWarmBit)) {
-    apply_impulse(j_n, ln_apply, v, m);
-    apply_impulse(j_f, lf_apply, v, m);
-  } else {
-    apply_impulse_split<SHAPES_SOLVER_INT_MUL>(j_n, ln_apply, v, m);
-    apply_impulse_split<SHAPES_SOLVER_INT_MUL>(j_f, lf_apply, v, m);
-  }
+  apply_impulse(j_n, ln_apply, v, m);
+  apply_impulse(j_f, lf_apply, v, m);
   if (info & kInfoDynA) vs.store(ga, delta, v[0], v[1], v[2]);
   if (info & kInfoDynB) vs.store(gb, delta, v[3], v[4], v[5]);
 }
