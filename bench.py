@@ -313,14 +313,21 @@ def run_reference(args, rank, world):
 
 
 INCREMENTAL_PAIRS = True  # --no-incremental turns the fat-box pair lists off
+SWEEP_PRUNE = 0  # --sweep-prune N: grid worlds of N bodies or more pair by sweep and prune (incremental off)
+
+
+def broadphase_setup(b):
+    if not INCREMENTAL_PAIRS:
+        b.set_incremental(False)
+    if SWEEP_PRUNE:
+        b.set_sweep_prune(SWEEP_PRUNE)
 
 
 def new_batch(_lib, scene, stream, tuned=None):
     b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"],
                    scene.get("shape_kind"))
     b.set_stream(stream.cuda_stream)
-    if not INCREMENTAL_PAIRS:
-        b.set_incremental(False)
+    broadphase_setup(b)
     if tuned:
         b.set_launch_groups(*tuned[:3])
         b.set_world_order(tuned[3])
@@ -350,8 +357,7 @@ class Lanes:
             b = _lib.Batch(sc["world_body_offsets"], sc["bodies"], sc["vert_offsets"], sc["local_xy"],
                            sc.get("shape_kind"))
             b.set_stream(st.cuda_stream)
-            if not INCREMENTAL_PAIRS:
-                b.set_incremental(False)
+            broadphase_setup(b)
             if tuned:
                 b.set_launch_groups(*tuned[:3])
                 b.set_parallel_levels(tuned[4])
@@ -799,8 +805,9 @@ def run_ours(args, rank, world, local):
                        "lanes": lanes,
                        "l2": "inputs larger than L2 (state + contacts + constraints of all worlds)",
                        "launch": "CUDA graph per step",
-                       "broadphase": "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
-                       else "grid, full 3x3 search every frame",
+                       "broadphase": (f"sweep and prune for grid worlds of {SWEEP_PRUNE}+ bodies" if SWEEP_PRUNE
+                                      else "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
+                                      else "grid, full 3x3 search every frame"),
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
                                           "warps_per_group": tuned[2], "parallel_levels": bool(tuned[4]),
                                           "heavy_groups_spread": bool(tuned[5]),
@@ -855,6 +862,8 @@ def run_contacts(args, rank, world, local, scene, stream):
         bi.close()
     b = new_batch(_lib, scene, stream)
     b.set_incremental(False)
+    if SWEEP_PRUNE:
+        b.set_sweep_prune(SWEEP_PRUNE)
     for _ in range(args.warmup):
         b.collide()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -926,8 +935,10 @@ def run_contacts(args, rank, world, local, scene, stream):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": "contacts", "description": WORKLOADS["contacts"], "bodies_per_gpu": n_bodies,
                        "step": "one collide", "l2": "inputs larger than L2 are not needed: 65,536 hulls (~30 MB)",
-                       "broadphase": "grid, full 3x3 search every collide (incremental pair lists off: the "
-                                     "bodies never move in this workload)",
+                       "broadphase": (f"sweep and prune (worlds of {SWEEP_PRUNE}+ bodies), every collide"
+                                      if SWEEP_PRUNE else
+                                      "grid, full 3x3 search every collide (incremental pair lists off: the "
+                                      "bodies never move in this workload)"),
                        "incremental_pairs_value": inc_value},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": total * args.steps / (e_ms * 1e-3), "unit": UNIT,
@@ -1057,6 +1068,9 @@ def main():
                          "(0 = 8 for scenes of 256 worlds or more, 4 from 64, else 1)")
     ap.add_argument("--no-incremental", action="store_true",
                     help="grid worlds search every body's 3x3 cells every frame (no fat-box pair lists)")
+    ap.add_argument("--sweep-prune", type=int, default=0,
+                    help="grid worlds of this many bodies or more pair their small bodies by sweep and prune "
+                         "(implies --no-incremental; 0 = off)")
     ap.add_argument("--large-quality", action="store_true",
                     help="container: residual, depth and speed of ordered vs coloured, with and without the network")
     ap.add_argument("--train-source", choices=["auto", "batched", "learned"], default="auto",
@@ -1073,8 +1087,9 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.settle < 0:
         args.settle = SETTLE[args.workload]
-    global INCREMENTAL_PAIRS
-    INCREMENTAL_PAIRS = not args.no_incremental
+    global INCREMENTAL_PAIRS, SWEEP_PRUNE
+    INCREMENTAL_PAIRS = not args.no_incremental and not args.sweep_prune
+    SWEEP_PRUNE = args.sweep_prune
     rank, world, local = dist_init()
     if args.impl == "reference":
         return run_reference(args, rank, world)

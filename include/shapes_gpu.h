@@ -317,6 +317,18 @@ int shapes_batch_set_graphs(shapes_batch* b, int32_t enabled);
  * grid every frame); the pair contract of culledKeys (Aabb.hs:168-183) stays. */
 int shapes_batch_set_incremental(shapes_batch* b, int32_t enabled);
 
+/* Sweep and prune for large worlds (off by default: min_bodies = 0).  With
+ * incremental pairs off, grid worlds of at least min_bodies bodies pair their
+ * small bodies by sorting them on their boxes' lower x (a counting sort over
+ * 65,536 buckets of the world's range) and sweeping forward from each body
+ * while the candidates' lower x can still reach its upper x, instead of
+ * searching 3x3 grid cells; bodies too large for the grid keep their own
+ * rows.  The pair list is identical either way (exact overlap test, rows
+ * sorted descending).  Replaces: nothing in the reference
+ * (Broadphase/Aabb.hs:155-183 tests every pair; the pair contract of
+ * culledKeys stays). */
+int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies);
+
 /* Per-stage device timing.  While enabled, CUDA events on the handle's stream
  * bracket each stage of every step; get_profile returns the accumulated
  * milliseconds and kernel launches per stage since profiling was enabled or

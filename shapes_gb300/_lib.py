@@ -179,6 +179,7 @@ SIGNATURES = [
     ("shapes_batch_set_judge", ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     ("shapes_batch_collect", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     ("shapes_batch_get_samples", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _lp]),
+    ("shapes_batch_set_sweep_prune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]
@@ -489,6 +490,11 @@ class Batch:
         check(lib().shapes_batch_set_incremental(self._h, int(bool(enabled))), "shapes_batch_set_incremental")
 
     # ---- learned warm start ----
+    def set_sweep_prune(self, min_bodies: int) -> None:
+        """Grid worlds of at least `min_bodies` bodies pair their small bodies by
+        sweep and prune (with incremental pairs off); 0 turns it off."""
+        check(lib().shapes_batch_set_sweep_prune(self._h, int(min_bodies)), "shapes_batch_set_sweep_prune")
+
     def set_mlp(self, net: "Mlp | None") -> None:
         """Attach a network (every world's learned mask is set); None detaches."""
         self._mlp = net

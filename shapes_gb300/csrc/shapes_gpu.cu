@@ -152,6 +152,70 @@ struct shapes_batch {
   double* ext_part_sum = nullptr;
   int32_t* ext_part_cnt = nullptr;
   int32_t n_ext_chunks = 0;
+  /* sweep and prune for the small bodies of large grid worlds (incremental pairs off) */
+  int32_t sap_min_bodies = 0; /* 0: off */
+  bool any_sap = false;
+  int32_t n_sap_buckets = 0;
+  uint8_t* world_sap = nullptr;
+  int32_t *sap_base = nullptr, *sap_cnt = nullptr, *sap_off = nullptr, *sap_ids = nullptr, *sap_qs = nullptr;
+  int32_t *sap_cursor = nullptr, *sap_end = nullptr;
+  uint64_t* sap_range = nullptr;
+
+  /* Tile sums every scan of a step needs: the longest scanned array is the
+   * bodies, the contact slots, the grid buckets or the sweep buckets. */
+  int32_t scan_tiles_needed() const {
+    const int64_t scan_n =
+        std::max<int64_t>(std::max<int64_t>(std::max<int64_t>(N, contact_cap), n_buckets), n_sap_buckets) + 1;
+    return (int32_t)((scan_n + shapes::kScanTile - 1) / shapes::kScanTile) + 1;
+  }
+
+  void free_sap() {
+    dfree(world_sap); dfree(sap_base); dfree(sap_cnt); dfree(sap_off); dfree(sap_ids); dfree(sap_qs);
+    dfree(sap_cursor); dfree(sap_end); dfree(sap_range);
+    world_sap = nullptr;
+    sap_base = sap_cnt = sap_off = sap_ids = sap_qs = sap_cursor = sap_end = nullptr;
+    sap_range = nullptr;
+    any_sap = false;
+    n_sap_buckets = 0;
+  }
+
+  /* Marks the grid worlds of at least sap_min_bodies bodies and sizes their
+   * buckets (kSapBuckets per world). */
+  void setup_sap() {
+    free_sap();
+    if (sap_min_bodies <= 0) return;
+    std::vector<uint8_t> flag(W, 0);
+    std::vector<int32_t> base(W, 0);
+    int64_t nb = 0;
+    for (int w = 0; w < W; ++w) {
+      const int32_t n = h_world_body_off[w + 1] - h_world_body_off[w];
+      if (n >= grid_min_bodies && n >= sap_min_bodies) {
+        flag[w] = 1;
+        base[w] = (int32_t)nb;
+        nb += shapes::kSapBuckets;
+      }
+    }
+    if (nb == 0) return;
+    if (nb > INT32_MAX / 2) throw CudaError{cudaErrorMemoryAllocation};
+    any_sap = true;
+    n_sap_buckets = (int32_t)nb;
+    world_sap = dalloc<uint8_t>(W, "cudaMalloc sweep");
+    sap_base = dalloc<int32_t>(W, "cudaMalloc sweep");
+    sap_cnt = dalloc<int32_t>((size_t)nb + 1, "cudaMalloc sweep");
+    sap_off = dalloc<int32_t>((size_t)nb + 1, "cudaMalloc sweep");
+    sap_ids = dalloc<int32_t>(std::max<int32_t>(N, 1), "cudaMalloc sweep");
+    sap_qs = dalloc<int32_t>(std::max<int32_t>(N, 1), "cudaMalloc sweep");
+    sap_cursor = dalloc<int32_t>(std::max<int32_t>(N, 1), "cudaMalloc sweep");
+    sap_end = dalloc<int32_t>(W, "cudaMalloc sweep");
+    sap_range = dalloc<uint64_t>(2 * (size_t)W, "cudaMalloc sweep");
+    ck(cudaMemcpy(world_sap, flag.data(), W, cudaMemcpyHostToDevice), "upload sweep");
+    ck(cudaMemcpy(sap_base, base.data(), sizeof(int32_t) * W, cudaMemcpyHostToDevice), "upload sweep");
+    if (tile_sums && tile_cap < scan_tiles_needed()) { /* the sweep buckets' scan is the longest */
+      dfree(tile_sums);
+      tile_cap = scan_tiles_needed();
+      tile_sums = dalloc<int32_t>(tile_cap, "cudaMalloc scan");
+    }
+  }
   int32_t* np_cls = nullptr; /* [2 * kNpClasses + 1] */
   int32_t* world_pair_off = nullptr;
   /* contacts: ping-pong between two buffers, the cache of step s is the
@@ -389,6 +453,18 @@ struct shapes_batch {
     d.ext_part_sum = ext_part_sum;
     d.ext_part_cnt = ext_part_cnt;
     d.n_ext_chunks = n_ext_chunks;
+    if (any_sap) {
+      d.world_sap = world_sap;
+      d.sap_base = sap_base;
+      d.sap_cnt = sap_cnt;
+      d.sap_off = sap_off;
+      d.n_sap_buckets = n_sap_buckets;
+      d.sap_ids = sap_ids;
+      d.sap_qs = sap_qs;
+      d.sap_cursor = sap_cursor;
+      d.sap_range = sap_range;
+      d.sap_end = sap_end;
+    }
     d.lx = lx;
     d.ly = ly;
     d.radius = radius;
@@ -591,8 +667,7 @@ struct shapes_batch {
     gdesc = dalloc<int4>(item_cap + W + 1, "cudaMalloc items");
     ghist = dalloc<int32_t>(item_cap + W + 1, "cudaMalloc items");
     idesc = dalloc<int4>(item_cap, "cudaMalloc items");
-    const int64_t scan_n = std::max<int64_t>(std::max<int64_t>(N, contact_cap), n_buckets) + 1;
-    tile_cap = (int32_t)((scan_n + shapes::kScanTile - 1) / shapes::kScanTile) + 1;
+    tile_cap = scan_tiles_needed();
     tile_sums = dalloc<int32_t>(tile_cap, "cudaMalloc scan");
     if (!large_worlds.empty()) {
       lw_refs = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc large world");
@@ -897,6 +972,7 @@ struct shapes_batch {
       ck(cudaMemcpy(ext_chunk_off, choff.data(), sizeof(int32_t) * (W + 1), cudaMemcpyHostToDevice), "upload grid");
     }
     setup_incremental();
+    setup_sap();
   }
   int32_t smem_last_cap = 0; /* bodies whose last level fits the solver's shared memory */
 
@@ -937,6 +1013,8 @@ struct shapes_batch {
     ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * 2, stream), "memset");
     ck(cudaMemsetAsync(counters + shapes::kCntGroupAlloc, 0, sizeof(unsigned long long), stream), "memset");
     const bool inc = any_grid && d.nbr != nullptr;
+    const bool sap = any_sap && !inc;
+    if (!sap) d.world_sap = nullptr;
     if (inc) {
       stage(0, 7, [&]() {
         ck(cudaMemsetAsync(bucket_cnt, 0, sizeof(int32_t) * ((size_t)n_buckets + 1), stream), "memset");
@@ -961,21 +1039,34 @@ struct shapes_batch {
       });
       scan(bucket_cnt, n_buckets, nullptr, bucket_off);
       stage(0, 1, [&]() { shapes::k_grid_scatter<<<grid_for(N, 256), 256, 0, stream>>>(d); });
+      if (sap) {
+        stage(0, 2, [&]() {
+          ck(cudaMemsetAsync(sap_cnt, 0, sizeof(int32_t) * ((size_t)n_sap_buckets + 1), stream), "memset");
+          shapes::k_sap_count<<<grid_for(N, 256), 256, 0, stream>>>(d);
+        });
+        scan(sap_cnt, n_sap_buckets, nullptr, sap_off);
+        stage(0, 2, [&]() {
+          shapes::k_sap_scatter<<<grid_for(N, 256), 256, 0, stream>>>(d);
+          shapes::k_sap_ends<<<grid_for(W, 128), 128, 0, stream>>>(d);
+        });
+      }
     }
-    stage(0, any_grid ? 2 : 1, [&]() {
+    stage(0, any_grid ? (sap ? 3 : 2) : 1, [&]() {
       shapes::k_broadphase<true><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
       if (inc)
         shapes::k_inc_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
       else if (any_grid)
         shapes::k_grid_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
+      if (sap) shapes::k_sap_rows<true><<<grid_for(N, 128), 128, 0, stream>>>(d);
     });
     scan(row_cnt, N, nullptr, row_off);
-    stage(0, any_grid ? 3 : 1, [&]() {
+    stage(0, any_grid ? (sap ? 4 : 3) : 1, [&]() {
       shapes::k_broadphase<false><<<grid_for((long long)N * 32, 256), 256, 0, stream>>>(d);
       if (inc)
         shapes::k_inc_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
       else if (any_grid)
         shapes::k_grid_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
+      if (sap) shapes::k_sap_rows<false><<<grid_for(N, 128), 128, 0, stream>>>(d);
       if (any_grid) shapes::k_grid_sort_rows<<<grid_for(N, 128), 128, 0, stream>>>(d);
     });
     stage(6, 1, [&]() { shapes::k_world_pair_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
@@ -1418,6 +1509,7 @@ struct shapes_batch {
     dfree(grid_T); dfree(grid_base); dfree(grid_inv_s); dfree(grid_lim); dfree(bucket_cnt); dfree(bucket_off);
     dfree(grid_ids); dfree(cell_x); dfree(cell_y); dfree(row_mode); dfree(large_cnt); dfree(large_ids);
     dfree(ext_chunk); dfree(ext_chunk_off); dfree(ext_part_sum); dfree(ext_part_cnt);
+    free_sap();
     free_incremental();
     dfree(radius);
     dfree(metric_part);
@@ -2743,6 +2835,17 @@ int shapes_batch_set_incremental(shapes_batch* b, int32_t enabled) {
     b->incremental = enabled != 0;
     b->invalidate_graphs();
     b->reset_incremental();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies) {
+  if (!b || min_bodies < 0) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->sap_min_bodies = min_bodies;
+    b->invalidate_graphs();
+    b->setup_sap();
     return SHAPES_OK;
   });
 }

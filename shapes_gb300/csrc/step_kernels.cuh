@@ -115,6 +115,16 @@ struct Dev {
   double* ext_part_sum;         /* [n_ext_chunks] chunk sums of box extents */
   int32_t* ext_part_cnt;        /* [n_ext_chunks] chunk counts */
   int32_t n_ext_chunks;
+  const uint8_t* world_sap; /* [n_worlds] 1: the world's small bodies pair by sweep and prune (null: none) */
+  const int32_t* sap_base;  /* [n_worlds] first of the world's kSapBuckets buckets */
+  int32_t* sap_cnt;         /* [n_sap_buckets + 1] bucket counts */
+  int32_t* sap_off;         /* [n_sap_buckets + 1] their exclusive scan: bucket starts, then ends */
+  int32_t n_sap_buckets;
+  int32_t* sap_ids;         /* [n_bodies] small bodies of sweep worlds, in bucket order */
+  int32_t* sap_qs;          /* [n_bodies] their buckets, in the same order */
+  int32_t* sap_cursor;      /* [n_bodies] per row (mirrored index): the next free slot of the row */
+  uint64_t* sap_range;      /* [2 * n_worlds] min and max order key of the small bodies' lower x */
+  int32_t* sap_end;         /* [n_worlds] end of the world's run in sap_ids */
   const int32_t* pose_order; /* [n_bodies] pose-kernel order: within chunks of 1024 bodies, grouped by vertex
                                 count, so that a warp's vertex loops have one length (null: index order) */
   int32_t* np_cls;     /* [2 * kNpClasses + 1] class counts, then offsets and cursors */
@@ -672,6 +682,10 @@ __global__ void k_grid_stats(Dev d) {
   d.grid_inv_s[wld] = inv;
   d.grid_lim[wld] = inv > 0.0 ? (1.0 - 0x1p-20) / inv : 0.0;
   d.large_cnt[wld] = 0;
+  if (d.world_sap && d.world_sap[wld]) { /* the small bodies' range of lower x, gathered by k_grid_bin */
+    d.sap_range[2 * wld] = ~0ull;
+    d.sap_range[2 * wld + 1] = 0ull;
+  }
 }
 
 /* One thread per body: grid bodies get a cell and a bucket count, the rest go
@@ -701,7 +715,13 @@ __global__ void k_grid_bin(Dev d) {
         mode = 1;
         d.cell_x[g] = cx;
         d.cell_y[g] = cy;
-        atomicAdd(&d.bucket_cnt[d.grid_base[wld] + cell_bucket(cx, cy, T)], 1);
+        if (d.world_sap && d.world_sap[wld]) {
+          const uint64_t k = okey(d.box[4 * g + 0]);
+          atomicMin(reinterpret_cast<unsigned long long*>(&d.sap_range[2 * wld]), (unsigned long long)k);
+          atomicMax(reinterpret_cast<unsigned long long*>(&d.sap_range[2 * wld + 1]), (unsigned long long)k);
+        } else {
+          atomicAdd(&d.bucket_cnt[d.grid_base[wld] + cell_bucket(cx, cy, T)], 1);
+        }
       } else {
         const int k = atomicAdd(&d.large_cnt[wld], 1);
         d.large_ids[d.world_body_off[wld] + k] = g;
@@ -716,6 +736,7 @@ __global__ void k_grid_scatter(Dev d) {
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
     if (!d.row_mode[g]) continue;
     const int wld = d.body_world[g];
+    if (d.world_sap && d.world_sap[wld]) continue; /* swept, not binned */
     const int b = d.grid_base[wld] + cell_bucket(d.cell_x[g], d.cell_y[g], d.grid_T[wld]);
     const int pos = atomicAdd(&d.bucket_off[b], 1);
     d.grid_ids[pos] = g;
@@ -744,7 +765,8 @@ __global__ void k_grid_rows(Dev d) {
     ki[3] = d.boxk[4 * g + 3];
     int count = 0;
     const int out = COUNT ? 0 : d.row_off[q];
-    for (int dy = -1; dy <= 1; ++dy) {
+    const bool sap = d.world_sap && d.world_sap[wld]; /* the sweep adds the small-body pairs */
+    for (int dy = sap ? 2 : -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
         const int ncx = cx + dx, ncy = cy + dy;
         const int b = base + cell_bucket(ncx, ncy, T);
@@ -773,7 +795,107 @@ __global__ void k_grid_rows(Dev d) {
         ++count;
       }
     }
-    if (COUNT) d.row_cnt[q] = count;
+    if (COUNT) {
+      d.row_cnt[q] = count;
+      if (sap) d.sap_cursor[q] = count; /* the sweep's pairs follow the large ones */
+    }
+  }
+}
+
+/* ---- sweep and prune ------------------------------------------------------
+ * For large single worlds, the small bodies (the grid's classification: box
+ * below the cell limit) can be paired by sweep and prune along x instead of
+ * the 3x3 cell search.  The bodies are sorted by their box's lower x
+ * quantised to kSapBuckets buckets over the world's range, q(x) =
+ * floor((x - xmin) * (kSapBuckets - 1) / (xmax - xmin)) clamped to the last
+ * bucket; q is non-decreasing in x (each operation is a monotone rounding),
+ * so two small bodies whose closed boxes overlap, x0_j <= x1_i, have
+ * q(x0_j) <= q(x1_i).  A counting sort (one 16-bit radix digit) orders them;
+ * from each body the sweep walks forward while q(x0) <= q(x1) of the body
+ * and tests every candidate with the exact test every path uses
+ * (pair_overlaps).  Each overlapping pair is met once, from the body earlier
+ * in the order (within a bucket the order is arbitrary: the walk from the
+ * earlier one still reaches the later one).  It is added to the row of its
+ * larger index with an atomic slot after that row's large-body pairs, and the
+ * rows are then sorted descending like the grid's, so the pairs and their
+ * order are exactly those of culledKeys. */
+constexpr int kSapBuckets = 65536;
+
+__device__ __forceinline__ double from_okey(uint64_t k) {
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ int sap_bucket(const Dev& d, int wld, double x) {
+  const double lo = from_okey(d.sap_range[2 * wld]), hi = from_okey(d.sap_range[2 * wld + 1]);
+  const double span = hi - lo;
+  const double scale = span > 0.0 && small_mag(span) ? (double)(kSapBuckets - 1) / span : 0.0;
+  const double t = (x - lo) * scale;
+  if (!(t > 0.0)) return 0;
+  return t >= (double)(kSapBuckets - 1) ? kSapBuckets - 1 : (int)t;
+}
+
+__global__ void k_sap_count(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (!d.row_mode[g]) continue;
+    const int wld = d.body_world[g];
+    if (!d.world_sap[wld]) continue;
+    atomicAdd(&d.sap_cnt[d.sap_base[wld] + sap_bucket(d, wld, d.box[4 * g + 0])], 1);
+  }
+}
+
+/* Places the swept bodies by bucket (sap_cnt turns from starts into ends);
+ * records the end of each world's run. */
+__global__ void k_sap_scatter(Dev d) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < d.n_bodies; g += gridDim.x * blockDim.x) {
+    if (!d.row_mode[g]) continue;
+    const int wld = d.body_world[g];
+    if (!d.world_sap[wld]) continue;
+    const int q = sap_bucket(d, wld, d.box[4 * g + 0]);
+    const int pos = atomicAdd(&d.sap_off[d.sap_base[wld] + q], 1);
+    d.sap_ids[pos] = g;
+    d.sap_qs[pos] = q;
+  }
+}
+
+__global__ void k_sap_ends(Dev d) {
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < d.n_worlds; w += gridDim.x * blockDim.x)
+    if (d.world_sap[w]) d.sap_end[w] = d.sap_off[d.sap_base[w] + kSapBuckets - 1];
+}
+
+/* One thread per position of the sorted run: the forward sweep.  COUNT adds
+ * to the rows' counts; otherwise writes the pairs at atomic slots. */
+template <bool COUNT>
+__global__ void k_sap_rows(Dev d) {
+  const int n_swept = d.sap_off[d.n_sap_buckets - 1]; /* end of the last bucket */
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n_swept; p += gridDim.x * blockDim.x) {
+    const int g = d.sap_ids[p];
+    const int wld = d.body_world[g];
+    const int off = d.world_body_off[wld];
+    const int n = d.world_body_off[wld + 1] - off;
+    const int end = d.sap_end[wld];
+    const int q1 = sap_bucket(d, wld, d.box[4 * g + 1]);
+    const uint8_t fi = d.flags[g];
+    uint64_t ki[4];
+    ki[0] = d.boxk[4 * g + 0];
+    ki[1] = d.boxk[4 * g + 1];
+    ki[2] = d.boxk[4 * g + 2];
+    ki[3] = d.boxk[4 * g + 3];
+    for (int t = p + 1; t < end && d.sap_qs[t] <= q1; ++t) {
+      const int j = d.sap_ids[t];
+      if (!pair_overlaps(d, g, j, fi, ki)) continue;
+      const int hi = g > j ? g : j, lo = g > j ? j : g;
+      const int q = off + (n - 1 - (hi - off));
+      if (COUNT) {
+        atomicAdd(&d.row_cnt[q], 1);
+      } else {
+        const int pos = d.row_off[q] + atomicAdd(&d.sap_cursor[q], 1);
+        if (pos < d.pair_cap) {
+          d.pair_a[pos] = hi;
+          d.pair_b[pos] = lo;
+        }
+      }
+    }
   }
 }
 
