@@ -24,8 +24,9 @@ NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-rel
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2,-pthread", "-shared", "-lpthread"]
 
 SOURCES = [CSRC / "shapes_gpu.cu", CSRC / "mlp.cu"]
-HEADERS = [CSRC / "step_kernels.cuh", CSRC / "large_world.cuh", CSRC / "learned.cuh", CSRC / "fp64_ops.cuh",
-           CSRC / "shapes_sincos.h", CSRC / "mlp.h", CSRC / "tc05.cuh", HERE.parent / "include" / "shapes_gpu.h"]
+HEADERS = [CSRC / "step_kernels.cuh", CSRC / "large_world.cuh", CSRC / "lw_order.cuh", CSRC / "learned.cuh",
+           CSRC / "fp64_ops.cuh", CSRC / "shapes_sincos.h", CSRC / "shapes_sincos_tables.h", CSRC / "mlp.h",
+           CSRC / "tc05.cuh", HERE.parent / "include" / "shapes_gpu.h"]
 
 
 def nvcc() -> str:
@@ -57,7 +58,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if force or needs_build(LIB, SOURCES + HEADERS):
         jobs.append(_compile(LIB, SOURCES, verbose))
     probe_src = [CSRC / "fp64_probe.cu"]
-    if force or needs_build(PROBE_LIB, probe_src + [CSRC / "fp64_ops.cuh", CSRC / "tc05.cuh"]):
+    if force or needs_build(PROBE_LIB, probe_src + [CSRC / "fp64_ops.cuh", CSRC / "tc05.cuh", CSRC / "lw_order.cuh"]):
         jobs.append(_compile(PROBE_LIB, probe_src, verbose))
     for proc, tmp, lib in jobs:
         if proc.wait() != 0:

@@ -513,3 +513,37 @@ extern "C" int shapes_probe_split_rates(double* out6) {
   cudaFree(d);
   return err == cudaSuccess ? 0 : -5;
 }
+
+/* ---- ticket order of the ordered large-world solve (lw_order.cuh), on the host ---- */
+#include <algorithm>
+#include <vector>
+
+#include "lw_order.cuh"
+
+/* For every P <= max_p, R <= max_r and skew 1 <= S <= R: lw_ticket(t) for each
+ * ticket t against the tickets sorted by key p S + r (ties by p).  *cases is
+ * the number of tickets checked, *bad the number that differ. */
+extern "C" int shapes_probe_lw_ticket_check(int max_p, int max_r, unsigned long long* cases, unsigned long long* bad) {
+  unsigned long long n = 0, nbad = 0;
+  std::vector<std::pair<long long, int>> order;
+  for (int P = 1; P <= max_p; ++P)
+    for (int R = 1; R <= max_r; ++R)
+      for (int S = 1; S <= R; ++S) {
+        order.clear();
+        for (int p = 0; p < P; ++p)
+          for (int r = 0; r < R; ++r) order.push_back({(long long)p * S + r, p * R + r});
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) {
+                           return x.first < y.first;
+                         });
+        for (long long t = 0; t < (long long)P * R; ++t) {
+          int p, r;
+          shapes::lw_ticket(t, P, S, R, p, r);
+          ++n;
+          if (p * R + r != order[(size_t)t].second) ++nbad;
+        }
+      }
+  *cases = n;
+  *bad = nbad;
+  return 0;
+}

@@ -267,7 +267,10 @@ struct shapes_batch {
   int32_t* lw_hrank = nullptr;
   int32_t* lw_hitflag = nullptr;
   int32_t* lw_hitoff = nullptr;
-  int32_t* lw_hit_idx = nullptr;
+  int32_t* lw_rowflag = nullptr; /* ordered path by rows: row starts (flag, scanned, list) */
+  int32_t* lw_rowoff = nullptr;
+  int32_t* lw_row_start = nullptr;
+  int4* lw_side = nullptr;
   int32_t* lw_color = nullptr;
   int32_t* lw_color_cnt = nullptr;
   int32_t* lw_color_list = nullptr;
@@ -601,9 +604,12 @@ struct shapes_batch {
     dfree(tile_sums);
     dfree(snap_key); dfree(snap_lam);
     free_row_buffers();
-    dfree(lw_refs); dfree(lw_rank); dfree(lw_hrank); dfree(lw_hitflag); dfree(lw_hitoff); dfree(lw_hit_idx);
+    dfree(lw_refs); dfree(lw_rank); dfree(lw_hrank); dfree(lw_hitflag); dfree(lw_hitoff);
+    dfree(lw_rowflag); dfree(lw_rowoff); dfree(lw_row_start); dfree(lw_side);
+    lw_rowflag = lw_rowoff = lw_row_start = nullptr;
+    lw_side = nullptr;
     dfree(lw_color); dfree(lw_color_list); dfree(lw_seqflag); dfree(lw_seqoff); dfree(lw_seq_list);
-    lw_refs = lw_rank = lw_hrank = lw_hitflag = lw_hitoff = lw_hit_idx = lw_color = lw_color_list = nullptr;
+    lw_refs = lw_rank = lw_hrank = lw_hitflag = lw_hitoff = lw_color = lw_color_list = nullptr;
     lw_seqflag = lw_seqoff = lw_seq_list = nullptr;
     pair_a = pair_b = slot_cnt = slot_off = slot_feat = nullptr;
     slot_val = nullptr;
@@ -675,7 +681,10 @@ struct shapes_batch {
       lw_hrank = dalloc<int32_t>(2 * (size_t)contact_cap, "cudaMalloc large world");
       lw_hitflag = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
       lw_hitoff = dalloc<int32_t>((size_t)contact_cap + 1, "cudaMalloc large world");
-      lw_hit_idx = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_rowflag = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_rowoff = dalloc<int32_t>((size_t)contact_cap + 1, "cudaMalloc large world");
+      lw_row_start = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
+      lw_side = dalloc<int4>(2 * (size_t)contact_cap, "cudaMalloc large world");
       lw_color = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
       lw_color_list = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
       lw_seqflag = dalloc<int32_t>(contact_cap, "cudaMalloc large world");
@@ -794,6 +803,7 @@ struct shapes_batch {
     lw_done = dalloc<int32_t>(lw_nb_max, "cudaMalloc large world");
     lw_color_cnt = dalloc<int32_t>(shapes::kMaxColors + 1, "cudaMalloc large world");
     lw_ctl = dalloc<unsigned long long>(8 * large_worlds.size(), "cudaMalloc large world");
+    ck(cudaMemset(lw_ctl, 0, sizeof(unsigned long long) * 8 * large_worlds.size()), "memset");
     if (!metric_part) metric_part = dalloc<double>(shapes::kMetricParts, "cudaMalloc large world");
   }
 
@@ -812,7 +822,10 @@ struct shapes_batch {
     w.done = lw_done;
     w.hitflag = lw_hitflag;
     w.hitoff = lw_hitoff;
-    w.hit_idx = lw_hit_idx;
+    w.rowflag = lw_rowflag;
+    w.rowoff = lw_rowoff;
+    w.row_start = lw_row_start;
+    w.side = lw_side;
     w.color = lw_color;
     w.color_cnt = lw_color_cnt;
     w.color_list = lw_color_list;
@@ -847,21 +860,32 @@ struct shapes_batch {
   void solve_large_world(const Dev& d, size_t k, const shapes_config& cfg) {
     shapes::LW w = lw_view(k);
     const int cap = contact_cap;
-    stage(3, 5, [&]() {
+    const bool ordered = !(cfg.flags & SHAPES_FLAG_COLOURED);
+    stage(3, ordered ? 18 : 11, [&]() {
       shapes::k_lw_setup<<<grid_for(w.nb + 1, 256), 256, 0, stream>>>(d, w);
       shapes::k_lw_count<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
       scan_raw(w.bcnt, w.nb, nullptr, w.bstart);
       shapes::k_lw_scatter<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
       shapes::k_lw_rank<<<grid_for(w.nb, 128), 128, 0, stream>>>(d, w);
       scan_raw(w.hitflag, cap, w.ctl + 4, w.hitoff);
-      shapes::k_lw_hit_list<<<grid_for(cap, 256), 256, 0, stream>>>(w, counters + shapes::kCntHits,
-                                                                    counters + shapes::kCntItems, cfg.iterations);
+      shapes::k_lw_item_counts<<<1, 1, 0, stream>>>(w, counters + shapes::kCntHits, counters + shapes::kCntItems,
+                                                    cfg.iterations);
+      if (ordered) { /* the sequence's rows (runs of contacts with one first body), pass skew, side entries */
+        shapes::k_lw_rowflag<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+        scan_raw(w.rowflag, cap, w.ctl + 4, w.rowoff);
+        shapes::k_lw_row_list<<<grid_for(cap, 256), 256, 0, stream>>>(w);
+        shapes::k_lw_skew<<<grid_for(cap, 256), 256, 0, stream>>>(d, w);
+        shapes::k_lw_side<<<grid_for(2 * cap, 256), 256, 0, stream>>>(d, w);
+      }
     });
-    stage(4, 1, [&]() {
+    const int passes = cfg.iterations + (cfg.warm_start ? 1 : 0);
+    const int colour_launches = 1 + 128 + 1 + 3 + 1 + 3 + 1 + passes * (shapes::kSeqColor + 1);
+    stage(4, (ordered ? 1 : colour_launches) + (cfg.external ? 1 : 0), [&]() {
       if (cfg.external)
         shapes::k_lw_gravity<<<grid_for(w.nb, 256), 256, 0, stream>>>(d, w, cfg.accel_x, cfg.accel_y, cfg.dt);
-      if (!(cfg.flags & SHAPES_FLAG_COLOURED)) {
-        shapes::k_lw_ordered<<<kSMs * 8, 128, 0, stream>>>(d, w, cfg.iterations, cfg.warm_start);
+      if (ordered) {
+        shapes::k_lw_ordered<<<kSMs * shapes::kOrderedBlocksPerSM, shapes::kOrderedThreads, 0, stream>>>(
+            d, w, cfg.iterations, cfg.warm_start);
         return;
       }
       shapes::k_lw_color_init<<<grid_for(cap, 256), 256, 0, stream>>>(w);
@@ -1229,6 +1253,8 @@ struct shapes_batch {
 
   void enqueue_begin(bool solve) {
     ck(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * shapes::kCntSlots, stream), "memset");
+    if (lw_ctl) /* the large-world timeout flags stay set through the run's steps */
+      ck(cudaMemsetAsync(lw_ctl, 0, sizeof(unsigned long long) * 8 * large_worlds.size(), stream), "memset");
     run_saved_cache_buf = cache_buf;
     run_saved_cap = contact_cap;
     if (solve) snapshot();
