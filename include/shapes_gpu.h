@@ -165,8 +165,10 @@ int shapes_batches_step_io(shapes_batch* const* bs, int32_t n, const shapes_conf
 
 /* Called on the host after step `step` of handle `handle_index` has written
  * its result into state[handle_index]; the caller may read and change that
- * state before the next upload.  Non-zero stops that handle's loop.  Calls
- * for different handles may come from different threads at once. */
+ * state before the next upload: the values in its arrays, not the array
+ * pointers, whose device addresses are resolved once per call.  Non-zero
+ * stops that handle's loop.  Calls for different handles may come from
+ * different threads at once. */
 typedef int (*shapes_step_callback)(void* user, int32_t handle_index, int32_t step);
 
 /* nsteps steps of n handles whose body state lives in caller host memory:
@@ -360,10 +362,11 @@ void shapes_batch_destroy(shapes_batch* b);
  *   SHAPES_NOALLOC_MAX_VERTS, broadphase pairs <= SHAPES_NOALLOC_MAX_PAIRS;
  *   beyond them it returns SHAPES_E_CAPACITY.  The array (about 10 MB) is
  *   held by every GPU that loads the library until the process exits.
- *   The first call on a device looks up the array's device address
- *   (cudaGetSymbolAddress); make that first call before any stream capture.
- *   The address is kept for the life of the process: after cudaDeviceReset
- *   on that device the function must not be called again.
+ *   The call cannot be captured into a CUDA graph: it synchronizes
+ *   `cuda_stream` and reads counters on the host between kernels.  The first
+ *   call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress) and keeps it for the life of the process: after
+ *   cudaDeviceReset on that device the function must not be called again.
  *   All calls share the one array: calls that overlap on the GPU (different
  *   streams, threads or processes sharing the library) race.  The call
  *   synchronizes `cuda_stream` (NULL = legacy default stream) before it
