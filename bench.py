@@ -314,6 +314,10 @@ def run_reference(args, rank, world):
 
 INCREMENTAL_PAIRS = True  # --no-incremental turns the fat-box pair lists off
 SWEEP_PRUNE = 0  # --sweep-prune N: grid worlds of N bodies or more pair by sweep and prune (incremental off)
+NP_DESC = {1: "SAT one thread per pair (pairs ordered by vertex counts)", 32: "SAT one warp per pair, shuffle-reduced "
+           "axis search"}
+NP_DESC.update({k: f"SAT {k} lanes per pair, shuffle-reduced axis search" for k in (2, 4, 8, 16)})
+NP_LANES = 1  # --np-lanes L: lanes per pair in the narrowphase (1 = a thread per pair, 32 = a warp per pair)
 
 
 def broadphase_setup(b):
@@ -321,6 +325,8 @@ def broadphase_setup(b):
         b.set_incremental(False)
     if SWEEP_PRUNE:
         b.set_sweep_prune(SWEEP_PRUNE)
+    if NP_LANES != 1:
+        b.set_narrowphase_lanes(NP_LANES)
 
 
 def new_batch(_lib, scene, stream, tuned=None):
@@ -808,6 +814,7 @@ def run_ours(args, rank, world, local):
                        "broadphase": (f"sweep and prune for grid worlds of {SWEEP_PRUNE}+ bodies" if SWEEP_PRUNE
                                       else "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
                                       else "grid, full 3x3 search every frame"),
+                       "narrowphase": NP_DESC[NP_LANES],
                        "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
                                           "warps_per_group": tuned[2], "parallel_levels": bool(tuned[4]),
                                           "heavy_groups_spread": bool(tuned[5]),
@@ -864,6 +871,8 @@ def run_contacts(args, rank, world, local, scene, stream):
     b.set_incremental(False)
     if SWEEP_PRUNE:
         b.set_sweep_prune(SWEEP_PRUNE)
+    if NP_LANES != 1:
+        b.set_narrowphase_lanes(NP_LANES)
     for _ in range(args.warmup):
         b.collide()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -939,6 +948,7 @@ def run_contacts(args, rank, world, local, scene, stream):
                                       if SWEEP_PRUNE else
                                       "grid, full 3x3 search every collide (incremental pair lists off: the "
                                       "bodies never move in this workload)"),
+                       "narrowphase": NP_DESC[NP_LANES],
                        "incremental_pairs_value": inc_value},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": total * args.steps / (e_ms * 1e-3), "unit": UNIT,
@@ -1071,6 +1081,8 @@ def main():
     ap.add_argument("--sweep-prune", type=int, default=0,
                     help="grid worlds of this many bodies or more pair their small bodies by sweep and prune "
                          "(implies --no-incremental; 0 = off)")
+    ap.add_argument("--np-lanes", type=int, default=1, choices=[1, 2, 4, 8, 16, 32],
+                    help="lanes per pair in the narrowphase's axis search (1 = a thread per pair, 32 = a warp per pair)")
     ap.add_argument("--large-quality", action="store_true",
                     help="container: residual, depth and speed of ordered vs coloured, with and without the network")
     ap.add_argument("--train-source", choices=["auto", "batched", "learned"], default="auto",
@@ -1087,9 +1099,10 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.settle < 0:
         args.settle = SETTLE[args.workload]
-    global INCREMENTAL_PAIRS, SWEEP_PRUNE
+    global INCREMENTAL_PAIRS, SWEEP_PRUNE, NP_LANES
     INCREMENTAL_PAIRS = not args.no_incremental and not args.sweep_prune
     SWEEP_PRUNE = args.sweep_prune
+    NP_LANES = args.np_lanes
     rank, world, local = dist_init()
     if args.impl == "reference":
         return run_reference(args, rank, world)

@@ -331,6 +331,14 @@ int shapes_batch_set_incremental(shapes_batch* b, int32_t enabled);
  * culledKeys stays). */
 int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies);
 
+/* Lanes per pair in the narrowphase: 1 (default) runs one pair per thread;
+ * 2, 4, 8, 16 or 32 split each pair's separating-axis search over that many
+ * lanes of a warp (32: one warp per pair) and reduce it with shuffles, then
+ * build the manifold on the pair's first lane.  The contacts are identical
+ * either way.  Replaces: nothing (SAT.hs:121-138's minOverlap fold is kept
+ * exactly, including which axis wins among equal or NaN depths). */
+int shapes_batch_set_narrowphase_lanes(shapes_batch* b, int32_t lanes);
+
 /* Per-stage device timing.  While enabled, CUDA events on the handle's stream
  * bracket each stage of every step; get_profile returns the accumulated
  * milliseconds and kernel launches per stage since profiling was enabled or

@@ -180,6 +180,7 @@ SIGNATURES = [
     ("shapes_batch_collect", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     ("shapes_batch_get_samples", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _lp]),
     ("shapes_batch_set_sweep_prune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_set_narrowphase_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]
@@ -494,6 +495,11 @@ class Batch:
         """Grid worlds of at least `min_bodies` bodies pair their small bodies by
         sweep and prune (with incremental pairs off); 0 turns it off."""
         check(lib().shapes_batch_set_sweep_prune(self._h, int(min_bodies)), "shapes_batch_set_sweep_prune")
+
+    def set_narrowphase_lanes(self, lanes: int) -> None:
+        """Lanes per pair in the narrowphase: 1 (default, a thread per pair) or 2-32
+        (the axis search split over lanes, 32 = a warp per pair); same contacts."""
+        check(lib().shapes_batch_set_narrowphase_lanes(self._h, int(lanes)), "shapes_batch_set_narrowphase_lanes")
 
     def set_mlp(self, net: "Mlp | None") -> None:
         """Attach a network (every world's learned mask is set); None detaches."""

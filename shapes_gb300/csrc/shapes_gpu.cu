@@ -154,6 +154,7 @@ struct shapes_batch {
   int32_t n_ext_chunks = 0;
   /* sweep and prune for the small bodies of large grid worlds (incremental pairs off) */
   int32_t sap_min_bodies = 0; /* 0: off */
+  int32_t np_lanes = 1;       /* lanes per pair in the narrowphase (1: k_narrowphase) */
   bool any_sap = false;
   int32_t n_sap_buckets = 0;
   uint8_t* world_sap = nullptr;
@@ -1099,7 +1100,14 @@ struct shapes_batch {
       shapes::k_np_count<<<grid_for(pair_cap, 256), 256, 0, stream>>>(d);
       shapes::k_np_offsets<<<1, 32, 0, stream>>>(d);
       shapes::k_np_scatter<<<grid_for(pair_cap, 256), 256, 0, stream>>>(d);
-      shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d);
+      switch (np_lanes) {
+        case 2: shapes::k_narrowphase_lanes<2><<<grid_for(2LL * pair_cap, 128), 128, 0, stream>>>(d); break;
+        case 4: shapes::k_narrowphase_lanes<4><<<grid_for(4LL * pair_cap, 128), 128, 0, stream>>>(d); break;
+        case 8: shapes::k_narrowphase_lanes<8><<<grid_for(8LL * pair_cap, 128), 128, 0, stream>>>(d); break;
+        case 16: shapes::k_narrowphase_lanes<16><<<grid_for(16LL * pair_cap, 128), 128, 0, stream>>>(d); break;
+        case 32: shapes::k_narrowphase_lanes<32><<<grid_for(32LL * pair_cap, 128), 128, 0, stream>>>(d); break;
+        default: shapes::k_narrowphase<<<grid_for(pair_cap, 128), 128, 0, stream>>>(d);
+      }
     });
     scan(slot_cnt, pair_cap, counters + shapes::kCntPairs, slot_off);
     stage(6, 1, [&]() { shapes::k_world_contact_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
@@ -2872,6 +2880,17 @@ int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies) {
     b->sap_min_bodies = min_bodies;
     b->invalidate_graphs();
     b->setup_sap();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_narrowphase_lanes(shapes_batch* b, int32_t lanes) {
+  if (!b || (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32))
+    return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->np_lanes = lanes;
+    b->invalidate_graphs();
     return SHAPES_OK;
   });
 }

@@ -1652,6 +1652,161 @@ __global__ void k_narrowphase(Dev d) {
   }
 }
 
+/* ---- L lanes per pair: the axis search spread over lanes, shuffle-reduced ----
+ * The same contacts as k_narrowphase, with each pair's separating-axis search
+ * split over L lanes of a warp (L = 32: one warp per pair; 32 / L pairs per
+ * warp).  Lane e of a pair's lanes tests axes e, e + L, ... of both hulls
+ * (sat_axis, unchanged); the lanes then agree, by shuffles, on whether any
+ * axis separates and on each direction's minimum, taken exactly as
+ * min_overlap's fold takes it: the first axis of the least depth, except that
+ * a NaN depth on axis 0 keeps axis 0 and a NaN on any other axis is never
+ * chosen.  The manifold, circles and the writes run on the pair's first
+ * lane.  Selected by shapes_batch_set_narrowphase_lanes. */
+struct AxisBest {
+  uint64_t key; /* okey of the depth; ~0 when the lane holds no eligible axis */
+  int e;        /* axis (kNoAxis when none) */
+  int pen;
+  double dep;
+};
+constexpr int kNoAxis = 0x7fffffff;
+
+__device__ __forceinline__ void axis_take(AxisBest& b, int e, double dep, int pen) {
+  if (nan_bits(dep)) return; /* never the fold's choice except on axis 0 (handled apart) */
+  const uint64_t k = okey(dep);
+  if (k < b.key || (k == b.key && e < b.e)) {
+    b.key = k;
+    b.e = e;
+    b.pen = pen;
+    b.dep = dep;
+  }
+}
+
+template <int L>
+__device__ __forceinline__ void axis_reduce(AxisBest& b) {
+#pragma unroll
+  for (int o = L / 2; o; o >>= 1) {
+    const uint64_t k = __shfl_xor_sync(0xffffffffu, b.key, o, L);
+    const int e = __shfl_xor_sync(0xffffffffu, b.e, o, L);
+    const int pen = __shfl_xor_sync(0xffffffffu, b.pen, o, L);
+    const double dep = __shfl_xor_sync(0xffffffffu, b.dep, o, L);
+    if (k < b.key || (k == b.key && e < b.e)) {
+      b.key = k;
+      b.e = e;
+      b.pen = pen;
+      b.dep = dep;
+    }
+  }
+}
+
+/* One direction of minOverlap over this lane's axes; *sep set when one of
+ * them separates; axis 0's result (on lane 0 of the pair) kept in *d0/*p0. */
+template <int L>
+__device__ __forceinline__ void axes_lane(const HullView& se, const HullView& sp, int sub, AxisBest& best, bool* sep,
+                                          double* d0, int* p0) {
+  for (int e = sub; e < se.nv; e += L) {
+    double dep;
+    int pen;
+    if (!sat_axis(se, e, sp, &dep, &pen)) {
+      *sep = true;
+      continue;
+    }
+    if (e == 0) {
+      *d0 = dep;
+      *p0 = pen;
+    }
+    axis_take(best, e, dep, pen);
+  }
+}
+
+template <int L>
+__global__ void k_narrowphase_lanes(Dev d) {
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  constexpr int G = 32 / L; /* pairs per warp */
+  const int lane = threadIdx.x & 31, sub = lane & (L - 1);
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long n_warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp * G; base < P; base += n_warps * G) { /* warp-uniform */
+    const int i = (int)base + lane / L;
+    const bool live = i < P;
+    const int p = live ? (d.np_perm ? d.np_perm[i] : i) : 0;
+    const int ga = live ? d.pair_a[p] : 0, gb = live ? d.pair_b[p] : 0;
+    HullView a{}, b{};
+    double ra = 0.0, rb = 0.0;
+    if (live) {
+      a = hull_view(d, ga);
+      b = hull_view(d, gb);
+      ra = d.radius ? d.radius[ga] : 0.0;
+      rb = d.radius ? d.radius[gb] : 0.0;
+    }
+    const bool circ = ra > 0.0 || rb > 0.0;
+    AxisBest ab{~0ull, kNoAxis, 0, 0.0}, ba{~0ull, kNoAxis, 0, 0.0};
+    bool sep = false;
+    double d0_ab = 0.0, d0_ba = 0.0;
+    int p0_ab = 0, p0_ba = 0;
+    if (live && !circ) {
+      axes_lane<L>(a, b, sub, ab, &sep, &d0_ab, &p0_ab);
+      axes_lane<L>(b, a, sub, ba, &sep, &d0_ba, &p0_ba);
+    }
+    axis_reduce<L>(ab);
+    axis_reduce<L>(ba);
+    const unsigned group_mask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << (lane & ~(L - 1));
+    sep = (__ballot_sync(0xffffffffu, sep) & group_mask) != 0;
+    if (!live || sub != 0) continue;
+    if (circ) { /* Contact.generateContacts (Contact.hs:22-40), as k_narrowphase */
+      double v[5];
+      int f = 0, fa = 0, fb = 0, flip = 0;
+      bool hit;
+      if (ra > 0.0 && rb > 0.0) {
+        hit = circle_circle(a.wx[0], a.wy[0], ra, b.wx[0], b.wy[0], rb, v);
+      } else if (ra > 0.0) {
+        hit = circle_hull(a.wx[0], a.wy[0], ra, b, &f, v);
+        fb = f;
+      } else {
+        hit = circle_hull(b.wx[0], b.wy[0], rb, a, &f, v);
+        fa = f;
+        flip = 1;
+      }
+      if (hit) {
+        d.slot_feat[2 * p] = fa | (fb << 12) | (flip << 24);
+        double* o = d.slot_val + 5 * (2 * (size_t)p);
+        for (int k = 0; k < 5; ++k) o[k] = v[k];
+      }
+      d.slot_cnt[p] = hit ? 1 : 0;
+      continue;
+    }
+    int cnt = 0;
+    if (!sep) {
+      /* axis 0 with a NaN depth stays the fold's choice */
+      const int e_ab = nan_bits(d0_ab) ? 0 : ab.e, pen_ab = nan_bits(d0_ab) ? p0_ab : ab.pen;
+      const double dep_ab = nan_bits(d0_ab) ? d0_ab : ab.dep;
+      const int e_ba = nan_bits(d0_ba) ? 0 : ba.e, pen_ba = nan_bits(d0_ba) ? p0_ba : ba.pen;
+      const double dep_ba = nan_bits(d0_ba) ? d0_ba : ba.dep;
+      const bool flip = !f_lt(dep_ab, dep_ba);
+      const HullView& se = flip ? b : a;
+      const HullView& sp = flip ? a : b;
+      const int e = flip ? e_ba : e_ab;
+      const int pen = flip ? pen_ba : pen_ab;
+      int idx[2];
+      double xs[2], ys[2];
+      cnt = manifold(se, e, sp, pen, idx, xs, ys);
+      const double nx = se.nx[e], ny = se.ny[e];
+      const double vdot = se.wx[e] * nx + se.wy[e] * ny;
+      for (int q = 0; q < cnt; ++q) {
+        const int fa = flip ? idx[q] : e;
+        const int fb = flip ? e : idx[q];
+        d.slot_feat[2 * p + q] = fa | (fb << 12) | ((flip ? 1 : 0) << 24);
+        double* v = d.slot_val + 5 * (2 * (size_t)p + q);
+        v[0] = nx;
+        v[1] = ny;
+        v[2] = xs[q];
+        v[3] = ys[q];
+        v[4] = vdot - (xs[q] * nx + ys[q] * ny);
+      }
+    }
+    d.slot_cnt[p] = cnt;
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* A8-A9 constraint build + warm-start lookup                                 */
 /* ------------------------------------------------------------------------ */
