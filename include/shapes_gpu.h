@@ -339,6 +339,13 @@ int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies);
  * exactly, including which axis wins among equal or NaN depths). */
 int shapes_batch_set_narrowphase_lanes(shapes_batch* b, int32_t lanes);
 
+/* The order-preserving solve of large worlds waits for each update's
+ * predecessors by polling completion counts; a lane that polls one dependency
+ * more than `polls` times (default 2^22, restored by 0) makes the step return
+ * SHAPES_E_TIMEOUT, with the state of the steps that ran partly solved.  The
+ * next run starts with the flag clear.  No counterpart in the reference. */
+int shapes_batch_set_wait_limit(shapes_batch* b, int64_t polls);
+
 /* Per-stage device timing.  While enabled, CUDA events on the handle's stream
  * bracket each stage of every step; get_profile returns the accumulated
  * milliseconds and kernel launches per stage since profiling was enabled or

@@ -181,6 +181,7 @@ SIGNATURES = [
     ("shapes_batch_get_samples", ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _lp]),
     ("shapes_batch_set_sweep_prune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_set_narrowphase_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("shapes_batch_set_wait_limit", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]
@@ -495,6 +496,11 @@ class Batch:
         """Grid worlds of at least `min_bodies` bodies pair their small bodies by
         sweep and prune (with incremental pairs off); 0 turns it off."""
         check(lib().shapes_batch_set_sweep_prune(self._h, int(min_bodies)), "shapes_batch_set_sweep_prune")
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls of one dependency before the large-world ordered solve gives up with
+        SHAPES_E_TIMEOUT (0 restores the default, 2**22)."""
+        check(lib().shapes_batch_set_wait_limit(self._h, int(polls)), "shapes_batch_set_wait_limit")
 
     def set_narrowphase_lanes(self, lanes: int) -> None:
         """Lanes per pair in the narrowphase: 1 (default, a thread per pair) or 2-32

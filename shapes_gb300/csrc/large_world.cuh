@@ -309,13 +309,15 @@ __device__ __forceinline__ int lw_want(int4 e, int pass) { return pass == 0 ? e.
  * update separately).  A lane whose row is finished takes the next ticket on
  * the following pass (one atomic per warp).  The earliest unfinished ticket
  * finds its dependencies met on its warp's next poll, so the solve always
- * progresses; a lane that polls one dependency kPollLimit times raises the
+ * progresses; a lane that polls one dependency poll_limit times (default
+ * kPollLimit, shapes_batch_set_wait_limit) raises the
  * timeout flag and every warp returns. */
 constexpr int kOrderedThreads = 128;
 constexpr long long kPollLimit = 1ll << 22; /* polls of one dependency before giving up */
 constexpr int kOrderedBlocksPerSM = 2;
 
-__global__ void __launch_bounds__(kOrderedThreads) k_lw_ordered(Dev d, LW w, int iterations, int warm_start) {
+__global__ void __launch_bounds__(kOrderedThreads) k_lw_ordered(Dev d, LW w, int iterations, int warm_start,
+                                                                  long long poll_limit) {
   if (d.counters[kCntOverflow]) return;
   lw_range(w);
   const unsigned kAll = 0xffffffffu;
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(kOrderedThreads) k_lw_ordered(Dev d, LW w, int
         }
         has = false;
       }
-    } else if (has && ++polls > kPollLimit) {
+    } else if (has && ++polls > poll_limit) {
       atomicExch(&w.ctl[1], 1ull);
     }
     if (!__any_sync(kAll, ready)) {

@@ -155,6 +155,7 @@ struct shapes_batch {
   /* sweep and prune for the small bodies of large grid worlds (incremental pairs off) */
   int32_t sap_min_bodies = 0; /* 0: off */
   int32_t np_lanes = 1;       /* lanes per pair in the narrowphase (1: k_narrowphase) */
+  long long lw_poll_limit = shapes::kPollLimit; /* ordered large-world solve: polls of one dependency */
   bool any_sap = false;
   int32_t n_sap_buckets = 0;
   uint8_t* world_sap = nullptr;
@@ -886,7 +887,7 @@ struct shapes_batch {
         shapes::k_lw_gravity<<<grid_for(w.nb, 256), 256, 0, stream>>>(d, w, cfg.accel_x, cfg.accel_y, cfg.dt);
       if (ordered) {
         shapes::k_lw_ordered<<<kSMs * shapes::kOrderedBlocksPerSM, shapes::kOrderedThreads, 0, stream>>>(
-            d, w, cfg.iterations, cfg.warm_start);
+            d, w, cfg.iterations, cfg.warm_start, lw_poll_limit);
         return;
       }
       shapes::k_lw_color_init<<<grid_for(cap, 256), 256, 0, stream>>>(w);
@@ -2880,6 +2881,16 @@ int shapes_batch_set_sweep_prune(shapes_batch* b, int32_t min_bodies) {
     b->sap_min_bodies = min_bodies;
     b->invalidate_graphs();
     b->setup_sap();
+    return SHAPES_OK;
+  });
+}
+
+int shapes_batch_set_wait_limit(shapes_batch* b, int64_t polls) {
+  if (!b || polls < 0) return SHAPES_E_INVALID_ARG;
+  return guarded([&]() -> int {
+    ck(cudaStreamSynchronize(b->stream), "sync");
+    b->lw_poll_limit = polls ? (long long)polls : shapes::kPollLimit;
+    b->invalidate_graphs();
     return SHAPES_OK;
   });
 }

@@ -70,3 +70,27 @@ def test_large_world_coloured_sweep():
     assert not np.array_equal(o_body["vel_y"], c_body["vel_y"])  # a different order
     assert np.isfinite(c_res) and np.isfinite(o_res)
     assert c_depth <= 3.0 * max(o_depth, 0.02), (o_depth, c_depth)
+
+
+def test_ordered_wait_limit_reports_timeout_and_recovers():
+    """A wait limit of one poll cannot be met once the pile's dependency chains
+    form: the step returns SHAPES_E_TIMEOUT instead of hanging, every warp of
+    the solve returns, and the context stays usable (the same handle steps
+    again with the default limit, and a new handle reproduces the oracle)."""
+    sc = scenes.container_world(n=6000, width=90.0, steps=1)
+    b = batch_from_scene(sc)
+    b.step(_cfg(sc), 200)
+    assert b.stats()["contacts"] > 300
+    b.set_wait_limit(1)
+    with pytest.raises(_lib.ShapesError) as e:
+        b.step(_cfg(sc), 3)
+    assert e.value.status == _lib.SHAPES_E_TIMEOUT
+    b.set_wait_limit(0)
+    b.step(_cfg(sc), 2)  # the flag is cleared per run: no error, state no longer the oracle's
+    b.close()
+    fresh = batch_from_scene(sc)
+    ow = oracle_worlds(sc)
+    fresh.step(_cfg(sc), 80)
+    step_oracles(ow, sc, 80)
+    compare_bodies(fresh, ow, sc, "after a timed-out solve")
+    fresh.close()
