@@ -54,6 +54,10 @@ def test_strerror_and_argument_errors(built):
                                    None) == _lib.SHAPES_E_INVALID_ARG
     assert L.shapes_batches_run_io(none, 1, ctypes.byref(cfg), 1, bodies, _lib.STEP_CALLBACK(),
                                    None) == _lib.SHAPES_E_INVALID_ARG
+    # per-handle options refuse a missing handle
+    assert L.shapes_batch_set_narrowphase_lanes(None, 32) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batch_set_wait_limit(None, 1) == _lib.SHAPES_E_INVALID_ARG
+    assert L.shapes_batch_set_sweep_prune(None, 1) == _lib.SHAPES_E_INVALID_ARG
 
 
 def test_product_does_not_import_oracle():

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from shapes_gb300 import scenes
+from shapes_gb300 import _lib, scenes
 from tests.parity import batch_from_scene, compare_bodies, compare_collision, config_of, oracle_worlds, step_oracles
 
 pytestmark = pytest.mark.gpu
@@ -67,4 +67,15 @@ def test_switching_lanes_mid_run():
         b.step(cfg, 25)
     step_oracles(ow, sc, 75)
     compare_bodies(b, ow, sc, "lanes switched mid-run")
+    b.close()
+
+
+def test_lane_counts_other_than_powers_of_two_are_refused():
+    b = batch_from_scene(scenes.batched_mixed(n_worlds=2, n_bodies=32))
+    for bad in (0, 3, 64, -1):
+        with pytest.raises(_lib.ShapesError) as e:
+            b.set_narrowphase_lanes(bad)
+        assert e.value.status == _lib.SHAPES_E_INVALID_ARG
+    with pytest.raises(_lib.ShapesError):
+        b.set_wait_limit(-1)
     b.close()
