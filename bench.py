@@ -329,16 +329,27 @@ def broadphase_setup(b):
         b.set_narrowphase_lanes(NP_LANES)
 
 
+def apply_packing(b, tuned):
+    """The solver packing (worlds per group, threads, warps per group, world order,
+    parallel levels, heavy groups spread, target bodies per group); groups close at
+    the target body count when it is non-zero, else at the world count."""
+    if tuned[6]:
+        b.set_launch(tuned[6], tuned[1])
+        b.set_group_warps(tuned[2])
+    else:
+        b.set_launch_groups(*tuned[:3])
+    b.set_parallel_levels(tuned[4])
+    b.set_spread_heavy(tuned[5])
+
+
 def new_batch(_lib, scene, stream, tuned=None):
     b = _lib.Batch(scene["world_body_offsets"], scene["bodies"], scene["vert_offsets"], scene["local_xy"],
                    scene.get("shape_kind"))
     b.set_stream(stream.cuda_stream)
     broadphase_setup(b)
     if tuned:
-        b.set_launch_groups(*tuned[:3])
         b.set_world_order(tuned[3])
-        b.set_parallel_levels(tuned[4])
-        b.set_spread_heavy(tuned[5])
+        apply_packing(b, tuned)
     return b
 
 
@@ -365,9 +376,7 @@ class Lanes:
             b.set_stream(st.cuda_stream)
             broadphase_setup(b)
             if tuned:
-                b.set_launch_groups(*tuned[:3])
-                b.set_parallel_levels(tuned[4])
-                b.set_spread_heavy(tuned[5])
+                apply_packing(b, tuned)
             b.set_world_order(np.arange(len(sc["world_body_offsets"]) - 1, dtype=np.int32))
             self.handles.append(b)
         assert sum(len(w) for w in self.worlds) == W
@@ -567,13 +576,14 @@ def run_ours(args, rank, world, local):
         wpg, thr, gw = vals[:3]
         par = bool(vals[3]) if len(vals) > 3 else True
         spread = bool(vals[4]) if len(vals) > 4 else False
+        target = vals[5] if len(vals) > 5 else 0
         tuned = (wpg, thr, gw, np.argsort(-np.diff(scene["world_body_offsets"]), kind="stable").astype(np.int32), par,
-                 spread)
+                 spread, target)
     elif not args.no_tune:
         t = new_batch(_lib, scene, stream)
         t.step(cfg_for(plain_it, False), args.tune_after)
         tuned = t.autotune(cfg_for(plain_it, False), args.tune_steps) + (t.world_order(), t.parallel_levels(),
-                                                                         t.spread_heavy())
+                                                                         t.spread_heavy(), t.group_target())
         t.close()
 
     n_worlds = len(scene["world_body_offsets"]) - 1
@@ -815,7 +825,8 @@ def run_ours(args, rank, world, local):
                                       else "grid, incremental fat-box pair lists" if INCREMENTAL_PAIRS
                                       else "grid, full 3x3 search every frame"),
                        "narrowphase": NP_DESC[NP_LANES],
-                       "solver_packing": {"worlds_per_group": tuned[0], "threads": tuned[1],
+                       "solver_packing": {"worlds_per_group": tuned[0] if not tuned[6] else None,
+                                          "target_bodies_per_group": tuned[6] or None, "threads": tuned[1],
                                           "warps_per_group": tuned[2], "parallel_levels": bool(tuned[4]),
                                           "heavy_groups_spread": bool(tuned[5]),
                                           "world_order": "by size" if np.array_equal(
@@ -1063,7 +1074,8 @@ def main():
     ap.add_argument("--worlds", type=int, default=None, help="override the world count (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="skip the solver-packing autotuner")
     ap.add_argument("--packing", default="", help="fixed solver packing 'worlds_per_group,threads,warps_per_group"
-                    "[,parallel_levels[,spread_heavy]]' (size order) instead of the autotuner")
+                    "[,parallel_levels[,spread_heavy[,target_bodies]]]' (size order) instead of the autotuner; "
+                    "target_bodies > 0 closes groups at that many bodies instead")
     ap.add_argument("--tune-after", type=int, default=120, help="steps run on the tuning copy before tuning")
     ap.add_argument("--tune-steps", type=int, default=30, help="steps per autotuner trial")
     ap.add_argument("--quality-steps", type=int, default=100,

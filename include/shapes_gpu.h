@@ -274,8 +274,13 @@ int shapes_batch_get_parallel_levels(shapes_batch* b, int32_t* enabled);
  * group shares its SM with light ones.  Results do not depend on it. */
 int shapes_batch_set_spread_heavy(shapes_batch* b, int32_t enabled);
 int shapes_batch_get_spread_heavy(shapes_batch* b, int32_t* enabled);
-/* The packing in use (any pointer may be NULL). */
+/* The packing in use (any pointer may be NULL); worlds_per_group is 0 when
+ * groups are packed by body count (shapes_batch_get_group_target). */
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps);
+/* The body count at which groups close (shapes_batch_set_launch; the
+ * autotuner tries such packings for batches of uneven world sizes), 0 when
+ * they are packed by world count. */
+int shapes_batch_get_group_target(shapes_batch* b, int32_t* target_bodies);
 /* The order in which worlds are packed into groups: a permutation of
  * 0..n_worlds-1 (NULL = by body count, largest first, the default).  The
  * autotuner may choose an order by dependency levels; get_world_order reads

@@ -182,6 +182,7 @@ SIGNATURES = [
     ("shapes_batch_set_sweep_prune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_set_narrowphase_lanes", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("shapes_batch_set_wait_limit", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    ("shapes_batch_get_group_target", ctypes.c_int, [ctypes.c_void_p, _ip]),
     ("shapes_strerror", ctypes.c_char_p, [ctypes.c_int]),
     ("shapes_last_error_detail", ctypes.c_char_p, []),
 ]
@@ -369,6 +370,12 @@ class Batch:
         check(lib().shapes_batch_get_launch(self._h, ctypes.byref(wpg), ctypes.byref(thr), ctypes.byref(gw)),
               "shapes_batch_get_launch")
         return wpg.value, thr.value, gw.value
+
+    def group_target(self) -> int:
+        """Body count at which solver groups close (0: packed by world count)."""
+        v = ctypes.c_int32()
+        check(lib().shapes_batch_get_group_target(self._h, ctypes.byref(v)), "shapes_batch_get_group_target")
+        return v.value
 
     def parallel_levels(self) -> bool:
         v = ctypes.c_int32()

@@ -2321,10 +2321,12 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
       return (b->h_world_body_off[a + 1] - b->h_world_body_off[a]) > (b->h_world_body_off[c + 1] - b->h_world_body_off[c]);
     });
     /* (worlds per group, threads per CTA, warps per group, level order,
-     * parallel levels, heavy groups spread) */
-    std::vector<std::array<int, 6>> cands;
-    auto add = [&](int wpg, int thr, int gw, int lo, int par, int spread = 0) {
-      const std::array<int, 6> c{wpg, thr, gw, lo, par, spread};
+     * parallel levels, heavy groups spread, target bodies per group: when
+     * non-zero, groups close at that many bodies instead of at a world
+     * count, so the largest worlds of a ragged batch get groups of their own) */
+    std::vector<std::array<int, 7>> cands;
+    auto add = [&](int wpg, int thr, int gw, int lo, int par, int spread = 0, int target = 0) {
+      const std::array<int, 7> c{wpg, thr, gw, lo, par, spread, target};
       if (wpg >= 1 && wpg <= shapes::kMaxGroupWorlds && std::find(cands.begin(), cands.end(), c) == cands.end())
         cands.push_back(c);
     };
@@ -2338,18 +2340,29 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
             if (par) add(std::min(wpg, W), 32 * gw, gw, lo, par, 1);
           }
     }
+    int32_t min_n = INT32_MAX, max_n = 0;
+    for (int w = 0; w < W; ++w) {
+      const int32_t n = b->h_world_body_off[w + 1] - b->h_world_body_off[w];
+      if (n >= b->large_world_bodies) continue;
+      min_n = std::min(min_n, n);
+      max_n = std::max(max_n, n);
+    }
+    if (max_n > 2 * min_n) /* ragged batches: packings by body count */
+      for (int target : {256, 512, 1024, 2048})
+        for (int gw : {2, 4, 8})
+          for (int par : {0, 1}) add(1, 32 * gw, gw, 0, par, 1, target);
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
     float best = 1e30f;
     const bool par0 = b->parallel_levels, spread0 = b->spread_heavy;
-    std::array<int, 6> best_c{wpg0, thr0, gw0, -1, par0 ? 1 : 0, spread0 ? 1 : 0};
+    std::array<int, 7> best_c{wpg0, thr0, gw0, -1, par0 ? 1 : 0, spread0 ? 1 : 0, tgt0};
     int rc = rc0;
     if (rc0 != SHAPES_OK) cands.clear();
     for (const auto& c : cands) {
       restore_state();
-      b->worlds_per_group_override = c[0];
-      b->target_group_bodies = 0;
+      b->worlds_per_group_override = c[6] ? 0 : c[0];
+      b->target_group_bodies = c[6];
       b->solve_threads = c[1];
       b->group_warps = c[2];
       b->parallel_levels = c[4] != 0;
@@ -2375,8 +2388,8 @@ int shapes_batch_autotune(shapes_batch* b, const shapes_config* cfg, int32_t ste
     cudaEventDestroy(e1);
     restore_state();
     if (rc == SHAPES_OK && best_c[3] >= 0) {
-      b->worlds_per_group_override = best_c[0];
-      b->target_group_bodies = 0;
+      b->worlds_per_group_override = best_c[6] ? 0 : best_c[0];
+      b->target_group_bodies = best_c[6];
       b->solve_threads = best_c[1];
       b->group_warps = best_c[2];
       b->parallel_levels = best_c[4] != 0;
@@ -3010,6 +3023,12 @@ int shapes_batch_set_parallel_levels(shapes_batch* b, int32_t enabled) {
     b->invalidate_graphs();
     return SHAPES_OK;
   });
+}
+
+int shapes_batch_get_group_target(shapes_batch* b, int32_t* target_bodies) {
+  if (!b || !target_bodies) return SHAPES_E_INVALID_ARG;
+  *target_bodies = b->target_group_bodies;
+  return SHAPES_OK;
 }
 
 int shapes_batch_get_launch(shapes_batch* b, int32_t* worlds_per_group, int32_t* threads, int32_t* group_warps) {

@@ -218,6 +218,25 @@ def test_solver_packing_does_not_change_results(target, threads):
     b.close()
 
 
+@pytest.mark.parametrize("target,warps,par", [(256, 4, 0), (512, 2, 1), (1024, 8, 0)])
+def test_cooperative_groups_packed_by_body_count(target, warps, par):
+    """Ragged worlds packed by body count (groups close at `target` bodies, so
+    the largest worlds get groups of their own) on cooperative warps."""
+    sc = scenes.subset_worlds(scenes.batched_columns(n_worlds=64), list(range(24)))
+    b = batch_from_scene(sc)
+    b.set_launch(target, 32 * warps)
+    b.set_group_warps(warps)
+    b.set_parallel_levels(bool(par))
+    b.set_spread_heavy(True)
+    assert b.group_target() == target and b.get_launch()[0] == 0
+    ow = oracle_worlds(sc)
+    cfg = config_of(sc)
+    b.step(cfg, 40)
+    step_oracles(ow, sc, 40)
+    compare_bodies(b, ow, sc, f"packed by {target} bodies on {warps} warps")
+    b.close()
+
+
 def test_cache_checkpoint_resume():
     sc = scenes.stacks_make_scene((8, 8))
     cfg = config_of(sc)
@@ -426,7 +445,9 @@ def test_autotune_keeps_state_and_results():
     before = b.get_bodies()
     k0, l0, _ = b.get_cache()
     wpg, thr, gw = b.autotune(cfg, 3)
-    assert 1 <= wpg <= 32 and gw in (1, 2, 4, 8) and (thr in (32, 64, 128) if gw == 1 else thr == 32 * gw)
+    target = b.group_target()
+    assert (1 <= wpg <= 32) if target == 0 else (wpg == 0 and target > 0)
+    assert gw in (1, 2, 4, 8) and (thr in (32, 64, 128) if gw == 1 else thr == 32 * gw)
     after = b.get_bodies()
     k1, l1, _ = b.get_cache()
     for f in STATE_FIELDS:
