@@ -21,8 +21,9 @@ value      body-steps/s with the state resident in HBM: CUDA events on the
            library's stream around K steps replayed from CUDA graphs, max
            over ranks.
 e2e        the same steps through the public C ABI with host buffers: every
-           step uploads the body state from pinned host memory, steps, and
-           reads the state back.
+           step uploads the body state (all ten arrays) from pinned host
+           memory, steps, and reads back the six arrays a step writes
+           (velocities and pose).
 roofline   the solver kernel (the dominant one), from a separate profiled
            pass: algorithmic bytes per launch over its average launch time
            against the measured HBM copy bandwidth; `fp64` holds its FP64-pipe
@@ -836,7 +837,7 @@ def run_ours(args, rank, world, local):
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * 8 * n_bodies,
-                    "d2h_bytes_per_step": 10 * 8 * n_bodies},
+                    "d2h_bytes_per_step": 6 * 8 * n_bodies},
             "gpu_launches": int(round(launches_per_step * args.steps * lanes)),
             "clocks": clocks.summary(),
             "stages_ms_per_step": {k: v[0] / prof_steps for k, v in prof.items()},

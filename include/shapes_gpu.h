@@ -173,8 +173,10 @@ typedef int (*shapes_step_callback)(void* user, int32_t handle_index, int32_t st
 
 /* nsteps steps of n handles whose body state lives in caller host memory:
  * every step of handle k uploads and checks state[k] (as
- * shapes_batch_set_bodies), steps, writes the result back into state[k] and
- * waits for it, then calls on_step (may be NULL).  Each handle runs its steps
+ * shapes_batch_set_bodies), steps, writes the result back into state[k] (the
+ * arrays a step changes: vel_x, vel_y, rot_vel, pos_x, pos_y, rot; the inverse
+ * masses and material in state[k] are the values just uploaded) and waits for
+ * it, then calls on_step (may be NULL).  Each handle runs its steps
  * in order on a host thread of its own, so one handle's copies and host turn
  * overlap the others' steps.  Pinned buffers are resolved once per call and
  * copied by a kernel over the host link.  Returns the first error; a handle

@@ -1233,11 +1233,13 @@ struct shapes_batch {
     shapes::k_integrate_pose<<<grid_for(N, 128), 128, 0, stream>>>(d, 0.0, 0, body_changed);
     ck(cudaGetLastError(), "launch");
   }
-  void io_download(shapes_bodies* out, double* const* mapped = nullptr);
+  /* The first `fields` body arrays (10: all; kStepFields: velocities and pose,
+   * the only ones a step writes) into the caller's arrays. */
+  void io_download(shapes_bodies* out, double* const* mapped = nullptr, int fields = 10);
   /* After an io step was enqueued: waits, and on refused input undoes the
    * step (SHAPES_E_NAN); otherwise finishes it, re-running the staged input
    * alone after a buffer regrowth. */
-  int io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out = nullptr);
+  int io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out = nullptr, int fields = 10);
 
   /* One call of `nsteps` steps (or one collide when !solve) in three parts,
    * so that several handles can have their steps in flight at once
@@ -1582,6 +1584,10 @@ double* const* body_ptrs(const shapes_bodies* b, double* out[10]) {
   return out;
 }
 
+/* Body arrays a step writes: vel_x, vel_y, rot_vel, pos_x, pos_y, rot (the
+ * first six of the shapes_bodies order); inverse masses and material stay. */
+constexpr int kStepFields = 6;
+
 /* Strictly convex, counter-clockwise, no zero-length edge. */
 int check_hull(int nv, const double* xy) {
   if (nv < 3) return SHAPES_E_INVALID_ARG;
@@ -1832,9 +1838,9 @@ int shapes_batches_run_io(shapes_batch* const* bs, int32_t n, const shapes_confi
         b->io_upload(&state[k], mp);
         b->io_commit();
         b->enqueue_one(*cfg, true);
-        b->io_download(&state[k], mp);
+        b->io_download(&state[k], mp, kStepFields); /* the other four arrays are the ones just uploaded */
         b->enqueue_end();
-        const int r = b->io_finish(*cfg, &state[k], mp);
+        const int r = b->io_finish(*cfg, &state[k], mp, kStepFields);
         if (r != SHAPES_OK) return r;
         if (on_step && on_step(user, k, s) != 0) break;
       }
@@ -1887,12 +1893,13 @@ static bool mapped_host10(double* const host[10], double* dev[10]) {
   return true;
 }
 
-static dim3 copy10_grid(int n) {
+static dim3 copy10_grid(int n, int fields = 10) {
   const int64_t per_block = 256 * shapes::kCopy10PerThread;
-  return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, 1024)), 10);
+  return dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((n + per_block - 1) / per_block, 1024)),
+              (unsigned)fields);
 }
 
-int shapes_batch::io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out) {
+int shapes_batch::io_finish(const shapes_config& cfg, shapes_bodies* out, double* const* mapped_out, int fields) {
   ck(cudaStreamSynchronize(stream), "step");
   if (run_counters[shapes::kCntBadInput]) { /* refused: undo the step taken on the old state */
     cache_buf = run_saved_cache_buf;
@@ -1907,7 +1914,7 @@ int shapes_batch::io_finish(const shapes_config& cfg, shapes_bodies* out, double
     enqueue_begin(true);
     io_commit();
     enqueue_one(cfg, true);
-    io_download(out, mapped_out);
+    io_download(out, mapped_out, fields);
     enqueue_end();
     r = finish(cfg, true);
   }
@@ -1937,7 +1944,7 @@ void shapes_batch::io_upload(const shapes_bodies* in, double* const* mapped) {
   ck(cudaGetLastError(), "launch");
 }
 
-void shapes_batch::io_download(shapes_bodies* out, double* const* mapped) {
+void shapes_batch::io_download(shapes_bodies* out, double* const* mapped, int fields) {
   double* bp[10];
   body_ptrs(out, bp);
   double* dp[10];
@@ -1948,10 +1955,10 @@ void shapes_batch::io_download(shapes_bodies* out, double* const* mapped) {
       p.src[k] = body[k];
       p.dst[k] = dp[k];
     }
-    shapes::k_copy10<<<copy10_grid(N), 256, 0, stream>>>(p, N, nullptr);
+    shapes::k_copy10<<<copy10_grid(N, fields), 256, 0, stream>>>(p, N, nullptr);
     ck(cudaGetLastError(), "launch");
   } else {
-    for (int k = 0; k < 10; ++k)
+    for (int k = 0; k < fields; ++k)
       ck(cudaMemcpyAsync(bp[k], body[k], sizeof(double) * N, cudaMemcpyDeviceToHost, stream), "download");
   }
 }

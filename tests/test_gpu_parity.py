@@ -671,6 +671,8 @@ def test_batches_run_io_matches_separate_calls(pinned):
         for f in STATE_FIELDS:
             assert_bits_equal(keep[k][f].numpy(), want[f], f"run_io handle {k} {f}")
             assert_bits_equal(hs[k].get_bodies()[f], want[f], f"run_io device state {k} {f}")
+        for f in ("inv_mass_lin", "inv_mass_rot", "mu", "bounce"):  # uploaded, never written back
+            assert_bits_equal(keep[k][f].numpy(), want[f], f"run_io host {k} {f}")
 
     def poison(k, s):
         if k == 2 and s == 1:
