@@ -191,7 +191,8 @@ enum {
 };
 
 /* Narrowphase work classes: (min(nv_a, 9) - 3) * 7 + (min(nv_b, 9) - 3). */
-constexpr int kNpClasses = 49;
+constexpr int kNpHullClasses = 49;            /* hull pairs by vertex counts 3..9+ each */
+constexpr int kNpClasses = kNpHullClasses + 15; /* then circle-circle, circle-hull, hull-circle */
 
 /* Flags any non-finite value among n bodies' ten state arrays. */
 __global__ void k_check_finite(const double* a0, const double* a1, const double* a2, const double* a3,
@@ -1530,13 +1531,19 @@ __device__ bool circle_hull(double ox, double oy, double r, const HullView& hull
 
 /* Pairs are processed grouped by the vertex counts of their two hulls, so
  * that the lanes of a warp run SAT loops of the same trip counts (one thread
- * per pair, the warp pays for its longest loop).  The grouping is a
- * permutation of the processing order only: every pair still writes its own
- * slots, so the results do not depend on it. */
+ * per pair, the warp pays for its longest loop), and pairs with a circle
+ * (circle-circle, or GJK against a hull of a given vertex count) apart from
+ * them, so that no warp runs both the SAT and the circle code.  The grouping
+ * is a permutation of the processing order only: every pair still writes its
+ * own slots, so the results do not depend on it. */
 __device__ __forceinline__ int np_class(const Dev& d, int p) {
   const int ga = d.pair_a[p], gb = d.pair_b[p];
   const int na = max(3, min(d.vert_off[ga + 1] - d.vert_off[ga], 9));
   const int nb = max(3, min(d.vert_off[gb + 1] - d.vert_off[gb], 9));
+  const bool ca = d.radius && d.radius[ga] > 0.0, cb = d.radius && d.radius[gb] > 0.0;
+  if (ca && cb) return kNpHullClasses;
+  if (ca) return kNpHullClasses + 1 + (nb - 3);
+  if (cb) return kNpHullClasses + 8 + (na - 3);
   return (na - 3) * 7 + (nb - 3);
 }
 
