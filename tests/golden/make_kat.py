@@ -24,6 +24,31 @@ K2  OS.contact testOptBoxes (shapes/bench/Physics/Contact/Benchmark.hs:16-30):
       ((1,2), Flip (n=(0,-1), p=(0,2), d=0)), ((0,2), Flip (n=(0,-1), p=(2,2), d=0)).
 K3  length (unorderedPairs n) == n(n-1)/2 for n in [0, 30]
     (shapes/test/Physics/Broadphase/AabbSpec.hs:8-16).
+K4  Circle.contact (Circle (-1,0) 1.1) (Circle (1,0) 1.1)
+    (shapes/bench/Physics/Contact/Circle/Benchmark.hs:8-11; Contact/Circle.hs:27-56):
+    ab = (2, 0), rab = 1.1 + 1.1 = 2.2000000000000002, rab^2 = 4.840000000000001 >= 4,
+    |ab| = 2, n = (1, 0); a' = 1.1 n + (-1, 0) = (0.10000000000000009, 0),
+    b' = -1.1 n + (1, 0) = (-0.10000000000000009, 0) (the y sum -0 + 0 is +0), so the
+    centre is ((a' + b') / 2) = (0, 0) and the depth 2.2000000000000002 - 2 =
+    0.20000000000000018.  Keyed (0, 0), Same (Contact.hs:25-29).
+K5  GJK.closestSimplex (makeOptBox 0 0 1.9 1.9) p for the three points of
+    shapes/bench/Physics/Contact/GJK/Benchmark.hs:10-17, each taken through
+    CircleVsHull.generateContacts with a circle of radius 0.1 centred on p (the
+    circle penetrates; Contact.hs:30-34 keys it (0, hull feature), Same).  The box's
+    vertices are (+-0.95, +-0.95) counter-clockwise from (0.95, 0.95) (1.9 / 2 =
+    0.95).  support returns the first vertex of largest projection (ConvexHull.hs:124-128).
+    p = (1, 1): d = p - v0 = (0.05.., 0.05..), support v0 = the simplex's own vertex, so
+      the search stops at Simplex1 v0: the point v0, b = p - v0, |b| = sqrt(2) 0.05.. ,
+      normal -(b/|b|) = (-0.7071067811865475, -0.7071067811865475), depth 0.1 - |b| =
+      0.029289321881345184, feature 0.
+    p = (0, 1): d = (-0.95, 0.05..), support v1; Simplex2 (v1, v0); ab = (1.9, 0) and
+      ao = (0.95, 0.05..) point the same way, next d = (ab x ao) x ab = (-0, 0.18..);
+      support v0 (v1 ties, not strictly larger): a repeat, the search stops at
+      Simplex2 (v1, v0).  closestAlong: a = v1, u = (1, 0), t = 0.95, point (0, 0.95);
+      b = (0, 0.05..), normal (-0, -1), depth 0.1 - 0.05.. = 0.04999999999999996, feature 1.
+    p = (0, 0.9): d = (-0.95, -0.05..), support v2; Simplex2 (v2, v0), next d points
+      to (-, +), support v1; Simplex3 (v1, v2, v0) encloses p (neither abc x ac nor
+      ab x abc points toward p): no contact.
 """
 import json
 from pathlib import Path
@@ -46,6 +71,24 @@ KAT = {
         ],
     },
     "K3": {"n_max": 30},
+    "K4": {
+        "a": {"center": [-1.0, 0.0], "radius": 1.1},
+        "b": {"center": [1.0, 0.0], "radius": 1.1},
+        "contact": {"features": [0, 0], "flip": 0, "normal": [1.0, 0.0], "point": [0.0, 0.0],
+                    "depth": 0.20000000000000018},
+    },
+    "K5": {
+        "box": {"center": [0.0, 0.0], "size": [1.9, 1.9]},
+        "radius": 0.1,
+        "cases": [
+            {"center": [1.0, 1.0], "contact": {"features": [0, 0], "flip": 0,
+                                               "normal": [-0.7071067811865475, -0.7071067811865475],
+                                               "point": [0.95, 0.95], "depth": 0.029289321881345184}},
+            {"center": [0.0, 1.0], "contact": {"features": [0, 1], "flip": 0, "normal": [-0.0, -1.0],
+                                               "point": [0.0, 0.95], "depth": 0.04999999999999996}},
+            {"center": [0.0, 0.9], "contact": None},
+        ],
+    },
 }
 
 if __name__ == "__main__":

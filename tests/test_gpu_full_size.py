@@ -145,6 +145,20 @@ def test_k2_box_contact_fixture_on_gpu():
         assert list(gv[:2]) == want["normal"] and list(gv[2:4]) == want["point"] and gv[4] == want["depth"]
 
 
+def test_k4_k5_circle_fixtures_on_gpu():
+    """Circle.contact on the circle fixture, and circle-hull contacts over the
+    three GJK.closestSimplex fixtures (a vertex, an edge, an enclosed point),
+    against the hand-derived answers, bit for bit."""
+    from tests.test_oracle import check_circle_contact, circle_scenes
+
+    for k, (sc, want) in enumerate(circle_scenes()):
+        bt = batch_from_scene(sc)
+        bt.collide()
+        keys, vals, _ = bt.get_contacts()
+        bt.close()
+        check_circle_contact(np.asarray(keys).reshape(-1, 5), np.asarray(vals).reshape(-1, 5), want, f"case {k}")
+
+
 def test_static_body_negative_zero_velocity_is_kept():
     """The documented difference: the reference adds (J lambda) * 0 to a static
     body's velocity (Constraint.hs:197-204), which turns a -0.0 component into +0.0;

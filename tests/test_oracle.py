@@ -1,6 +1,6 @@
 """The oracle pinned against the reference's fixtures (CPU only).
 
-K1/K2/K3 are known answers for the reference's own bench/test fixtures
+K1-K5 are known answers for the reference's own bench/test fixtures
 (tests/golden/kat.json, derived by hand from the reference source); the Grid
 restatement checks that the step's Grid broadphase (Grid.hs) and the Aabb
 pair list the oracle produces are the same list.
@@ -48,6 +48,45 @@ def test_k2_box_contact(O):
         assert list(got_v[:2]) == want["normal"]
         assert list(got_v[2:4]) == want["point"]
         assert got_v[4] == want["depth"]
+
+
+def _bits(x):
+    return np.asarray(x, dtype=np.float64).view(np.int64).tolist()
+
+
+def circle_scenes():
+    """K4 (two circles) and the K5 cases (a circle against a box): the penetrated
+    shape is body 0, the penetrator body 1, so each world's one pair is (1, 0)."""
+    k4, k5 = kat()["K4"], kat()["K5"]
+    out = []
+    b_ = scenes.SceneBuilder()
+    b_.add_circle(k4["b"]["radius"], tuple(k4["b"]["center"]))
+    b_.add_circle(k4["a"]["radius"], tuple(k4["a"]["center"]))
+    out.append((b_.build(dt=1 / 60, accel=(0.0, 0.0)), k4["contact"]))
+    for case in k5["cases"]:
+        b_ = scenes.SceneBuilder()
+        b_.add(scenes.rectangle_vertices(*k5["box"]["size"]), tuple(k5["box"]["center"]))
+        b_.add_circle(k5["radius"], tuple(case["center"]))
+        out.append((b_.build(dt=1 / 60, accel=(0.0, 0.0)), case["contact"]))
+    return out
+
+
+def check_circle_contact(keys, vals, want, what):
+    if want is None:
+        assert len(keys) == 0, what
+        return
+    assert len(keys) == 1, what
+    assert list(keys[0][:2]) == [1, 0] and list(keys[0][2:4]) == want["features"] and keys[0][4] == want["flip"], what
+    got = [vals[0][0], vals[0][1], vals[0][2], vals[0][3], vals[0][4]]
+    assert _bits(got) == _bits(want["normal"] + want["point"] + [want["depth"]]), (what, got)
+
+
+def test_k4_k5_circle_contacts(O):
+    for k, (sc, want) in enumerate(circle_scenes()):
+        w = O.world_from_scene(sc)
+        w.collide()
+        keys, vals = w.contacts()
+        check_circle_contact(np.asarray(keys).reshape(-1, 5), np.asarray(vals).reshape(-1, 5), want, f"case {k}")
 
 
 def test_k3_unordered_pairs_count(O):
