@@ -229,6 +229,7 @@ struct shapes_batch {
   int results_buf = 0; /* buffer holding the last pairs/contacts results */
   bool have_results = false;
   int32_t* c_ga = nullptr;
+  int32_t* c_slot = nullptr; /* [contact_cap] slot of each contact */
   int32_t* c_gb = nullptr;
   uint8_t* c_flip = nullptr;
   uint8_t* c_hit = nullptr;
@@ -531,6 +532,7 @@ struct shapes_batch {
     d.slot_val = slot_val;
     d.c_key = c_key[write_buf];
     d.c_ga = c_ga;
+    d.c_slot = c_slot;
     d.c_gb = c_gb;
     d.c_flip = c_flip;
     d.c_hit = c_hit;
@@ -597,7 +599,7 @@ struct shapes_batch {
     dfree(np_perm);
     np_perm = nullptr;
     for (int k = 0; k < 2; ++k) { dfree(c_key[k]); dfree(lam[k]); }
-    dfree(c_ga); dfree(c_gb); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
+    dfree(c_ga); dfree(c_gb); dfree(c_slot); dfree(c_flip); dfree(c_hit); dfree(c_val); dfree(con);
     dfree(c_pred); dfree(c_lvl);
     c_pred = nullptr;
     c_lvl = nullptr;
@@ -617,7 +619,7 @@ struct shapes_batch {
     slot_val = nullptr;
     c_key[0] = c_key[1] = nullptr;
     lam[0] = lam[1] = nullptr;
-    c_ga = c_gb = nullptr;
+    c_ga = c_gb = c_slot = nullptr;
     c_flip = c_hit = nullptr;
     c_val = nullptr;
     con = nullptr;
@@ -661,6 +663,7 @@ struct shapes_batch {
       lam[k] = dalloc<double>(2 * (size_t)contact_cap, "cudaMalloc contacts");
     }
     c_ga = dalloc<int32_t>(contact_cap, "cudaMalloc contacts");
+    c_slot = dalloc<int32_t>(contact_cap, "cudaMalloc contacts");
     c_gb = dalloc<int32_t>(contact_cap, "cudaMalloc contacts");
     c_flip = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
     c_hit = dalloc<uint8_t>(contact_cap, "cudaMalloc contacts");
@@ -1112,9 +1115,10 @@ struct shapes_batch {
     });
     scan(slot_cnt, pair_cap, counters + shapes::kCntPairs, slot_off);
     stage(6, 1, [&]() { shapes::k_world_contact_offsets<<<grid_for(W + 1, 128), 128, 0, stream>>>(d); });
-    stage(2, 1, [&]() {
-      shapes::k_build<<<grid_for(2LL * pair_cap, 128), 128, 0, stream>>>(d, cfg.dt, cfg.baumgarte, cfg.slop,
-                                                                           cfg.warm_start, solve ? 1 : 0);
+    stage(2, 2, [&]() {
+      shapes::k_contact_slots<<<grid_for(2LL * pair_cap, 256), 256, 0, stream>>>(d);
+      shapes::k_build<<<grid_for(contact_cap, 128), 128, 0, stream>>>(d, cfg.dt, cfg.baumgarte, cfg.slop,
+                                                                      cfg.warm_start, solve ? 1 : 0);
     });
     if (!solve) return;
     if (learn || collect) {

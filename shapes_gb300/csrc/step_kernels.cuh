@@ -131,6 +131,7 @@ struct Dev {
   double* slot_val;    /* [2*pair_cap*5] nx ny px py depth */
   uint64_t* c_key;     /* [contact_cap] packed world-local key */
   int32_t* c_ga;       /* [contact_cap] */
+  int32_t* c_slot;     /* [contact_cap] each contact's slot t = 2 pair + s (k_contact_slots), or null */
   int32_t* c_gb;       /* [contact_cap] */
   uint8_t* c_flip;     /* [contact_cap] */
   uint8_t* c_hit;      /* [contact_cap] kInfo* bits */
@@ -1843,14 +1844,34 @@ __global__ void k_world_contact_offsets(Dev d) {
  * descending key lists pairs each new key with an equal old key exactly when
  * one exists, which a binary search over the world's old entries finds.
  * `build_solver` = 0 compacts contacts only (collide). */
-__global__ void k_build(Dev d, double dt, double beta, double slop, int warm_start, int build_solver) {
+/* The slot of every contact, so that k_build's threads take contacts rather
+ * than slots: about half the slots of a settled pile are empty (separated
+ * pairs, pairs with one contact), and an idle lane still costs its warp's FP64
+ * instructions. */
+__global__ void k_contact_slots(Dev d) {
   const int P = min((int)d.counters[kCntPairs], d.pair_cap);
   const int C = (int)d.counters[kCntContacts];
   if (C > d.contact_cap) return;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * P; t += gridDim.x * blockDim.x) {
     const int p = t >> 1, s = t & 1;
-    if (s >= d.slot_cnt[p]) continue;
-    const int c = d.slot_off[p] + s;
+    if (s < d.slot_cnt[p]) d.c_slot[d.slot_off[p] + s] = t;
+  }
+}
+
+__global__ void k_build(Dev d, double dt, double beta, double slop, int warm_start, int build_solver) {
+  const int P = min((int)d.counters[kCntPairs], d.pair_cap);
+  const int C = (int)d.counters[kCntContacts];
+  if (C > d.contact_cap) return;
+  const int n = d.c_slot ? C : 2 * P; /* contacts (k_contact_slots ran), else slots */
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int t = i, c = i;
+    if (d.c_slot) {
+      t = d.c_slot[i];
+    } else {
+      if ((t & 1) >= d.slot_cnt[t >> 1]) continue;
+      c = d.slot_off[t >> 1] + (t & 1);
+    }
+    const int p = t >> 1;
     const int ga = d.pair_a[p], gb = d.pair_b[p];
     const int wld = d.body_world[ga];
     const int off = d.world_body_off[wld];
