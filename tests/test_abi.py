@@ -58,6 +58,8 @@ def test_strerror_and_argument_errors(built):
     assert L.shapes_batch_set_narrowphase_lanes(None, 32) == _lib.SHAPES_E_INVALID_ARG
     assert L.shapes_batch_set_wait_limit(None, 1) == _lib.SHAPES_E_INVALID_ARG
     assert L.shapes_batch_set_sweep_prune(None, 1) == _lib.SHAPES_E_INVALID_ARG
+    v = ctypes.c_int32()
+    assert L.shapes_batch_get_group_target(None, ctypes.byref(v)) == _lib.SHAPES_E_INVALID_ARG
 
 
 def test_product_does_not_import_oracle():
