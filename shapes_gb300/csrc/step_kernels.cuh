@@ -1706,8 +1706,9 @@ __device__ __forceinline__ void axis_reduce(AxisBest& b) {
   }
 }
 
-/* One direction of minOverlap over this lane's axes; *sep set when one of
- * them separates; axis 0's result (on lane 0 of the pair) kept in *d0/*p0. */
+/* One direction of minOverlap over this lane's axes: sep is set when one of
+ * them separates; axis 0's depth and penetrator (on lane 0 of the pair) are
+ * kept in d0 and p0. */
 template <int L>
 __device__ __forceinline__ void axes_lane(const HullView& se, const HullView& sp, int sub, AxisBest& best, bool* sep,
                                           double* d0, int* p0) {
